@@ -1,0 +1,582 @@
+// fia_advect.cu -- the flux-interpolated advection pass on the GPU.
+//
+// One pass of the reference (advect_density_flux_advection_3D_std_thread,
+// move_substances_3d.cpp:585-841, and its velocity counterpart
+// advect_velocity_flux_advection_3d.cpp:252-576) becomes four kernels:
+//
+//   k_psi        one thread per (x,z) column: psi = running y-integral of the field
+//                (calc_psi_3D.cpp:10-308, :311-537)
+//   k_backtrace  one thread per UNIQUE cell vertex: x' = x - dt u(x), pin rule, clamp
+//                (calc_backtraced_face_3D.cpp:9-160).  The reference backtraces every
+//                vertex once per face that uses it (up to 24 times).
+//   k_faces      one thread per UNIQUE face: clip the backtraced face in (xi,eta) space
+//                at the integer iso-lines of its vertex colours (facecutter.h:59-324,
+//                split_face_3D.cpp:17-93), and for every piece evaluate the quadrature
+//                of polygon_3D.cpp:257-487 with WENO6 / linear interpolation; the face
+//                flux is accumulated in registers.  The reference computes each interior
+//                face twice (once per adjacent cell, with reversed vertex order); the two
+//                computations produce the same pieces with opposite normals, so one
+//                signed flux per face is exact.
+//   k_gather     one thread per cell: rho' = (sum of the six signed face fluxes) / V.
+//                Deterministic, no atomics (the reference's per-thread += is racy).
+#include "fia_advect.cuh"
+
+#include <cmath>
+#include <vector>
+#include <algorithm>
+
+namespace fia {
+
+// ------------------------------------------------------------------------------------
+// host helpers
+// ------------------------------------------------------------------------------------
+static void legendre(int n, double x, double* p, double* dp) {
+    double p0 = 1.0, p1 = x;
+    for (int m = 2; m <= n; ++m) {
+        double p2 = ((2.0 * m - 1.0) * x * p1 - (m - 1.0) * p0) / m;
+        p0 = p1; p1 = p2;
+    }
+    if (n == 0) { *p = 1.0; *dp = 0.0; return; }
+    *p = p1;
+    *dp = n * (x * p1 - p0) / (x * x - 1.0);
+}
+
+// Gauss-Legendre rule on [-1,1]: Newton iteration on P_k from Chebyshev-like starting
+// points; nodes ordered centre first then -/+ pairs by increasing |x| (the order of
+// gauss_quadrature_points.cpp:18-60); weights normalised to sum 1.
+void make_gauss(int k, double* x, double* w) {
+    std::vector<std::pair<double, double>> nodes;
+    const double pi = 3.14159265358979323846;
+    for (int i = 0; i < (k + 1) / 2; ++i) {
+        double z = std::cos(pi * (i + 0.75) / (k + 0.5));
+        for (int it = 0; it < 100; ++it) {
+            double p, dp; legendre(k, z, &p, &dp);
+            double dz = p / dp; z -= dz;
+            if (std::fabs(dz) < 1e-17) break;
+        }
+        double p, dp; legendre(k, z, &p, &dp);
+        double wt = 2.0 / ((1.0 - z * z) * dp * dp);
+        if (std::fabs(z) < 1e-15) nodes.push_back({0.0, wt});
+        else { nodes.push_back({-std::fabs(z), wt}); nodes.push_back({std::fabs(z), wt}); }
+    }
+    std::stable_sort(nodes.begin(), nodes.end(),
+                     [](const std::pair<double, double>& a, const std::pair<double, double>& b) {
+                         return std::fabs(a.first) < std::fabs(b.first);
+                     });
+    for (int i = 0; i < k; ++i) { x[i] = nodes[i].first; w[i] = nodes[i].second / 2.0; }
+}
+
+NodeField cell_field(const int* N, int comp) {
+    NodeField F;
+    F.Mx = N[0] + (comp == 0); F.My = N[1] + (comp == 1); F.Mz = N[2] + (comp == 2);
+    F.ox = comp == 0 ? 0.0 : 0.5; F.oy = comp == 1 ? 0.0 : 0.5; F.oz = comp == 2 ? 0.0 : 0.5;
+    return F;
+}
+
+NodeField psi_field(const NodeField& A) {
+    NodeField P = A;
+    P.My = A.My + 1;
+    P.oy = A.oy - 0.5;
+    return P;
+}
+
+// ------------------------------------------------------------------------------------
+// psi: one thread per column (i,k); psi(.,0,.) = 0, psi(.,j,.) = psi(.,j-1,.) + incr(j-1)
+// ------------------------------------------------------------------------------------
+template <typename T>
+__global__ void k_psi(PassDesc d, const T* __restrict__ a, T* __restrict__ psi) {
+    const int Mx = d.A.Mx, My = d.A.My, Mz = d.A.Mz;
+    const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= (long long)Mx * Mz) return;
+    const int i = (int)(col / Mz), k = (int)(col % Mz);
+    const T h = T(d.h);
+    const T px = (T(i) + T(d.A.ox)) * h, pz = (T(k) + T(d.A.oz)) * h;
+    T acc = T(0);
+    psi[idx3(d.P, i, 0, k)] = T(0);
+    for (int j = 1; j <= My; ++j) {
+        if (d.psi_mode == PSI_PLAIN) {
+            acc = acc + ldg(a + idx3(d.A, i, j - 1, k)) * h;
+        } else if (d.psi_mode == PSI_WENO6) {
+            // cell j-1 spans [(j-1+oy-.5)h, (j+oy-.5)h]; k Gauss points per half
+            const T ylo = (T(j) - T(1.0) + T(d.A.oy) - T(0.5)) * h;
+            const T ymid = (T(j) - T(0.5) + T(d.A.oy) - T(0.5)) * h;
+            const T yhi = (T(j) + T(d.A.oy) - T(0.5)) * h;
+            for (int half = 0; half < 2; ++half) {
+                const T lo = half ? ymid : ylo, hi = half ? yhi : ymid;
+                const T L = hi - lo;
+                for (int q = 0; q < d.k; ++q) {
+                    const T py = (L / T(2)) * T(d.gx[q]) + (L / T(2)) + lo;
+                    acc += weno6_1dy(a, d.A, h, px, py, pz) * (h / T(2)) * T(d.gw[q]);
+                }
+            }
+        } else {
+            const T y0 = ((T(j - 1) + T(0.25)) + T(d.A.oy) - T(0.5)) * h;
+            const T y1 = ((T(j - 1) + T(0.75)) + T(d.A.oy) - T(0.5)) * h;
+            const T a0 = lin3d(a, d.A, h, px, y0, pz), a1 = lin3d(a, d.A, h, px, y1, pz);
+            acc = acc + a0 * (h / T(2)) + a1 * (h / T(2));
+        }
+        psi[idx3(d.P, i, j, k)] = acc;
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// vertex positions
+// ------------------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void vertex_rest_position(const PassDesc& d, int i, int j, int k, T* p) {
+    const T h = T(d.h);
+    p[0] = T(i) * h; p[1] = T(j) * h; p[2] = T(k) * h;
+    if (d.comp >= 0) p[d.comp] -= T(1) * T(0.5) * h;
+}
+
+template <typename T>
+__global__ void k_backtrace(PassDesc d, const T* __restrict__ u, const T* __restrict__ v,
+                            const T* __restrict__ w, NodeField fu, NodeField fv, NodeField fw,
+                            T* __restrict__ verts) {
+    const int Lx = d.A.Mx + 1, Ly = d.A.My + 1, Lz = d.A.Mz + 1;
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= (long long)Lx * Ly * Lz) return;
+    const int k = (int)(id % Lz);
+    const int j = (int)((id / Lz) % Ly);
+    const int i = (int)(id / ((long long)Lz * Ly));
+    const T h = T(d.h);
+    T p[3];
+    vertex_rest_position(d, i, j, k, p);
+    bool pinned = false;
+    if (d.comp >= 0) {
+        const int vi = d.comp == 0 ? i : (d.comp == 1 ? j : k);
+        pinned = (vi <= 1 || vi >= d.N[d.comp]);
+    }
+    if (!pinned) {
+        const T vx = interp(d.interp, u, fu, h, p[0], p[1], p[2]);
+        const T vy = interp(d.interp, v, fv, h, p[0], p[1], p[2]);
+        const T vz = interp(d.interp, w, fw, h, p[0], p[1], p[2]);
+        const T dt = T(d.dt);
+        p[0] -= vx * dt; p[1] -= vy * dt; p[2] -= vz * dt;
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const int e = (c == d.comp);
+        const T lo = T(0) - T(e) * T(0.5) * h;
+        const T hi = T(0) + h * T(d.N[c]) + T(e) * T(0.5) * h;
+        if (p[c] < lo) p[c] = lo;
+        if (p[c] > hi) p[c] = hi;
+    }
+    verts[3 * id + 0] = p[0]; verts[3 * id + 1] = p[1]; verts[3 * id + 2] = p[2];
+}
+
+// ------------------------------------------------------------------------------------
+// clipping in (xi, eta) space with an explicit stack
+// ------------------------------------------------------------------------------------
+template <typename T>
+struct CV { T p0, p1, c0, c1; };   // xi, eta, colour component 0, colour component 1
+
+constexpr int kPool = 144;     // vertex pool (LIFO) for pending pieces
+constexpr int kMaxVerts = 32;  // vertices per piece (MAX_TMP_POINTS of facecutter.h)
+constexpr int kMaxStack = 48;
+
+template <typename T> __device__ __forceinline__ T cv_c(const CV<T>& v, int dim) { return dim ? v.c1 : v.c0; }
+
+// Robust bilinear map: v0 + xi (v1-v0) + eta (v3-v0) + xi eta (v0-v1+v2-v3); exact for
+// faces lying in a grid plane (the form the oracle uses).
+template <typename T>
+__device__ __forceinline__ T bilin(const T* v, T xi, T eta) {
+    const T a = v[1] - v[0], b = v[3] - v[0], c = (v[0] - v[1]) + (v[2] - v[3]);
+    return v[0] + xi * a + eta * b + (xi * eta) * c;
+}
+
+template <typename T>
+struct FaceGeom {
+    T x[4], y[4], z[4];   // backtraced vertex coordinates in face order
+};
+
+// centroid and area of a polygon in (xi,eta) (facecutter.h:226-253)
+template <typename T>
+__device__ __forceinline__ void centroid(const T* px, const T* py, int num, T& cx, T& cy, T& area) {
+    T a = T(0), sx = T(0), sy = T(0);
+    for (int n = 0; n < num; ++n) {
+        const int m = (n + 1 == num) ? 0 : n + 1;
+        const T c = px[n] * py[m] - px[m] * py[n];
+        a += c;
+        sx += c * (px[n] + px[m]);
+        sy += c * (py[n] + py[m]);
+    }
+    a = fabs(T(0.5) * a);
+    if (a != T(0)) {
+        const T s = T(1.0) / (T(6.0) * a);
+        cx = sx * s; cy = sy * s;
+    } else {
+        sx = T(0); sy = T(0);
+        for (int n = 0; n < num; ++n) { sx = sx + px[n]; sy = sy + py[n]; }
+        const T s = T(1.0) / T(num);
+        cx = sx * s; cy = sy * s;
+    }
+    area = a;
+}
+
+// Accumulates the flux of one emitted piece (xi-eta polygon px/py with centroid c).
+template <typename T>
+__device__ __forceinline__ T piece_flux(const PassDesc& d, const FaceGeom<T>& g, const T* px, const T* py,
+                                        int num, T cxi, T ceta, const T* __restrict__ a,
+                                        const T* __restrict__ psi) {
+    const T h = T(d.h);
+    // 3D centroid and the y component of the scaled normal (split_face_3D.cpp:67-93)
+    const T cx = bilin(g.x, cxi, ceta), cy = bilin(g.y, cxi, ceta), cz = bilin(g.z, cxi, ceta);
+    T ny;
+    if (num == 3) {
+        const T ax = bilin(g.x, px[1], py[1]) - bilin(g.x, px[0], py[0]);
+        const T az = bilin(g.z, px[1], py[1]) - bilin(g.z, px[0], py[0]);
+        const T bx = bilin(g.x, px[2], py[2]) - bilin(g.x, px[0], py[0]);
+        const T bz = bilin(g.z, px[2], py[2]) - bilin(g.z, px[0], py[0]);
+        ny = T(0.5) * (az * bx - ax * bz);
+    } else {
+        T acc = T(0);
+        T x0 = bilin(g.x, px[0], py[0]) - cx, z0 = bilin(g.z, px[0], py[0]) - cz;
+        const T xs = x0, zs = z0;
+        for (int n = 0; n < num; ++n) {
+            T x1, z1;
+            if (n + 1 == num) { x1 = xs; z1 = zs; }
+            else { x1 = bilin(g.x, px[n + 1], py[n + 1]) - cx; z1 = bilin(g.z, px[n + 1], py[n + 1]) - cz; }
+            acc += z0 * x1 - x0 * z1;
+            x0 = x1; z0 = z1;
+        }
+        ny = acc * T(0.5);
+    }
+    if (ny == T(0)) return T(0);
+    T F = T(0);
+    if (d.use_integral) {
+        // polygon_3D.cpp:257-487 with the grid origin shifted by -h/2 along a staggered axis
+        const T oy = (d.comp == 1) ? T(-1) * T(0.5) * h : T(0);
+        const int iy0 = (int)floor((cy - oy) / h);
+        const T f = ((cy - oy) / h) - T(iy0);
+        if (f < T(0.5)) {
+            const T lo = T(iy0) * h + oy, L = cy - lo;
+            for (int q = 0; q < d.k; ++q) {
+                const T yq = (L / T(2)) * T(d.gx[q]) + (L / T(2)) + lo;
+                F += interp(d.interp, a, d.A, h, cx, yq, cz) * (ny * f * h * T(d.gw[q]));
+            }
+        } else {
+            T lo = T(iy0) * h + oy, hi = (T(iy0) + T(0.5)) * h + oy, L = hi - lo;
+            for (int q = 0; q < d.k; ++q) {
+                const T yq = (L / T(2)) * T(d.gx[q]) + (L / T(2)) + lo;
+                F += interp(d.interp, a, d.A, h, cx, yq, cz) * (ny * T(0.5) * h * T(d.gw[q]));
+            }
+            lo = (T(iy0) + T(0.5)) * h + oy; hi = (T(iy0) + f) * h + oy; L = hi - lo;
+            for (int q = 0; q < d.k; ++q) {
+                const T yq = (L / T(2)) * T(d.gx[q]) + (L / T(2)) + lo;
+                F += interp(d.interp, a, d.A, h, cx, yq, cz) * (ny * (f - T(0.5)) * h * T(d.gw[q]));
+            }
+        }
+        F += interp(d.interp, psi, d.P, h, cx, T(iy0) * h + oy, cz) * ny;
+    } else {
+        F += interp(d.interp, psi, d.P, h, cx, cy, cz) * ny;
+    }
+    return F;
+}
+
+// Emits a polygon (optionally triangulated to minimal_area, facecutter.h:255-324).
+template <typename T>
+__device__ T emit_polygon(const PassDesc& d, const FaceGeom<T>& g, const T* px, const T* py, int num,
+                          const T* __restrict__ a, const T* __restrict__ psi, unsigned& st, int& npieces) {
+    T cx, cy, area;
+    centroid(px, py, num, cx, cy, area);
+    const T minA = T(d.minimal_area);
+    if (!(area > minA)) {
+        if (area != T(0)) { ++npieces; return piece_flux(d, g, px, py, num, cx, cy, a, psi); }
+        return T(0);
+    }
+    // triangulate: fan from the centroid (num > 3) then recursive longest-edge bisection
+    T F = T(0);
+    T tri[24][6];
+    int top = 0;
+    if (num == 3) {
+        tri[top][0] = px[0]; tri[top][1] = py[0]; tri[top][2] = px[1]; tri[top][3] = py[1];
+        tri[top][4] = px[2]; tri[top][5] = py[2]; ++top;
+    } else {
+        for (int n = num - 1; n >= 0; --n) {
+            const int m = (n + 1 == num) ? 0 : n + 1;
+            if (top >= 24) { st |= ST_SUBDIV_OVERFLOW; return F; }
+            tri[top][0] = cx; tri[top][1] = cy; tri[top][2] = px[n]; tri[top][3] = py[n];
+            tri[top][4] = px[m]; tri[top][5] = py[m]; ++top;
+        }
+    }
+    while (top > 0) {
+        --top;
+        T tx[3] = {tri[top][0], tri[top][2], tri[top][4]};
+        T ty[3] = {tri[top][1], tri[top][3], tri[top][5]};
+        T tcx, tcy, tarea;
+        centroid(tx, ty, 3, tcx, tcy, tarea);
+        if (tarea > minA) {
+            int mi = 0; T ml = T(-1);
+            for (int n = 0; n < 3; ++n) {
+                const int m = (n + 1) % 3;
+                const T len = (tx[n] - tx[m]) * (tx[n] - tx[m]) + (ty[n] - ty[m]) * (ty[n] - ty[m]);
+                if (ml < len) { ml = len; mi = n; }
+            }
+            const int i1 = (mi + 1) % 3, i2 = (mi + 2) % 3;
+            const T mx = T(0.5) * (tx[mi] + tx[i1]), my = T(0.5) * (ty[mi] + ty[i1]);
+            if (top + 2 > 24) { st |= ST_SUBDIV_OVERFLOW; return F; }
+            // push second half first so the first half is processed first
+            tri[top][0] = mx; tri[top][1] = my; tri[top][2] = tx[i1]; tri[top][3] = ty[i1];
+            tri[top][4] = tx[i2]; tri[top][5] = ty[i2]; ++top;
+            tri[top][0] = tx[mi]; tri[top][1] = ty[mi]; tri[top][2] = mx; tri[top][3] = my;
+            tri[top][4] = tx[i2]; tri[top][5] = ty[i2]; ++top;
+        } else if (tarea != T(0)) {
+            ++npieces;
+            F += piece_flux(d, g, tx, ty, 3, tcx, tcy, a, psi);
+        }
+    }
+    return F;
+}
+
+// Clips one face and returns its flux (sum over pieces of the quadrature terms).
+template <typename T>
+__device__ T clip_face(const PassDesc& d, const FaceGeom<T>& g, const T* __restrict__ a,
+                       const T* __restrict__ psi, unsigned& st, int& npieces) {
+    const T h = T(d.h);
+    CV<T> pool[kPool];
+    unsigned char sstart[kMaxStack], snum[kMaxStack], sdim[kMaxStack];
+    int sp = 0, top = 4;
+    const T xi[4] = {T(0), T(1), T(1), T(0)}, eta[4] = {T(0), T(0), T(1), T(1)};
+    for (int q = 0; q < 4; ++q) {
+        pool[q].p0 = xi[q]; pool[q].p1 = eta[q];
+        pool[q].c0 = g.x[q] / h - T(d.color_off[0]);
+        pool[q].c1 = g.z[q] / h - T(d.color_off[1]);
+    }
+    sstart[0] = 0; snum[0] = 4; sdim[0] = 0; sp = 1;
+    T F = T(0);
+    CV<T> tmp0[kMaxVerts + 2];
+    while (sp > 0) {
+        --sp;
+        const int pstart = sstart[sp], num = snum[sp], dim = sdim[sp];
+        const CV<T>* poly = pool + pstart;
+        T mn = cv_c(poly[0], dim), mx = mn;
+        for (int n = 1; n < num; ++n) { const T c = cv_c(poly[n], dim); mn = fmin(mn, c); mx = fmax(mx, c); }
+        int start = (int)ceil(mn), end = (int)floor(mx);
+        if (mn - T(start) == T(0)) start += 1;
+        if (mx - T(end) == T(0)) end -= 1;
+        bool cut = false;
+        if (start <= end) {
+            if (pstart + 3 * num + 2 > kPool) { st |= ST_CLIP_OVERFLOW; top = pstart; continue; }
+            const T iso = T(start);
+            int h0 = 0, h1 = 0, slot = 0;
+            int wpos = pstart + num;          // pieces on the far side are written here
+            int p1start = wpos;
+            int nchild = 0;
+            unsigned char cst[kMaxStack], cnum[kMaxStack];
+            tmp0[h0++] = poly[0];
+            bool bad = false;
+            for (int n = 0; n < num && !bad; ++n) {
+                const int m = (n + 1 == num) ? 0 : n + 1;
+                const T v0 = cv_c(poly[n], dim) - iso, v1 = cv_c(poly[m], dim) - iso;
+                if ((v0 < T(0)) != (v1 < T(0))) {
+                    const T inv = T(1.0) / (v1 - v0);
+                    const T t0 = v1 * inv, t1 = -v0 * inv;
+                    cut = true;
+                    CV<T> X;
+                    X.p0 = t0 * poly[n].p0 + t1 * poly[m].p0;
+                    X.p1 = t0 * poly[n].p1 + t1 * poly[m].p1;
+                    const T other = t0 * cv_c(poly[n], 1 - dim) + t1 * cv_c(poly[m], 1 - dim);
+                    if (dim == 0) { X.c0 = iso; X.c1 = other; } else { X.c1 = iso; X.c0 = other; }
+                    if (slot == 0) {
+                        tmp0[h0++] = X;
+                        slot = 1; h1 = 0; p1start = wpos;
+                        if (t1 < T(1.0)) pool[p1start + h1++] = X;
+                    } else {
+                        pool[p1start + h1++] = X;
+                        if (nchild >= kMaxStack - 1) { bad = true; break; }
+                        cst[nchild] = (unsigned char)p1start; cnum[nchild] = (unsigned char)h1; ++nchild;
+                        wpos = p1start + h1;
+                        slot = 0;
+                        if (t1 < T(1.0)) tmp0[h0++] = X;
+                    }
+                }
+                if (n < num - 1) {
+                    if (slot == 0) tmp0[h0++] = poly[m];
+                    else pool[p1start + h1++] = poly[m];
+                }
+                if (h0 >= kMaxVerts || h1 >= kMaxVerts || p1start + h1 + 2 >= kPool) bad = true;
+            }
+            if (bad) { st |= ST_CLIP_OVERFLOW; top = pstart; continue; }
+            if (cut) {
+                if (slot != 0) { st |= ST_CLIP_ODD_CUT; top = pstart; continue; }
+                if (wpos + h0 >= kPool || sp + nchild + 1 > kMaxStack) { st |= ST_CLIP_OVERFLOW; top = pstart; continue; }
+                // piece 0 goes after the far-side pieces; then the block moves down over the parent
+                for (int q = 0; q < h0; ++q) pool[wpos + q] = tmp0[q];
+                const int src = pstart + num, len = wpos + h0 - src;
+                for (int q = 0; q < len; ++q) pool[pstart + q] = pool[src + q];
+                for (int c = 0; c < nchild; ++c) {
+                    sstart[sp] = (unsigned char)(cst[c] - num); snum[sp] = cnum[c]; sdim[sp] = (unsigned char)dim; ++sp;
+                }
+                sstart[sp] = (unsigned char)(wpos - num); snum[sp] = (unsigned char)h0; sdim[sp] = (unsigned char)dim; ++sp;
+                top = pstart + len;
+            }
+        }
+        if (!cut) {
+            if (dim == 0) {
+                sstart[sp] = (unsigned char)pstart; snum[sp] = (unsigned char)num; sdim[sp] = 1; ++sp;
+                top = pstart + num;
+            } else {
+                if (num >= 3) {
+                    T px[kMaxVerts], py[kMaxVerts];
+                    for (int q = 0; q < num; ++q) { px[q] = poly[q].p0; py[q] = poly[q].p1; }
+                    F += emit_polygon(d, g, px, py, num, a, psi, st, npieces);
+                }
+                top = pstart;
+            }
+        }
+    }
+    (void)top;
+    return F;
+}
+
+// Face families: 0 = faces normal to x, 1 = normal to y, 2 = normal to z, in the vertex
+// order of the face as seen from the lower cell (faces 1, 2, 5 of
+// backtrace_..._for_integrate_density.cpp:83-112).
+__device__ __forceinline__ void face_corners(int fam, int i, int j, int k, int* ci, int* cj, int* ck) {
+    if (fam == 0) {
+        ci[0] = i; cj[0] = j;     ck[0] = k;
+        ci[1] = i; cj[1] = j + 1; ck[1] = k;
+        ci[2] = i; cj[2] = j + 1; ck[2] = k + 1;
+        ci[3] = i; cj[3] = j;     ck[3] = k + 1;
+    } else if (fam == 1) {
+        ci[0] = i;     cj[0] = j; ck[0] = k;
+        ci[1] = i;     cj[1] = j; ck[1] = k + 1;
+        ci[2] = i + 1; cj[2] = j; ck[2] = k + 1;
+        ci[3] = i + 1; cj[3] = j; ck[3] = k;
+    } else {
+        ci[0] = i;     cj[0] = j;     ck[0] = k;
+        ci[1] = i + 1; cj[1] = j;     ck[1] = k;
+        ci[2] = i + 1; cj[2] = j + 1; ck[2] = k;
+        ci[3] = i;     cj[3] = j + 1; ck[3] = k;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_faces(PassDesc d, int fam, const T* __restrict__ a,
+                                               const T* __restrict__ psi, const T* __restrict__ verts,
+                                               T* __restrict__ flux, unsigned* status,
+                                               unsigned long long* counters) {
+    const int Fx = d.A.Mx + (fam == 0), Fy = d.A.My + (fam == 1), Fz = d.A.Mz + (fam == 2);
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long nface = (long long)Fx * Fy * Fz;
+    unsigned st = 0;
+    int npieces = 0;
+    if (id < nface) {
+        const int k = (int)(id % Fz);
+        const int j = (int)((id / Fz) % Fy);
+        const int i = (int)(id / ((long long)Fz * Fy));
+        int ci[4], cj[4], ck[4];
+        face_corners(fam, i, j, k, ci, cj, ck);
+        FaceGeom<T> g;
+        const int Ly = d.A.My + 1, Lz = d.A.Mz + 1;
+        for (int q = 0; q < 4; ++q) {
+            if (d.zero_velocity) {
+                T p[3];
+                vertex_rest_position(d, ci[q], cj[q], ck[q], p);
+                g.x[q] = p[0]; g.y[q] = p[1]; g.z[q] = p[2];
+            } else {
+                const long long vid = ((long long)ci[q] * Ly + cj[q]) * Lz + ck[q];
+                g.x[q] = verts[3 * vid]; g.y[q] = verts[3 * vid + 1]; g.z[q] = verts[3 * vid + 2];
+            }
+        }
+        T F = clip_face(d, g, a, psi, st, npieces);
+        if (!isfinite(F)) st |= ST_NONFINITE;
+        flux[id] = F;
+    }
+    // warp-aggregated counters and status
+    unsigned long long pc = (unsigned long long)npieces;
+    unsigned fc = id < nface ? 1u : 0u;
+    for (int o = 16; o > 0; o >>= 1) {
+        pc += __shfl_down_sync(0xffffffffu, pc, o);
+        fc += __shfl_down_sync(0xffffffffu, fc, o);
+        st |= __shfl_down_sync(0xffffffffu, st, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (fc) { atomicAdd(&counters[0], (unsigned long long)fc); atomicAdd(&counters[1], pc); }
+        if (st) atomicOr(status, st);
+    }
+}
+
+// rho'(i,j,k) = (Fx(i+1)-Fx(i) + Fy(j+1)-Fy(j) + Fz(k+1)-Fz(k)) / V
+template <typename T>
+__global__ void k_gather(PassDesc d, const T* __restrict__ fx, const T* __restrict__ fy,
+                         const T* __restrict__ fz, const T* __restrict__ in, T* __restrict__ out, int mode) {
+    const int Mx = d.A.Mx, My = d.A.My, Mz = d.A.Mz;
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= (long long)Mx * My * Mz) return;
+    const int k = (int)(id % Mz);
+    const int j = (int)((id / Mz) % My);
+    const int i = (int)(id / ((long long)Mz * My));
+    const T h = T(d.h);
+    const T V = h * h * h;
+    const long long ix0 = ((long long)i * My + j) * Mz + k;             // (Mx+1) x My x Mz
+    const long long ix1 = ((long long)(i + 1) * My + j) * Mz + k;
+    const long long iy0 = ((long long)i * (My + 1) + j) * Mz + k;       // Mx x (My+1) x Mz
+    const long long iy1 = ((long long)i * (My + 1) + j + 1) * Mz + k;
+    const long long iz0 = ((long long)i * My + j) * (Mz + 1) + k;       // Mx x My x (Mz+1)
+    const T s = ((fx[ix1] - fx[ix0]) + (fy[iy1] - fy[iy0])) + (fz[iz0 + 1] - fz[iz0]);
+    const T val = s / V;
+    if (mode == 0) out[id] = val;
+    else if (mode == 1) out[id] = in[id] - val;
+    else out[id] = out[id] + val;
+}
+
+// ------------------------------------------------------------------------------------
+// launchers
+// ------------------------------------------------------------------------------------
+static inline unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+template <typename T>
+cudaError_t launch_psi(const PassDesc& d, const T* a, T* psi, cudaStream_t s) {
+    const long long cols = (long long)d.A.Mx * d.A.Mz;
+    k_psi<T><<<blocks_for(cols, 128), 128, 0, s>>>(d, a, psi);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_backtrace(const PassDesc& d, const VelocityFields& vel, T* verts, cudaStream_t s) {
+    const long long n = (long long)(d.A.Mx + 1) * (d.A.My + 1) * (d.A.Mz + 1);
+    k_backtrace<T><<<blocks_for(n, 128), 128, 0, s>>>(d, (const T*)vel.u, (const T*)vel.v, (const T*)vel.w,
+                                                      vel.fu, vel.fv, vel.fw, verts);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_faces(const PassDesc& d, const T* a, const PassWork<T>& w, cudaStream_t s) {
+    for (int fam = 0; fam < 3; ++fam) {
+        const long long n = (long long)(d.A.Mx + (fam == 0)) * (d.A.My + (fam == 1)) * (d.A.Mz + (fam == 2));
+        k_faces<T><<<blocks_for(n, 128), 128, 0, s>>>(d, fam, a, w.psi, w.verts, w.flux[fam], w.status, w.counters);
+    }
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_gather(const PassDesc& d, const PassWork<T>& w, const T* in, T* out, int mode, cudaStream_t s) {
+    const long long n = (long long)d.A.Mx * d.A.My * d.A.Mz;
+    k_gather<T><<<blocks_for(n, 256), 256, 0, s>>>(d, w.flux[0], w.flux[1], w.flux[2], in, out, mode);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t run_pass(const PassDesc& d, const VelocityFields& vel, const T* a, const PassWork<T>& w,
+                     const T* in, T* out, int mode, cudaStream_t s) {
+    cudaError_t e = launch_psi<T>(d, a, w.psi, s);
+    if (e != cudaSuccess) return e;
+    if (!d.zero_velocity) {
+        e = launch_backtrace<T>(d, vel, w.verts, s);
+        if (e != cudaSuccess) return e;
+    }
+    e = launch_faces<T>(d, a, w, s);
+    if (e != cudaSuccess) return e;
+    return launch_gather<T>(d, w, in, out, mode, s);
+}
+
+template cudaError_t launch_psi<double>(const PassDesc&, const double*, double*, cudaStream_t);
+template cudaError_t launch_backtrace<double>(const PassDesc&, const VelocityFields&, double*, cudaStream_t);
+template cudaError_t launch_faces<double>(const PassDesc&, const double*, const PassWork<double>&, cudaStream_t);
+template cudaError_t launch_gather<double>(const PassDesc&, const PassWork<double>&, const double*, double*, int, cudaStream_t);
+template cudaError_t run_pass<double>(const PassDesc&, const VelocityFields&, const double*, const PassWork<double>&,
+                                      const double*, double*, int, cudaStream_t);
+
+}  // namespace fia

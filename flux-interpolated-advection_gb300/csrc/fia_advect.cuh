@@ -1,0 +1,74 @@
+// fia_advect.cuh -- host-side description of one flux-advection pass and the launchers.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "fia_device.cuh"
+
+namespace fia {
+
+constexpr int kMaxGauss = 15;
+
+// Everything one flux pass needs; passed to the kernels by value.
+struct PassDesc {
+    NodeField A;            // advected node field (its cells are the control volumes)
+    NodeField P;            // psi of A (y-faces of A's cells)
+    int N[3];               // base grid (cells of the density)
+    int comp;               // -1 density, 0/1/2 velocity component: staggering + pin rule
+    int interp;             // Interp for the backtrace velocity, the values and psi
+    int psi_mode;           // PSI_PLAIN / PSI_WENO6 / PSI_LINEAR
+    int use_integral;       // 1: y-integral quadrature per piece (polygon_3D.cpp:257-487)
+    int zero_velocity;      // 1: faces are not moved (zero-velocity pass)
+    double color_off[2];    // split method: colour = x/h - off0, z/h - off1
+    int k;                  // Gauss points per half cell
+    double gx[kMaxGauss];   // Gauss nodes on [-1,1] (centre first, then -/+ pairs)
+    double gw[kMaxGauss];   // weights normalised to sum 1
+    double minimal_area;    // xi-eta area above which pieces are triangulated
+    double dt, h;
+};
+
+enum PsiMode : int { PSI_PLAIN = 0, PSI_WENO6 = 1, PSI_LINEAR = 2 };
+
+// Status bits (OR-ed into the device status word).
+enum StatusBits : unsigned {
+    ST_CLIP_OVERFLOW = 1u,      // a piece exceeded 32 vertices or the clip pool
+    ST_CLIP_ODD_CUT = 2u,       // odd number of iso-line crossings (facecutter.h:191-204)
+    ST_NONFINITE = 4u,          // a non-finite flux was produced
+    ST_SUBDIV_OVERFLOW = 8u,    // triangle subdivision stack exhausted
+};
+
+// Workspace owned by the caller (device pointers).
+template <typename T>
+struct PassWork {
+    T* psi;            // P.Mx*P.My*P.Mz
+    T* verts;          // 3 * (A.Mx+1)(A.My+1)(A.Mz+1)  backtraced vertex positions
+    T* flux[3];        // per face family: (Mx+1)MyMz, Mx(My+1)Mz, MxMy(Mz+1)
+    unsigned* status;  // one word
+    unsigned long long* counters;  // [0] faces visited, [1] pieces emitted
+};
+
+struct VelocityFields {
+    const void* u; const void* v; const void* w;   // T* on the device
+    NodeField fu, fv, fw;
+};
+
+void make_gauss(int k, double* x, double* w);
+NodeField cell_field(const int* N, int comp);
+NodeField psi_field(const NodeField& A);
+
+// Launchers (one CUDA stream); all return cudaError_t of the launches.
+template <typename T>
+cudaError_t launch_psi(const PassDesc& d, const T* a, T* psi, cudaStream_t s);
+template <typename T>
+cudaError_t launch_backtrace(const PassDesc& d, const VelocityFields& vel, T* verts, cudaStream_t s);
+template <typename T>
+cudaError_t launch_faces(const PassDesc& d, const T* a, const PassWork<T>& w, cudaStream_t s);
+// mode 0: out = div F / V; 1: out = in - div F / V; 2: out += div F / V
+template <typename T>
+cudaError_t launch_gather(const PassDesc& d, const PassWork<T>& w, const T* in, T* out, int mode, cudaStream_t s);
+
+// One complete pass: psi, backtrace (unless zero velocity), faces, gather.
+template <typename T>
+cudaError_t run_pass(const PassDesc& d, const VelocityFields& vel, const T* a, const PassWork<T>& w,
+                     const T* in, T* out, int mode, cudaStream_t s);
+
+}  // namespace fia

@@ -1,0 +1,596 @@
+// fia_api.cu -- the C ABI of include/fia.h: device-resident Grid_3D session and the
+// orchestration of the reference's entry points on one CUDA stream.
+#include "../../include/fia.h"
+#include "fia_advect.cuh"
+#include "fia_pressure.cuh"
+
+#include <cstdio>
+#include <cstring>
+#include <cmath>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+using namespace fia;
+
+struct fia_session {
+    int N[3];
+    double h;
+    int precision;
+    size_t es;                   // element size on the device
+    cudaStream_t stream;
+    int last_status;
+    bool status_pending;
+    bool counters_pending;
+    unsigned long long counters_host[2];
+    double wall_loss[3];
+    // device buffers
+    void* rho; void* rho_next; void* pres;
+    void* vel[3]; void* vel_next[3];
+    void* cbuf;                  // correction field (pass 2 result)
+    void* psi; void* verts; void* flux[3];
+    void* pw[5];                 // pressure work vectors r z d q (+ spare)
+    double* part; double* scal; double* sums;
+    unsigned* status; unsigned long long* counters;
+    double* red_part; double* red_out;
+    std::vector<void*> allocations;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int set_cuda_error(cudaError_t e, const char* where) {
+    g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
+    return FIA_ERR_CUDA;
+}
+#define CK(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return set_cuda_error(e_, #call); } while (0)
+
+long long field_count(const fia_session* s, int field) {
+    const long long nx = s->N[0], ny = s->N[1], nz = s->N[2];
+    switch (field) {
+        case FIA_FIELD_DENSITY: case FIA_FIELD_PRESSURE: return nx * ny * nz;
+        case FIA_FIELD_U: return (nx + 1) * ny * nz;
+        case FIA_FIELD_V: return nx * (ny + 1) * nz;
+        case FIA_FIELD_W: return nx * ny * (nz + 1);
+        default: return -1;
+    }
+}
+
+void* field_ptr(fia_session* s, int field) {
+    switch (field) {
+        case FIA_FIELD_DENSITY: return s->rho;
+        case FIA_FIELD_PRESSURE: return s->pres;
+        case FIA_FIELD_U: return s->vel[0];
+        case FIA_FIELD_V: return s->vel[1];
+        case FIA_FIELD_W: return s->vel[2];
+        default: return nullptr;
+    }
+}
+
+// element-type conversion on the device
+template <typename D, typename S>
+__global__ void k_convert(const S* __restrict__ src, D* __restrict__ dst, long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = (D)src[i];
+}
+
+// FP64 sum (kind 0) or max |x| (kind 1) of n values: per-block partials then one block.
+template <typename T>
+__global__ void k_reduce_part(const T* __restrict__ a, long long n, int kind, double* part) {
+    double acc = 0.0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double x = (double)a[i];
+        acc = kind == 0 ? acc + x : fmax(acc, fabs(x));
+    }
+    __shared__ double sh[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        const double y = __shfl_down_sync(0xffffffffu, acc, o);
+        acc = kind == 0 ? acc + y : fmax(acc, y);
+    }
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        acc = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) {
+            const double y = __shfl_down_sync(0xffffffffu, acc, o);
+            acc = kind == 0 ? acc + y : fmax(acc, y);
+        }
+        if (threadIdx.x == 0) part[blockIdx.x] = acc;
+    }
+}
+
+__global__ void k_reduce_final(const double* part, int nb, int kind, double* out, int accumulate) {
+    double acc = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) acc = kind == 0 ? acc + part[b] : fmax(acc, part[b]);
+    __shared__ double sh[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        const double y = __shfl_down_sync(0xffffffffu, acc, o);
+        acc = kind == 0 ? acc + y : fmax(acc, y);
+    }
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = kind == 0 ? 0.0 : 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = kind == 0 ? t + sh[w] : fmax(t, sh[w]);
+        if (accumulate && kind == 1) t = fmax(t, *out);
+        else if (accumulate) t += *out;
+        *out = t;
+    }
+}
+
+constexpr int kRedBlocks = 512;
+
+template <typename T>
+cudaError_t reduce(fia_session* s, const void* a, long long n, int kind, bool accumulate) {
+    k_reduce_part<T><<<kRedBlocks, 256, 0, s->stream>>>((const T*)a, n, kind, s->red_part);
+    k_reduce_final<<<1, 256, 0, s->stream>>>(s->red_part, kRedBlocks, kind, s->red_out, accumulate ? 1 : 0);
+    return cudaGetLastError();
+}
+
+// Split offsets (colour = pos/h - off) per field for the main and the error-advection pass
+// (move_substances_3d.cpp:189; advect_velocity_flux_advection_3d.cpp:622-628, :721,
+// :805-810, :913, :999-1002, :1096).
+void split_offsets(int comp, int error_pass, int density_split, double* off) {
+    static const double tbl[4][2] = {{0.5, 0.5}, {0.0, 0.0}, {0.5, 0.0}, {0.0, 0.5}};
+    if (comp < 0) {
+        const int m = error_pass ? FIA_SPLIT_XZ_AXIS : density_split;
+        off[0] = tbl[m][0]; off[1] = tbl[m][1];
+        return;
+    }
+    const double main_x = comp == 0 ? 0.0 : 0.5, main_z = comp == 2 ? 0.0 : 0.5;
+    if (!error_pass) { off[0] = main_x; off[1] = main_z; }
+    else if (comp == 1) { off[0] = 0.0; off[1] = 0.0; }
+    else { off[0] = 0.5 - main_x; off[1] = 0.5 - main_z; }
+}
+
+int check_params(const fia_advect_params* p) {
+    if (!p) return FIA_ERR_INVALID;
+    if (p->use_MacCormack_scheme || p->enable_cell_volume_correction) return FIA_ERR_UNSUPPORTED;
+    if (p->interpolation_method != FIA_INTERP_WENO6 && p->interpolation_method != FIA_INTERP_LINEAR) return FIA_ERR_INVALID;
+    if (p->split_method < 0 || p->split_method > 3) return FIA_ERR_INVALID;
+    const int k = p->num_gauss_quadrature_point_for_integrate_density;
+    if (k < 1 || k > kMaxGauss || (k % 2) == 0) return FIA_ERR_INVALID;
+    if (!(p->minimal_area > 0.0)) return FIA_ERR_INVALID;
+    return FIA_OK;
+}
+
+PassDesc base_desc(const fia_session* s, int comp, double dt) {
+    PassDesc d;
+    std::memset(&d, 0, sizeof(d));
+    for (int c = 0; c < 3; ++c) d.N[c] = s->N[c];
+    d.comp = comp;
+    d.A = comp < 0 ? cell_field(s->N, -1) : cell_field(s->N, comp);
+    d.P = psi_field(d.A);
+    d.h = s->h;
+    d.dt = dt;
+    return d;
+}
+
+template <typename T>
+PassWork<T> work(fia_session* s) {
+    PassWork<T> w;
+    w.psi = (T*)s->psi; w.verts = (T*)s->verts;
+    for (int f = 0; f < 3; ++f) w.flux[f] = (T*)s->flux[f];
+    w.status = s->status; w.counters = s->counters;
+    return w;
+}
+
+VelocityFields velocity(fia_session* s, void* const* v) {
+    VelocityFields vel;
+    vel.u = v[0]; vel.v = v[1]; vel.w = v[2];
+    vel.fu = cell_field(s->N, 0); vel.fv = cell_field(s->N, 1); vel.fw = cell_field(s->N, 2);
+    return vel;
+}
+
+// One field through move_substances_3D's pass structure (move_substances_3d.cpp:58-226);
+// velocity components follow the same structure with their own split methods.
+template <typename T>
+cudaError_t advect_field(fia_session* s, int comp, const T* in, T* out, double dt, const fia_advect_params* p,
+                         void* const* vel_fields) {
+    PassDesc d = base_desc(s, comp, dt);
+    d.k = p->num_gauss_quadrature_point_for_integrate_density;
+    make_gauss(d.k, d.gx, d.gw);
+    d.minimal_area = p->minimal_area;
+    const VelocityFields vel = velocity(s, vel_fields);
+    const PassWork<T> w = work<T>(s);
+    // pass 1
+    d.interp = p->interpolation_method == FIA_INTERP_WENO6 ? INTERP_WENO6 : INTERP_LINEAR;
+    d.use_integral = p->use_integral ? 1 : 0;
+    d.psi_mode = p->use_integral ? (d.interp == INTERP_WENO6 ? PSI_WENO6 : PSI_LINEAR) : PSI_PLAIN;
+    d.zero_velocity = 0;
+    split_offsets(comp, 0, p->split_method, d.color_off);
+    cudaError_t e = run_pass<T>(d, vel, in, w, in, out, 0, s->stream);
+    if (e != cudaSuccess || !p->enable_eliminate_zero_velocity_false_diffusion) return e;
+    // pass 2: zero velocity, psi at the piece centroid, plain psi; c = in - A2(in)
+    T* c = (T*)s->cbuf;
+    d.zero_velocity = 1; d.use_integral = 0; d.psi_mode = PSI_PLAIN;
+    e = run_pass<T>(d, vel, in, w, in, c, 1, s->stream);
+    if (e != cudaSuccess) return e;
+    // pass 3: advect the error with 1Dy-linear interpolation and the error split
+    d.zero_velocity = 0; d.interp = INTERP_1DY_LINEAR;
+    split_offsets(comp, 1, p->split_method, d.color_off);
+    return run_pass<T>(d, vel, c, w, nullptr, out, 2, s->stream);
+}
+
+cudaError_t reset_counters(fia_session* s) {
+    cudaError_t e = cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->stream);
+    if (e != cudaSuccess) return e;
+    s->status_pending = true; s->counters_pending = true;
+    return cudaMemsetAsync(s->counters, 0, 2 * sizeof(unsigned long long), s->stream);
+}
+
+int finish_status(fia_session* s) {
+    if (!s->status_pending) return s->last_status;
+    unsigned st = 0;
+    if (cudaMemcpyAsync(&st, s->status, sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream) != cudaSuccess) return FIA_ERR_CUDA;
+    if (cudaStreamSynchronize(s->stream) != cudaSuccess) return FIA_ERR_CUDA;
+    s->status_pending = false;
+    s->last_status = (int)st;
+    return s->last_status;
+}
+
+template <typename T>
+int move_substances(fia_session* s, double dt, const fia_advect_params* p) {
+    CK(reset_counters(s));
+    CK(advect_field<T>(s, -1, (const T*)s->rho, (T*)s->rho_next, dt, p, s->vel));
+    std::swap(s->rho, s->rho_next);
+    return FIA_OK;
+}
+
+template <typename T>
+int advect_velocity(fia_session* s, double dt, const fia_advect_params* p) {
+    CK(reset_counters(s));
+    for (int c = 0; c < 3; ++c)
+        CK(advect_field<T>(s, c, (const T*)s->vel[c], (T*)s->vel_next[c], dt, p, s->vel));
+    for (int c = 0; c < 3; ++c) std::swap(s->vel[c], s->vel_next[c]);
+    return FIA_OK;
+}
+
+template <typename T>
+int pressure(fia_session* s, const fia_solver_params* sp, fia_solver_report* rep, bool subtract) {
+    fia_solver_params def;
+    fia_default_solver_params(&def);
+    if (!sp) sp = &def;
+    if (sp->method != FIA_SOLVER_PCG_JACOBI) return FIA_ERR_UNSUPPORTED;
+    PressureWork<T> W;
+    W.p = (T*)s->pres; W.r = (T*)s->pw[0]; W.z = (T*)s->pw[1]; W.d = (T*)s->pw[2]; W.q = (T*)s->pw[3];
+    W.part = s->part; W.scal = s->scal; W.sums = s->sums;
+    PressureReport r;
+    CK(pressure_solve<T>(W, s->N[0], s->N[1], s->N[2], s->h, (const T*)s->vel[0], (const T*)s->vel[1],
+                         (const T*)s->vel[2], sp->tol, sp->max_iter, &r, s->stream));
+    if (subtract) {
+        CK(subtract_gradient<T>((const T*)s->pres, (T*)s->vel[0], (T*)s->vel[1], (T*)s->vel[2], s->N[0], s->N[1],
+                                s->N[2], s->h, s->part, s->sums, s->stream));
+        double loss[3];
+        CK(cudaMemcpyAsync(loss, s->sums, 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        for (int c = 0; c < 3; ++c) s->wall_loss[c] += loss[c];
+    }
+    int status = r.status ? FIA_STATUS_SOLVER_CAP : 0;
+    if (rep) { rep->iterations = r.iterations; rep->rel_residual = r.rel_residual; rep->status = status; }
+    return status;
+}
+
+template <typename T>
+int debug_flux_pass(fia_session* s, int comp, const double* field, double dt, int interp, int psi_mode,
+                    int use_integral, int zero_velocity, const double* co, int k, double minimal_area, double* out) {
+    PassDesc d = base_desc(s, comp, dt);
+    d.k = k; make_gauss(k, d.gx, d.gw);
+    d.interp = interp; d.psi_mode = psi_mode; d.use_integral = use_integral; d.zero_velocity = zero_velocity;
+    d.color_off[0] = co[0]; d.color_off[1] = co[1]; d.minimal_area = minimal_area;
+    const long long n = (long long)d.A.Mx * d.A.My * d.A.Mz;
+    double* tmp = nullptr;
+    CK(cudaMallocAsync((void**)&tmp, n * sizeof(double), s->stream));
+    CK(cudaMemcpyAsync(tmp, field, n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    T* a = (T*)s->cbuf;
+    k_convert<T, double><<<256, 256, 0, s->stream>>>(tmp, a, n);
+    CK(reset_counters(s));
+    CK(run_pass<T>(d, velocity(s, s->vel), a, work<T>(s), a, (T*)s->rho_next, 0, s->stream));
+    k_convert<double, T><<<256, 256, 0, s->stream>>>((const T*)s->rho_next, tmp, n);
+    CK(cudaMemcpyAsync(out, tmp, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaFreeAsync(tmp, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return finish_status(s);
+}
+
+template <typename T>
+int debug_backtrace(fia_session* s, int comp, double dt, int interp, double* out) {
+    PassDesc d = base_desc(s, comp, dt);
+    d.interp = interp;
+    const long long n = 3LL * (d.A.Mx + 1) * (d.A.My + 1) * (d.A.Mz + 1);
+    CK(launch_backtrace<T>(d, velocity(s, s->vel), (T*)s->verts, s->stream));
+    double* tmp = nullptr;
+    CK(cudaMallocAsync((void**)&tmp, n * sizeof(double), s->stream));
+    k_convert<double, T><<<256, 256, 0, s->stream>>>((const T*)s->verts, tmp, n);
+    CK(cudaMemcpyAsync(out, tmp, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaFreeAsync(tmp, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FIA_OK;
+}
+
+template <typename T>
+int debug_psi(fia_session* s, int comp, const double* field, int mode, int k, double* out) {
+    PassDesc d = base_desc(s, comp, 0.0);
+    d.k = k; make_gauss(k, d.gx, d.gw); d.psi_mode = mode;
+    const long long n = (long long)d.A.Mx * d.A.My * d.A.Mz;
+    const long long np = (long long)d.P.Mx * d.P.My * d.P.Mz;
+    double* tmp = nullptr;
+    CK(cudaMallocAsync((void**)&tmp, np * sizeof(double), s->stream));
+    CK(cudaMemcpyAsync(tmp, field, n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    k_convert<T, double><<<256, 256, 0, s->stream>>>(tmp, (T*)s->cbuf, n);
+    CK(launch_psi<T>(d, (const T*)s->cbuf, (T*)s->psi, s->stream));
+    k_convert<double, T><<<256, 256, 0, s->stream>>>((const T*)s->psi, tmp, np);
+    CK(cudaMemcpyAsync(out, tmp, np * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaFreeAsync(tmp, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FIA_OK;
+}
+
+}  // namespace
+
+// =====================================================================================
+extern "C" {
+
+int fia_api_version(void) { return FIA_API_VERSION; }
+
+const char* fia_error_string(int code) {
+    switch (code) {
+        case FIA_OK: return "ok";
+        case FIA_ERR_INVALID: return "invalid argument";
+        case FIA_ERR_CUDA: return g_last_error.empty() ? "CUDA error" : g_last_error.c_str();
+        case FIA_ERR_UNSUPPORTED: return "unsupported option";
+        case FIA_ERR_NOMEM: return "device allocation failed";
+        default: return code > 0 ? "completed with numerical status bits set" : "unknown error";
+    }
+}
+
+void fia_default_advect_params(fia_advect_params* p) {
+    if (!p) return;
+    p->interpolation_method = FIA_INTERP_WENO6;
+    p->split_method = FIA_SPLIT_XZ_CELLFACE;
+    p->num_gauss_quadrature_point_for_integrate_density = 3;
+    p->use_integral = 1;
+    p->enable_eliminate_zero_velocity_false_diffusion = 1;
+    p->use_MacCormack_scheme = 0;
+    p->enable_cell_volume_correction = 0;
+    p->minimal_area = 1.0;
+}
+
+void fia_default_solver_params(fia_solver_params* p) {
+    if (!p) return;
+    p->tol = 1e-6;
+    p->max_iter = 10000;
+    p->method = FIA_SOLVER_PCG_JACOBI;
+}
+
+fia_session* fia_create(int nx, int ny, int nz, double cell_length, int precision) {
+    if (nx < 2 || ny < 2 || nz < 2 || !(cell_length > 0.0)) { g_last_error = "fia_create: bad grid"; return nullptr; }
+    if (precision != FIA_FP64) { g_last_error = "fia_create: precision not available"; return nullptr; }
+    if ((long long)(nx + 2) * (ny + 2) * (nz + 2) > (1LL << 31)) { g_last_error = "fia_create: grid too large"; return nullptr; }
+    fia_session* s = new fia_session();
+    std::memset(s->wall_loss, 0, sizeof(s->wall_loss));
+    s->N[0] = nx; s->N[1] = ny; s->N[2] = nz; s->h = cell_length; s->precision = precision;
+    s->es = precision == FIA_FP64 ? sizeof(double) : sizeof(float);
+    s->last_status = 0; s->status_pending = false; s->counters_pending = false;
+    s->counters_host[0] = s->counters_host[1] = 0;
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        g_last_error = "fia_create: stream"; delete s; return nullptr;
+    }
+    const long long big = (long long)(nx + 2) * (ny + 2) * (nz + 2);
+    auto alloc = [&](size_t bytes) -> void* {
+        void* p = nullptr;
+        if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+        cudaMemset(p, 0, bytes);
+        s->allocations.push_back(p);
+        return p;
+    };
+    bool ok = true;
+    auto A = [&](void*& dst, size_t bytes) { dst = alloc(bytes); ok = ok && dst != nullptr; };
+    const size_t fb = (size_t)big * s->es;
+    A(s->rho, fb); A(s->rho_next, fb); A(s->pres, fb); A(s->cbuf, fb); A(s->psi, fb);
+    for (int c = 0; c < 3; ++c) { A(s->vel[c], fb); A(s->vel_next[c], fb); A(s->flux[c], fb); }
+    A(s->verts, 3 * fb);
+    for (int q = 0; q < 4; ++q) A(s->pw[q], fb);
+    s->pw[4] = nullptr;
+    void* t;
+    A(t, pressure_partials() * sizeof(double)); s->part = (double*)t;
+    A(t, 8 * sizeof(double)); s->scal = (double*)t;
+    A(t, 8 * sizeof(double)); s->sums = (double*)t;
+    A(t, sizeof(unsigned)); s->status = (unsigned*)t;
+    A(t, 4 * sizeof(unsigned long long)); s->counters = (unsigned long long*)t;
+    A(t, kRedBlocks * sizeof(double)); s->red_part = (double*)t;
+    A(t, 4 * sizeof(double)); s->red_out = (double*)t;
+    if (!ok) {
+        g_last_error = "fia_create: device allocation failed";
+        fia_destroy(s);
+        return nullptr;
+    }
+    cudaDeviceSynchronize();
+    return s;
+}
+
+void fia_destroy(fia_session* s) {
+    if (!s) return;
+    cudaStreamSynchronize(s->stream);
+    for (void* p : s->allocations) cudaFree(p);
+    cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+int fia_last_status(const fia_session* s) {
+    if (!s) return FIA_ERR_INVALID;
+    return finish_status(const_cast<fia_session*>(s));
+}
+
+void* fia_stream(fia_session* s) { return s ? (void*)s->stream : nullptr; }
+
+int fia_synchronize(fia_session* s) {
+    if (!s) return FIA_ERR_INVALID;
+    CK(cudaStreamSynchronize(s->stream));
+    return FIA_OK;
+}
+
+int fia_set_field(fia_session* s, int field, const void* host, int host_dtype) {
+    if (!s || !host) return FIA_ERR_INVALID;
+    const long long n = field_count(s, field);
+    void* dst = field_ptr(s, field);
+    if (n < 0 || !dst) return FIA_ERR_INVALID;
+    const size_t hb = host_dtype == FIA_HOST_F64 ? 8 : (host_dtype == FIA_HOST_F32 ? 4 : 0);
+    if (!hb) return FIA_ERR_INVALID;
+    if (hb == s->es) {
+        CK(cudaMemcpyAsync(dst, host, n * hb, cudaMemcpyHostToDevice, s->stream));
+    } else {
+        CK(cudaMemcpyAsync(s->cbuf, host, n * hb, cudaMemcpyHostToDevice, s->stream));
+        if (hb == 4) k_convert<double, float><<<512, 256, 0, s->stream>>>((const float*)s->cbuf, (double*)dst, n);
+        else k_convert<float, double><<<512, 256, 0, s->stream>>>((const double*)s->cbuf, (float*)dst, n);
+        CK(cudaGetLastError());
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    return FIA_OK;
+}
+
+int fia_get_field(fia_session* s, int field, void* host, int host_dtype) {
+    if (!s || !host) return FIA_ERR_INVALID;
+    const long long n = field_count(s, field);
+    void* src = field_ptr(s, field);
+    if (n < 0 || !src) return FIA_ERR_INVALID;
+    const size_t hb = host_dtype == FIA_HOST_F64 ? 8 : (host_dtype == FIA_HOST_F32 ? 4 : 0);
+    if (!hb) return FIA_ERR_INVALID;
+    if (hb == s->es) {
+        CK(cudaMemcpyAsync(host, src, n * hb, cudaMemcpyDeviceToHost, s->stream));
+    } else {
+        if (hb == 4) k_convert<float, double><<<512, 256, 0, s->stream>>>((const double*)src, (float*)s->cbuf, n);
+        else k_convert<double, float><<<512, 256, 0, s->stream>>>((const float*)src, (double*)s->cbuf, n);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(host, s->cbuf, n * hb, cudaMemcpyDeviceToHost, s->stream));
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    return FIA_OK;
+}
+
+int fia_field_device_ptr(fia_session* s, int field, void** dev_ptr) {
+    if (!s || !dev_ptr) return FIA_ERR_INVALID;
+    void* p = field_ptr(s, field);
+    if (!p) return FIA_ERR_INVALID;
+    *dev_ptr = p;
+    return FIA_OK;
+}
+
+int fia_move_substances_3D(fia_session* s, double dt, const fia_advect_params* p) {
+    if (!s || !(dt >= 0.0)) return FIA_ERR_INVALID;
+    const int c = check_params(p);
+    if (c != FIA_OK) return c;
+    return move_substances<double>(s, dt, p);
+}
+
+int fia_advect_velocity_xyz(fia_session* s, double dt, const fia_advect_params* p) {
+    if (!s || !(dt >= 0.0)) return FIA_ERR_INVALID;
+    const int c = check_params(p);
+    if (c != FIA_OK) return c;
+    return advect_velocity<double>(s, dt, p);
+}
+
+int fia_calc_pressure_3D(fia_session* s, const fia_solver_params* sp, fia_solver_report* rep) {
+    if (!s) return FIA_ERR_INVALID;
+    return pressure<double>(s, sp, rep, false);
+}
+
+int fia_calc_pressure_gradient_term_3D(fia_session* s, const fia_solver_params* sp, fia_solver_report* rep) {
+    if (!s) return FIA_ERR_INVALID;
+    return pressure<double>(s, sp, rep, true);
+}
+
+int fia_max_abs_velocity(fia_session* s, double* out) {
+    if (!s || !out) return FIA_ERR_INVALID;
+    CK(cudaMemsetAsync(s->red_out, 0, sizeof(double), s->stream));
+    for (int c = 0; c < 3; ++c) CK(reduce<double>(s, s->vel[c], field_count(s, FIA_FIELD_U + c), 1, true));
+    CK(cudaMemcpyAsync(out, s->red_out, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FIA_OK;
+}
+
+int fia_total_mass(fia_session* s, double* out) {
+    if (!s || !out) return FIA_ERR_INVALID;
+    CK(reduce<double>(s, s->rho, field_count(s, FIA_FIELD_DENSITY), 0, false));
+    double m = 0.0;
+    CK(cudaMemcpyAsync(&m, s->red_out, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    *out = m * (s->h * s->h * s->h);
+    return FIA_OK;
+}
+
+int fia_wall_momentum_loss(fia_session* s, double* out3) {
+    if (!s || !out3) return FIA_ERR_INVALID;
+    for (int c = 0; c < 3; ++c) out3[c] = s->wall_loss[c];
+    return FIA_OK;
+}
+
+int fia_pass_counters(fia_session* s, unsigned long long* out2) {
+    if (!s || !out2) return FIA_ERR_INVALID;
+    if (s->counters_pending) {
+        CK(cudaMemcpyAsync(s->counters_host, s->counters, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        s->counters_pending = false;
+    }
+    out2[0] = s->counters_host[0]; out2[1] = s->counters_host[1];
+    return FIA_OK;
+}
+
+int fia_move_substances_3D_host(fia_session* s, int host_dtype, void* rho, const void* u, const void* v,
+                                const void* w, double dt, const fia_advect_params* p) {
+    int r;
+    if ((r = fia_set_field(s, FIA_FIELD_DENSITY, rho, host_dtype)) != FIA_OK) return r;
+    if ((r = fia_set_field(s, FIA_FIELD_U, u, host_dtype)) != FIA_OK) return r;
+    if ((r = fia_set_field(s, FIA_FIELD_V, v, host_dtype)) != FIA_OK) return r;
+    if ((r = fia_set_field(s, FIA_FIELD_W, w, host_dtype)) != FIA_OK) return r;
+    if ((r = fia_move_substances_3D(s, dt, p)) < 0) return r;
+    if ((r = fia_get_field(s, FIA_FIELD_DENSITY, rho, host_dtype)) != FIA_OK) return r;
+    return fia_last_status(s);
+}
+
+int fia_advect_velocity_xyz_host(fia_session* s, int host_dtype, void* u, void* v, void* w, double dt,
+                                 const fia_advect_params* p) {
+    int r;
+    void* f[3] = {u, v, w};
+    for (int c = 0; c < 3; ++c) if ((r = fia_set_field(s, FIA_FIELD_U + c, f[c], host_dtype)) != FIA_OK) return r;
+    if ((r = fia_advect_velocity_xyz(s, dt, p)) < 0) return r;
+    for (int c = 0; c < 3; ++c) if ((r = fia_get_field(s, FIA_FIELD_U + c, f[c], host_dtype)) != FIA_OK) return r;
+    return fia_last_status(s);
+}
+
+int fia_calc_pressure_gradient_term_3D_host(fia_session* s, int host_dtype, void* u, void* v, void* w,
+                                            void* pressure_out, const fia_solver_params* sp,
+                                            fia_solver_report* rep) {
+    int r;
+    void* f[3] = {u, v, w};
+    for (int c = 0; c < 3; ++c) if ((r = fia_set_field(s, FIA_FIELD_U + c, f[c], host_dtype)) != FIA_OK) return r;
+    const int st = fia_calc_pressure_gradient_term_3D(s, sp, rep);
+    if (st < 0) return st;
+    for (int c = 0; c < 3; ++c) if ((r = fia_get_field(s, FIA_FIELD_U + c, f[c], host_dtype)) != FIA_OK) return r;
+    if (pressure_out && (r = fia_get_field(s, FIA_FIELD_PRESSURE, pressure_out, host_dtype)) != FIA_OK) return r;
+    return st;
+}
+
+int fia_debug_flux_pass(fia_session* s, int comp, const double* field, double dt, int interp, int psi_mode,
+                        int use_integral, int zero_velocity, const double* co, int k, double minimal_area,
+                        double* out) {
+    if (!s || !field || !out || !co || comp < -1 || comp > 2 || k < 1 || k > kMaxGauss || interp < 0 || interp > 2 ||
+        psi_mode < 0 || psi_mode > 2)
+        return FIA_ERR_INVALID;
+    return debug_flux_pass<double>(s, comp, field, dt, interp, psi_mode, use_integral, zero_velocity, co, k,
+                                   minimal_area, out);
+}
+
+int fia_debug_backtrace(fia_session* s, int comp, double dt, int interp, double* out) {
+    if (!s || !out || comp < -1 || comp > 2 || interp < 0 || interp > 2) return FIA_ERR_INVALID;
+    return debug_backtrace<double>(s, comp, dt, interp, out);
+}
+
+int fia_debug_psi(fia_session* s, int comp, const double* field, int mode, int k, double* out) {
+    if (!s || !field || !out || comp < -1 || comp > 2 || mode < 0 || mode > 2 || k < 1 || k > kMaxGauss)
+        return FIA_ERR_INVALID;
+    return debug_psi<double>(s, comp, field, mode, k, out);
+}
+
+}  // extern "C"

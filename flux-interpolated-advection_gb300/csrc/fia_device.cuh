@@ -1,0 +1,183 @@
+// fia_device.cuh -- device building blocks of the flux-interpolated advection path.
+//
+// Node fields: an array of M.x*M.y*M.z values, z fastest and x slowest (the reference
+// layout, utils.h:65-165), whose node (i,j,k) sits at ((i+off.x)h, (j+off.y)h, (k+off.z)h).
+//   density M=(N,N,N) off=(.5,.5,.5); u M=(N+1,N,N) off=(0,.5,.5); v, w likewise;
+//   psi of a field with offsets off: M=(Mx,My+1,Mz), off-(0,.5,0).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fia {
+
+struct NodeField {
+    int Mx, My, Mz;
+    double ox, oy, oz;  // node offsets in units of the cell length
+};
+
+__device__ __forceinline__ int clampi(int i, int hi) { return i < 0 ? 0 : (i > hi ? hi : i); }
+__device__ __forceinline__ long long idx3(const NodeField& F, int i, int j, int k) {
+    return (long long)F.Mz * ((long long)F.My * i + j) + k;
+}
+
+// Read-only load through the non-coherent cache.
+template <typename T> __device__ __forceinline__ T ldg(const T* p) { return __ldg(p); }
+
+// --------------------------------------------------------------------------------
+// WENO6 coefficients that depend only on the sample position: for signed distances
+// t_i = (p - x_i)/h of the six nodes, the three cubic candidates are
+//   P_i = f_i + (f_{i+1}-f_i) a_i + (f_{i+2}-2f_{i+1}+f_i) b_i + (f_{i+3}-3f_{i+2}+3f_{i+1}-f_i) c_i
+// with a_i = t_i, b_i = t_i t_{i+1}/2, c_i = t_i t_{i+1} t_{i+2}/6, and the ideal weights
+// C = (t4 t5/20, -t5 t0/10, t0 t1/20)  (WENO6_interpolation_3d.cpp:70-92).
+// --------------------------------------------------------------------------------
+template <typename T>
+struct WenoCoef {
+    T a[3], b[3], c[3], C[3];
+};
+
+template <typename T>
+__device__ __forceinline__ WenoCoef<T> weno_coef(const T* t) {
+    WenoCoef<T> w;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        w.a[i] = t[i];
+        w.b[i] = t[i] * t[i + 1] / T(2);
+        w.c[i] = t[i] * t[i + 1] * t[i + 2] / T(6);
+    }
+    w.C[0] = t[4] * t[5] / T(20);
+    w.C[1] = -t[5] * t[0] / T(10);
+    w.C[2] = t[0] * t[1] / T(20);
+    return w;
+}
+
+// One 1D WENO6 evaluation: smoothness indicators with integer coefficients over 180,
+// alpha_i = C_i / (1e-6 + beta_i)^2, normalised weights (WENO6_interpolation_3d.cpp:94-123).
+template <typename T>
+__device__ __forceinline__ T weno6_eval(const T* f, const WenoCoef<T>& w) {
+    T P[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        T d1 = f[i + 1] - f[i];
+        T d2 = f[i + 2] - T(2) * f[i + 1] + f[i];
+        T d3 = f[i + 3] - T(3) * f[i + 2] + T(3) * f[i + 1] - f[i];
+        P[i] = f[i] + d1 * w.a[i] + d2 * w.b[i] + d3 * w.c[i];
+    }
+    const T f0 = f[0], f1 = f[1], f2 = f[2], f3 = f[3], f4 = f[4], f5 = f[5];
+    T b0 = (T(-3579) * f3 * f2 + T(2634) * f3 * f1 - T(683) * f3 * f0
+            - T(6927) * f2 * f1 + T(1854) * f2 * f0 - T(1659) * f1 * f0
+            + T(814) * f3 * f3 + T(4326) * f2 * f2 + T(2976) * f1 * f1
+            + T(244) * f0 * f0) / T(180);
+    T b1 = (T(-3777) * f3 * f2 + T(1074) * f3 * f1 - T(1269) * f2 * f1
+            + T(1986) * f3 * f3 + T(1986) * f2 * f2 + T(244) * f1 * f1
+            + T(244) * f4 * f4 - T(1269) * f4 * f3 + T(1074) * f4 * f2
+            - T(293) * f4 * f1) / T(180);
+    T b2 = (T(-3579) * f3 * f2 + T(4326) * f3 * f3 + T(814) * f2 * f2
+            + T(2976) * f4 * f4 + T(244) * f5 * f5 - T(683) * f5 * f2
+            - T(6927) * f4 * f3 + T(2634) * f4 * f2 - T(1659) * f5 * f4
+            + T(1854) * f5 * f3) / T(180);
+    const T eps = T(0.000001);
+    T e0 = eps + b0, e1 = eps + b1, e2 = eps + b2;
+    T al0 = w.C[0] / (e0 * e0), al1 = w.C[1] / (e1 * e1), al2 = w.C[2] / (e2 * e2);
+    T s = al0 + al1 + al2;
+    return (al0 / s) * P[0] + (al1 / s) * P[1] + (al2 / s) * P[2];
+}
+
+// Tensor-product WENO6 of a node field at p (z, then y, then x), stencil indices clamped
+// to the array (WENO6_interpolation_3d.cpp:7-258 and the face-value variants).
+template <typename T>
+__device__ T weno6_3d(const T* __restrict__ a, const NodeField& F, T h, T px, T py, T pz) {
+    int bx = (int)floor((px - T(F.ox) * h) / h);
+    int by = (int)floor((py - T(F.oy) * h) / h);
+    int bz = (int)floor((pz - T(F.oz) * h) / h);
+    T tx[6], ty[6], tz[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        tx[i] = (px - (T(bx - 2 + i) + T(F.ox)) * h) / h;
+        ty[i] = (py - (T(by - 2 + i) + T(F.oy)) * h) / h;
+        tz[i] = (pz - (T(bz - 2 + i) + T(F.oz)) * h) / h;
+    }
+    const WenoCoef<T> cx = weno_coef(tx), cy = weno_coef(ty), cz = weno_coef(tz);
+    int kk[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) kk[i] = clampi(bz - 2 + i, F.Mz - 1);
+    T yv[6];
+#pragma unroll 1
+    for (int ix = 0; ix < 6; ++ix) {
+        const int ii = clampi(bx - 2 + ix, F.Mx - 1);
+        T zv[6];
+#pragma unroll
+        for (int iy = 0; iy < 6; ++iy) {
+            const int jj = clampi(by - 2 + iy, F.My - 1);
+            const T* row = a + (long long)F.Mz * ((long long)F.My * ii + jj);
+            T f[6];
+#pragma unroll
+            for (int iz = 0; iz < 6; ++iz) f[iz] = ldg(row + kk[iz]);
+            zv[iy] = weno6_eval(f, cz);
+        }
+        yv[ix] = weno6_eval(zv, cy);
+    }
+    return weno6_eval(yv, cx);
+}
+
+// WENO6 along y only; x and z take the node whose cell holds p
+// (WENO6_interpolation_1d.cpp:315-430).
+template <typename T>
+__device__ T weno6_1dy(const T* __restrict__ a, const NodeField& F, T h, T px, T py, T pz) {
+    const int ix = clampi((int)floor((px - (T(F.ox) * h - T(0.5) * h)) / h), F.Mx - 1);
+    const int iz = clampi((int)floor((pz - (T(F.oz) * h - T(0.5) * h)) / h), F.Mz - 1);
+    const int by = (int)floor((py - T(F.oy) * h) / h);
+    T t[6], f[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        t[i] = (py - (T(by - 2 + i) + T(F.oy)) * h) / h;
+        f[i] = ldg(a + idx3(F, ix, clampi(by - 2 + i, F.My - 1), iz));
+    }
+    return weno6_eval(f, weno_coef(t));
+}
+
+// Trilinear interpolation with clamped indices (linear_interpolation_3d.cpp:7-95).
+template <typename T>
+__device__ T lin3d(const T* __restrict__ a, const NodeField& F, T h, T px, T py, T pz) {
+    const T ox = T(F.ox) * h, oy = T(F.oy) * h, oz = T(F.oz) * h;
+    const int bx = (int)floor((px - ox) / h), by = (int)floor((py - oy) / h), bz = (int)floor((pz - oz) / h);
+    const T sx = (px - ox) / h - T(bx), sy = (py - oy) / h - T(by), sz = (pz - oz) / h - T(bz);
+    const int k0 = clampi(bz, F.Mz - 1), k1 = clampi(bz + 1, F.Mz - 1);
+    T yv[2];
+#pragma unroll
+    for (int ix = 0; ix < 2; ++ix) {
+        const int ii = clampi(bx + ix, F.Mx - 1);
+        T zv[2];
+#pragma unroll
+        for (int iy = 0; iy < 2; ++iy) {
+            const int jj = clampi(by + iy, F.My - 1);
+            const T* row = a + (long long)F.Mz * ((long long)F.My * ii + jj);
+            zv[iy] = (T(1) - sz) * ldg(row + k0) + sz * ldg(row + k1);
+        }
+        yv[ix] = (T(1) - sy) * zv[0] + sy * zv[1];
+    }
+    return (T(1) - sx) * yv[0] + sx * yv[1];
+}
+
+// Linear along y, nearest cell in x and z (linear_interpolation_1d.cpp:314-374).
+template <typename T>
+__device__ T lin1dy(const T* __restrict__ a, const NodeField& F, T h, T px, T py, T pz) {
+    const int ix = clampi((int)floor((px - (T(F.ox) * h - T(0.5) * h)) / h), F.Mx - 1);
+    const int iz = clampi((int)floor((pz - (T(F.oz) * h - T(0.5) * h)) / h), F.Mz - 1);
+    const T oy = T(F.oy) * h;
+    const int by = (int)floor((py - oy) / h);
+    const T f0 = ldg(a + idx3(F, ix, clampi(by, F.My - 1), iz));
+    const T f1 = ldg(a + idx3(F, ix, clampi(by + 1, F.My - 1), iz));
+    const T b0 = (py - oy) / h - T(by);
+    return (T(1) - b0) * f0 + b0 * f1;
+}
+
+enum Interp : int { INTERP_WENO6 = 0, INTERP_LINEAR = 1, INTERP_1DY_LINEAR = 2 };
+
+template <typename T>
+__device__ __forceinline__ T interp(int method, const T* __restrict__ a, const NodeField& F, T h, T px, T py, T pz) {
+    if (method == INTERP_WENO6) return weno6_3d(a, F, h, px, py, pz);
+    if (method == INTERP_LINEAR) return lin3d(a, F, h, px, py, pz);
+    return lin1dy(a, F, h, px, py, pz);
+}
+
+}  // namespace fia

@@ -1,0 +1,293 @@
+"""Host-side mirror of the reference's 3D entry points over the C ABI of libfia.so.
+
+The reference (nyhirasawa/Flux-Interpolated-Advection) is a C++ program; its hot path is
+called as
+
+    move_substances_3D(Grid_3D&, i_frame, dt, ...flags)            move_substances_3d.h:48-66
+    advect_velocity_xyz_flux_advection_3D_std_thread(Grid_3D&, dt, ...)   advect_velocity_flux_advection_3d.h:107-124
+    calc_pressure_3D(Grid_3D&) / calc_pressure_gradient_term_3D(Grid_3D&)  calc_pressure_3d.h:6-9
+
+This module keeps those names and flag names; a `Grid3D` owns a device-resident session
+(fia_create) with the Grid_3D arrays.  There is no CPU fallback: if libfia.so is not
+built for this machine, or no GPU is present, the calls raise.
+"""
+import ctypes
+import os
+import platform
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+LIBDIR = os.path.join(HERE, "lib")
+LIB = os.path.join(LIBDIR, "libfia_%s.so" % platform.machine())
+SOURCES = ["fia_api.cu", "fia_advect.cu", "fia_pressure.cu"]
+HEADERS = ["fia_device.cuh", "fia_advect.cuh", "fia_pressure.cuh"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+FIA_OK, FIA_ERR_INVALID, FIA_ERR_CUDA, FIA_ERR_UNSUPPORTED, FIA_ERR_NOMEM = 0, -1, -2, -3, -4
+FIA_FP64, FIA_FP32C = 0, 1
+FIA_HOST_F64, FIA_HOST_F32 = 0, 1
+FIELD = {"density": 0, "u": 1, "v": 2, "w": 3, "pressure": 4}
+INTERP = {"WENO6": 0, "linear": 1}
+SPLIT = {"xz-CellFaceAligned": 0, "xz-AxisAligned": 1, "x-CellFaceAligned_z-AxisAligned": 2,
+         "x-AxisAligned_z-CellFaceAligned": 3}
+STATUS_BITS = {1: "clip overflow", 2: "odd cut", 4: "non-finite flux", 8: "subdivision overflow",
+               16: "solver cap", 32: "solver fallback"}
+
+
+class FiaError(RuntimeError):
+    pass
+
+
+def _nvcc():
+    for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if c and (os.path.isabs(c) and os.path.exists(c) or not os.path.isabs(c)):
+            return c
+    return "nvcc"
+
+
+def build(force=False, jobs=None):
+    """Compile libfia for sm_103a into lib/ (in-tree).  Returns the library path."""
+    srcs = [os.path.join(CSRC, s) for s in SOURCES]
+    deps = srcs + [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(REPO, "include", "fia.h")]
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(d) for d in deps):
+        return LIB
+    objdir = os.path.join(HERE, "_build", platform.machine())
+    os.makedirs(objdir, exist_ok=True)
+    os.makedirs(LIBDIR, exist_ok=True)
+    nvcc = _nvcc()
+    flags = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", os.path.join(REPO, "include")]
+    procs, objs = [], []
+    for s in srcs:
+        o = os.path.join(objdir, os.path.basename(s) + ".o")
+        objs.append(o)
+        procs.append(subprocess.Popen([nvcc] + flags + ["-c", s, "-o", o]))
+    for p in procs:
+        if p.wait() != 0:
+            raise FiaError("nvcc failed building libfia")
+    tmp = LIB + ".tmp%d" % os.getpid()
+    subprocess.check_call([nvcc, "-shared"] + ARCH + ["-o", tmp] + objs + ["-lcudart"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def load():
+    """Load libfia (building it first if it is missing)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        lib = ctypes.CDLL(LIB)
+        _declare(lib)
+        _lib = lib
+    return _lib
+
+
+class AdvectParams(ctypes.Structure):
+    """Flags of move_substances_3D (main.cpp:48-83), same names."""
+    _fields_ = [("interpolation_method", ctypes.c_int), ("split_method", ctypes.c_int),
+                ("num_gauss_quadrature_point_for_integrate_density", ctypes.c_int),
+                ("use_integral", ctypes.c_int), ("enable_eliminate_zero_velocity_false_diffusion", ctypes.c_int),
+                ("use_MacCormack_scheme", ctypes.c_int), ("enable_cell_volume_correction", ctypes.c_int),
+                ("minimal_area", ctypes.c_double)]
+
+
+class SolverParams(ctypes.Structure):
+    _fields_ = [("tol", ctypes.c_double), ("max_iter", ctypes.c_int), ("method", ctypes.c_int)]
+
+
+class SolverReport(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("rel_residual", ctypes.c_double), ("status", ctypes.c_int)]
+
+
+def _declare(lib):
+    vp, dp, ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int
+    lib.fia_create.restype = vp
+    lib.fia_create.argtypes = [ip, ip, ip, ctypes.c_double, ip]
+    lib.fia_destroy.argtypes = [vp]
+    lib.fia_error_string.restype = ctypes.c_char_p
+    lib.fia_stream.restype = vp
+    lib.fia_stream.argtypes = [vp]
+    for name in ("fia_last_status", "fia_synchronize"):
+        getattr(lib, name).argtypes = [vp]
+    lib.fia_set_field.argtypes = [vp, ip, vp, ip]
+    lib.fia_get_field.argtypes = [vp, ip, vp, ip]
+    lib.fia_field_device_ptr.argtypes = [vp, ip, ctypes.POINTER(vp)]
+    lib.fia_move_substances_3D.argtypes = [vp, ctypes.c_double, ctypes.POINTER(AdvectParams)]
+    lib.fia_advect_velocity_xyz.argtypes = [vp, ctypes.c_double, ctypes.POINTER(AdvectParams)]
+    lib.fia_calc_pressure_3D.argtypes = [vp, ctypes.POINTER(SolverParams), ctypes.POINTER(SolverReport)]
+    lib.fia_calc_pressure_gradient_term_3D.argtypes = [vp, ctypes.POINTER(SolverParams), ctypes.POINTER(SolverReport)]
+    lib.fia_max_abs_velocity.argtypes = [vp, dp]
+    lib.fia_total_mass.argtypes = [vp, dp]
+    lib.fia_wall_momentum_loss.argtypes = [vp, dp]
+    lib.fia_pass_counters.argtypes = [vp, ctypes.POINTER(ctypes.c_ulonglong)]
+    lib.fia_move_substances_3D_host.argtypes = [vp, ip, vp, vp, vp, vp, ctypes.c_double, ctypes.POINTER(AdvectParams)]
+    lib.fia_advect_velocity_xyz_host.argtypes = [vp, ip, vp, vp, vp, ctypes.c_double, ctypes.POINTER(AdvectParams)]
+    lib.fia_calc_pressure_gradient_term_3D_host.argtypes = [vp, ip, vp, vp, vp, vp, ctypes.POINTER(SolverParams),
+                                                           ctypes.POINTER(SolverReport)]
+    lib.fia_debug_flux_pass.argtypes = [vp, ip, dp, ctypes.c_double, ip, ip, ip, ip, dp, ip, ctypes.c_double, dp]
+    lib.fia_debug_backtrace.argtypes = [vp, ip, ctypes.c_double, ip, dp]
+    lib.fia_debug_psi.argtypes = [vp, ip, dp, ip, ip, dp]
+    lib.fia_default_advect_params.argtypes = [ctypes.POINTER(AdvectParams)]
+    lib.fia_default_solver_params.argtypes = [ctypes.POINTER(SolverParams)]
+
+
+def _check(rc, what):
+    if rc < 0:
+        raise FiaError("%s failed: %s" % (what, load().fia_error_string(rc).decode()))
+    return rc
+
+
+def advect_params(interpolation_method="WENO6", split_method="xz-CellFaceAligned",
+                  num_gauss_quadrature_point_for_integrate_density=3, use_integral=True,
+                  enable_eliminate_zero_velocity_false_diffusion=True, use_MacCormack_scheme=False,
+                  enable_cell_volume_correction=False, minimal_area=1.0):
+    p = AdvectParams()
+    p.interpolation_method = INTERP[interpolation_method]
+    p.split_method = SPLIT[split_method]
+    p.num_gauss_quadrature_point_for_integrate_density = num_gauss_quadrature_point_for_integrate_density
+    p.use_integral = int(bool(use_integral))
+    p.enable_eliminate_zero_velocity_false_diffusion = int(bool(enable_eliminate_zero_velocity_false_diffusion))
+    p.use_MacCormack_scheme = int(bool(use_MacCormack_scheme))
+    p.enable_cell_volume_correction = int(bool(enable_cell_volume_correction))
+    p.minimal_area = minimal_area
+    return p
+
+
+def solver_params(tol=1e-6, max_iter=10000, method=0):
+    p = SolverParams()
+    p.tol, p.max_iter, p.method = tol, max_iter, method
+    return p
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Grid3D:
+    """Device-resident Grid_3D (grid_3d.h:14-88): nx*ny*nz cells of length cell_length."""
+
+    def __init__(self, nx, ny, nz, cell_length, precision=FIA_FP64):
+        self.lib = load()
+        self.N = (nx, ny, nz)
+        self.h = cell_length
+        self.precision = precision
+        self.s = self.lib.fia_create(nx, ny, nz, ctypes.c_double(cell_length), precision)
+        if not self.s:
+            raise FiaError("fia_create failed: " + self.lib.fia_error_string(FIA_ERR_CUDA).decode())
+
+    def close(self):
+        if self.s:
+            self.lib.fia_destroy(self.s)
+            self.s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sizes(self):
+        nx, ny, nz = self.N
+        return {"density": nx * ny * nz, "pressure": nx * ny * nz, "u": (nx + 1) * ny * nz,
+                "v": nx * (ny + 1) * nz, "w": nx * ny * (nz + 1)}
+
+    # ---- field access ----
+    def set(self, name, values):
+        a = np.ascontiguousarray(values, dtype=np.float64).ravel()
+        if a.size != self.sizes()[name]:
+            raise FiaError("field %s: expected %d values, got %d" % (name, self.sizes()[name], a.size))
+        _check(self.lib.fia_set_field(self.s, FIELD[name], a.ctypes.data, FIA_HOST_F64), "fia_set_field")
+
+    def get(self, name):
+        a = np.empty(self.sizes()[name], dtype=np.float64)
+        _check(self.lib.fia_get_field(self.s, FIELD[name], a.ctypes.data, FIA_HOST_F64), "fia_get_field")
+        return a
+
+    def device_ptr(self, name):
+        p = ctypes.c_void_p()
+        _check(self.lib.fia_field_device_ptr(self.s, FIELD[name], ctypes.byref(p)), "fia_field_device_ptr")
+        return p.value
+
+    def stream(self):
+        return self.lib.fia_stream(self.s)
+
+    def synchronize(self):
+        _check(self.lib.fia_synchronize(self.s), "fia_synchronize")
+
+    def last_status(self):
+        return _check(self.lib.fia_last_status(self.s), "fia_last_status")
+
+    # ---- the reference's entry points ----
+    def move_substances_3D(self, time_step_length, params=None):
+        p = params or advect_params()
+        return _check(self.lib.fia_move_substances_3D(self.s, ctypes.c_double(time_step_length), ctypes.byref(p)),
+                      "move_substances_3D")
+
+    def advect_velocity_xyz_flux_advection_3D(self, time_step_length, params=None):
+        p = params or advect_params()
+        return _check(self.lib.fia_advect_velocity_xyz(self.s, ctypes.c_double(time_step_length), ctypes.byref(p)),
+                      "advect_velocity_xyz_flux_advection_3D")
+
+    def calc_pressure_3D(self, sp=None):
+        rep = SolverReport()
+        _check(self.lib.fia_calc_pressure_3D(self.s, ctypes.byref(sp or solver_params()), ctypes.byref(rep)),
+               "calc_pressure_3D")
+        return rep
+
+    def calc_pressure_gradient_term_3D(self, sp=None):
+        rep = SolverReport()
+        _check(self.lib.fia_calc_pressure_gradient_term_3D(self.s, ctypes.byref(sp or solver_params()),
+                                                           ctypes.byref(rep)), "calc_pressure_gradient_term_3D")
+        return rep
+
+    def max_abs_velocity(self):
+        out = ctypes.c_double(0)
+        _check(self.lib.fia_max_abs_velocity(self.s, ctypes.byref(out)), "fia_max_abs_velocity")
+        return out.value
+
+    def total_mass(self):
+        out = ctypes.c_double(0)
+        _check(self.lib.fia_total_mass(self.s, ctypes.byref(out)), "fia_total_mass")
+        return out.value
+
+    def wall_momentum_loss(self):
+        out = (ctypes.c_double * 3)()
+        _check(self.lib.fia_wall_momentum_loss(self.s, out), "fia_wall_momentum_loss")
+        return tuple(out)
+
+    def pass_counters(self):
+        out = (ctypes.c_ulonglong * 2)()
+        _check(self.lib.fia_pass_counters(self.s, out), "fia_pass_counters")
+        return int(out[0]), int(out[1])
+
+    # ---- test hooks ----
+    def debug_flux_pass(self, comp, field, dt, interp, psi_mode, use_integral, zero_velocity, color_off, k,
+                        minimal_area=1.0):
+        f = np.ascontiguousarray(field, dtype=np.float64)
+        out = np.zeros(f.size)
+        co = np.array(color_off, dtype=np.float64)
+        st = _check(self.lib.fia_debug_flux_pass(self.s, comp, _dp(f), ctypes.c_double(dt), interp, psi_mode,
+                                                 use_integral, zero_velocity, _dp(co), k,
+                                                 ctypes.c_double(minimal_area), _dp(out)), "fia_debug_flux_pass")
+        return out, st
+
+    def debug_backtrace(self, comp, dt, interp):
+        L = [self.N[d] + 1 + (d == comp) for d in range(3)]
+        out = np.zeros(L[0] * L[1] * L[2] * 3)
+        _check(self.lib.fia_debug_backtrace(self.s, comp, ctypes.c_double(dt), interp, _dp(out)), "fia_debug_backtrace")
+        return out.reshape(L[0], L[1], L[2], 3)
+
+    def debug_psi(self, comp, field, mode, k):
+        f = np.ascontiguousarray(field, dtype=np.float64)
+        M = [self.N[d] + (d == comp) for d in range(3)]
+        out = np.zeros(M[0] * (M[1] + 1) * M[2])
+        _check(self.lib.fia_debug_psi(self.s, comp, _dp(f), mode, k, _dp(out)), "fia_debug_psi")
+        return out

@@ -1,0 +1,160 @@
+/*
+ * fia.h -- C ABI of the GB300 flux-interpolated advection library (libfia.so).
+ *
+ * The library replaces the 3D hot path of the reference program
+ * (nyhirasawa/Flux-Interpolated-Advection): the density flux advection
+ * (move_substances_3D), the velocity flux advection
+ * (advect_velocity_xyz_flux_advection_3D_std_thread), the pressure projection
+ * (calc_pressure_3D / calc_pressure_gradient_term_3D) and the CFL time step.
+ * Only plain C types cross this boundary; fields use the reference's Grid_3D layout
+ * (grid_3d.h:35-54): z fastest, x slowest; density and pressure nx*ny*nz, u (nx+1)*ny*nz,
+ * v nx*(ny+1)*nz, w nx*ny*(nz+1); cell length h, domain [0, n*h]^3, closed box.
+ *
+ * Errors: every function returns FIA_OK (0) or a negative FIA_ERR_* code; a positive
+ * return is a set of FIA_STATUS_* bits (the call completed, with numerical warnings).
+ * The reference itself has no error convention (void functions, exit(0) in the face
+ * clipper at facecutter.h:191-204); see INTEGRATION.md for the shim that keeps the
+ * reference's void signatures.
+ */
+#ifndef FIA_H
+#define FIA_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FIA_API_VERSION 1
+
+/* return codes */
+#define FIA_OK 0
+#define FIA_ERR_INVALID -1      /* bad argument (null pointer, size, enum value) */
+#define FIA_ERR_CUDA -2         /* a CUDA call failed (fia_error_string has the text) */
+#define FIA_ERR_UNSUPPORTED -3  /* option the library does not implement */
+#define FIA_ERR_NOMEM -4        /* device allocation failed */
+
+/* status bits (positive returns, also fia_last_status) */
+#define FIA_STATUS_CLIP_OVERFLOW 1    /* a clipped piece exceeded 32 vertices (MAX_TMP_POINTS) */
+#define FIA_STATUS_CLIP_ODD_CUT 2     /* odd number of iso-line crossings; the reference exit(0)s */
+#define FIA_STATUS_NONFINITE 4        /* a non-finite face flux was produced */
+#define FIA_STATUS_SUBDIV_OVERFLOW 8  /* minimal_area triangulation stack exhausted */
+#define FIA_STATUS_SOLVER_CAP 16      /* pressure solver stopped at max_iter before tol */
+#define FIA_STATUS_SOLVER_FALLBACK 32 /* learned-preconditioned FCG fell back to plain PCG */
+
+/* device precision of a session */
+#define FIA_FP64 0   /* plain form: FP64 throughout */
+#define FIA_FP32C 1  /* chosen form: FP32 advection with compensated sums, FP64 reductions */
+
+/* element type of host buffers */
+#define FIA_HOST_F64 0
+#define FIA_HOST_F32 1
+
+/* fields */
+#define FIA_FIELD_DENSITY 0
+#define FIA_FIELD_U 1
+#define FIA_FIELD_V 2
+#define FIA_FIELD_W 3
+#define FIA_FIELD_PRESSURE 4
+
+/* interpolation_method (main.cpp:60) */
+#define FIA_INTERP_WENO6 0
+#define FIA_INTERP_LINEAR 1
+
+/* split_method (split_face_3D.cpp:26-41); the density main pass uses the caller's */
+#define FIA_SPLIT_XZ_CELLFACE 0           /* "xz-CellFaceAligned" */
+#define FIA_SPLIT_XZ_AXIS 1               /* "xz-AxisAligned" */
+#define FIA_SPLIT_XCELLFACE_ZAXIS 2       /* "x-CellFaceAligned_z-AxisAligned" */
+#define FIA_SPLIT_XAXIS_ZCELLFACE 3       /* "x-AxisAligned_z-CellFaceAligned" */
+
+/* pressure solvers */
+#define FIA_SOLVER_PCG_JACOBI 0
+
+typedef struct fia_session fia_session;
+
+/* Flags of move_substances_3D / advect_velocity_xyz_flux_advection_3D_std_thread
+ * (move_substances_3d.h:48-66, advect_velocity_flux_advection_3d.h:107-124), same names. */
+typedef struct fia_advect_params {
+    int interpolation_method;                               /* FIA_INTERP_* */
+    int split_method;                                       /* FIA_SPLIT_*, density main pass */
+    int num_gauss_quadrature_point_for_integrate_density;   /* odd, 1..13 */
+    int use_integral;                                       /* y-integral quadrature (main.cpp:64) */
+    int enable_eliminate_zero_velocity_false_diffusion;     /* passes 2 and 3 (main.cpp:70) */
+    int use_MacCormack_scheme;                              /* must be 0 */
+    int enable_cell_volume_correction;                      /* must be 0 */
+    double minimal_area;                                    /* xi-eta triangulation threshold (main.cpp:82) */
+} fia_advect_params;
+
+typedef struct fia_solver_params {
+    double tol;        /* relative residual |b - A p| / |b| */
+    int max_iter;
+    int method;        /* FIA_SOLVER_* */
+} fia_solver_params;
+
+typedef struct fia_solver_report {
+    int iterations;
+    double rel_residual;
+    int status;        /* FIA_STATUS_* bits of the solve */
+} fia_solver_report;
+
+/* Reference defaults for the flags (main.cpp:48-83) with WENO6, xz-CellFaceAligned, k = 3. */
+void fia_default_advect_params(fia_advect_params* p);
+void fia_default_solver_params(fia_solver_params* p);
+
+int fia_api_version(void);
+const char* fia_error_string(int code);
+
+/* Session: device-resident Grid_3D of nx*ny*nz cells (replaces the Grid_3D ctor,
+ * grid_3d.cpp:13-47).  Returns NULL on failure. */
+fia_session* fia_create(int nx, int ny, int nz, double cell_length, int precision);
+void fia_destroy(fia_session* s);
+int fia_last_status(const fia_session* s);
+/* The session's CUDA stream (a cudaStream_t), for callers that order their own work. */
+void* fia_stream(fia_session* s);
+int fia_synchronize(fia_session* s);
+
+/* Host <-> device copies of one field (host_dtype FIA_HOST_F64 or FIA_HOST_F32). */
+int fia_set_field(fia_session* s, int field, const void* host, int host_dtype);
+int fia_get_field(fia_session* s, int field, void* host, int host_dtype);
+/* Device address of a field (element type is the session precision's). */
+int fia_field_device_ptr(fia_session* s, int field, void** dev_ptr);
+
+/* move_substances_3D (move_substances_3d.cpp:38-240), flux branch, on the device. */
+int fia_move_substances_3D(fia_session* s, double time_step_length, const fia_advect_params* p);
+/* advect_velocity_xyz_flux_advection_3D_std_thread (advect_velocity_flux_advection_3d.cpp:1138-1272). */
+int fia_advect_velocity_xyz(fia_session* s, double time_step_length, const fia_advect_params* p);
+/* calc_pressure_3D (calc_pressure_3d.cpp:18-181): pressure of the current velocity. */
+int fia_calc_pressure_3D(fia_session* s, const fia_solver_params* sp, fia_solver_report* rep);
+/* calc_pressure_gradient_term_3D (calc_pressure_3d.cpp:183-270): solve, subtract, wall tallies. */
+int fia_calc_pressure_gradient_term_3D(fia_session* s, const fia_solver_params* sp, fia_solver_report* rep);
+/* The CFL reduction of calc_time_step_length_from_CFL_number_3D (:90-117). */
+int fia_max_abs_velocity(fia_session* s, double* out);
+/* Sum of density * cell volume (the mass of main.cpp:520-531), FP64. */
+int fia_total_mass(fia_session* s, double* out);
+/* total_loss_of_momentum_{x,y,z} accumulated by calc_pressure_gradient_term_3D. */
+int fia_wall_momentum_loss(fia_session* s, double* out3);
+/* Faces visited and pieces emitted by the last advection call. */
+int fia_pass_counters(fia_session* s, unsigned long long* out2);
+
+/* Drop-in bodies with host buffers: copy in, run on the device, copy out (synchronous). */
+int fia_move_substances_3D_host(fia_session* s, int host_dtype, void* substance_density, const void* u,
+                                const void* v, const void* w, double time_step_length,
+                                const fia_advect_params* p);
+int fia_advect_velocity_xyz_host(fia_session* s, int host_dtype, void* u, void* v, void* w,
+                                 double time_step_length, const fia_advect_params* p);
+int fia_calc_pressure_gradient_term_3D_host(fia_session* s, int host_dtype, void* u, void* v, void* w,
+                                            void* pressure, const fia_solver_params* sp,
+                                            fia_solver_report* rep);
+
+/* Test hooks: single pieces of the path on host data (FP64 buffers), mirroring the oracle. */
+/* one flux pass of a node field (comp -1 density, 0..2 velocity) with the session velocity */
+int fia_debug_flux_pass(fia_session* s, int comp, const double* field, double dt, int interp, int psi_mode,
+                        int use_integral, int zero_velocity, const double* color_off2, int k,
+                        double minimal_area, double* out);
+/* backtraced vertex positions of the cell lattice of a field (3 doubles per vertex) */
+int fia_debug_backtrace(fia_session* s, int comp, double dt, int interp, double* out);
+/* psi of a node field (mode 0 plain, 1 WENO6 integral, 2 linear integral) */
+int fia_debug_psi(fia_session* s, int comp, const double* field, int mode, int k, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FIA_H */

@@ -1,0 +1,209 @@
+"""GPU (libfia, FP64 plain form) against the CPU oracle, through the C ABI.
+
+Bar: 1e-10 relative L2 for the flux passes and entry points (the plain form's parity
+target), 1e-12 for psi and the backtraced vertex positions.
+"""
+import numpy as np
+import pytest
+
+import scenes
+from oracle import Oracle
+
+fia = pytest.importorskip("fia")
+
+pytestmark = pytest.mark.gpu
+
+O = Oracle()
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+def make(nx, ny, nz, seed=1, cfl=2.0):
+    n = max(nx, ny, nz)
+    h = 1.0 / n
+    # velocity on the cube of the largest side, cropped to the grid (still a valid MAC field)
+    u, v, w = scenes.fourier_velocity(n, seed=seed)
+    u = u.reshape(n + 1, n, n)[:nx + 1, :ny, :nz].ravel()
+    v = v.reshape(n, n + 1, n)[:nx, :ny + 1, :nz].ravel()
+    w = w.reshape(n, n, n + 1)[:nx, :ny, :nz + 1].ravel()
+    rho = scenes.gaussian_blobs(n, seed=seed + 1).reshape(n, n, n)[:nx, :ny, :nz].ravel()
+    dt = cfl * h
+    g = fia.Grid3D(nx, ny, nz, h)
+    for name, a in (("density", rho), ("u", u), ("v", v), ("w", w)):
+        g.set(name, a)
+    return g, h, u, v, w, rho, dt
+
+
+@pytest.fixture(scope="module")
+def cube16():
+    g, h, u, v, w, rho, dt = make(16, 16, 16)
+    yield g, h, u, v, w, rho, dt
+    g.close()
+
+
+def field_of(comp, rho, u, v, w):
+    return rho if comp < 0 else (u, v, w)[comp]
+
+
+def offsets(comp):
+    return (0.5, 0.5, 0.5) if comp < 0 else tuple(0.0 if d == comp else 0.5 for d in range(3))
+
+
+@pytest.mark.parametrize("comp", [-1, 0, 1, 2])
+@pytest.mark.parametrize("mode,k", [(0, 1), (1, 3), (1, 1), (2, 1)])
+def test_psi(cube16, comp, mode, k):
+    g, h, u, v, w, rho, dt = cube16
+    f = field_of(comp, rho, u, v, w)
+    M = [16 + (d == comp) for d in range(3)]
+    ref = O.psi(f, M, offsets(comp), h, mode, k)
+    got = g.debug_psi(comp, f, mode, k)
+    assert np.abs(got - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max())
+
+
+@pytest.mark.parametrize("comp", [-1, 0, 1, 2])
+@pytest.mark.parametrize("interp", [0, 1, 2])
+def test_backtrace_vertices(cube16, comp, interp):
+    g, h, u, v, w, rho, dt = cube16
+    ref = O.backtrace_vertices((16, 16, 16), h, u, v, w, dt, comp, interp)
+    got = g.debug_backtrace(comp, dt, interp)
+    assert np.abs(got - ref).max() <= 1e-13
+
+
+PASSES = {  # interp, psi_mode, use_integral, zero_velocity, colour offsets
+    "weno6_integral": (0, 1, 1, 0, (0.5, 0.5)),
+    "weno6_zero_velocity": (0, 0, 0, 1, (0.5, 0.5)),
+    "error_1dy_linear": (2, 0, 0, 0, (0.0, 0.0)),
+    "linear_integral": (1, 2, 1, 0, (0.5, 0.5)),
+    "weno6_axis_split": (0, 1, 1, 0, (0.0, 0.5)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(PASSES))
+@pytest.mark.parametrize("comp", [-1, 0, 1, 2])
+def test_flux_pass(cube16, name, comp):
+    g, h, u, v, w, rho, dt = cube16
+    interp, psi_mode, integ, zv, co = PASSES[name]
+    f = field_of(comp, rho, u, v, w)
+    ref, ost, nf, npoly = O.flux_pass((16, 16, 16), h, u, v, w, comp, f, dt, interp, psi_mode, integ, zv, co, 3)
+    got, st = g.debug_flux_pass(comp, f, dt, interp, psi_mode, integ, zv, co, 3)
+    assert st == ost == 0
+    assert rel(got, ref) < 1e-10
+
+
+@pytest.mark.parametrize("interp,k,corr", [("WENO6", 3, True), ("WENO6", 1, False), ("linear", 3, True),
+                                           ("WENO6", 5, True)])
+def test_move_substances(interp, k, corr):
+    g, h, u, v, w, rho, dt = make(16, 16, 16, seed=5)
+    p = fia.advect_params(interpolation_method=interp, num_gauss_quadrature_point_for_integrate_density=k,
+                          enable_eliminate_zero_velocity_false_diffusion=corr)
+    st = g.move_substances_3D(dt, p)
+    got = g.get("density")
+    ref, ost = O.move_substances_3D((16, 16, 16), h, u, v, w, rho, dt, interp=fia.INTERP[interp], k=k,
+                                    correction=int(corr))
+    g.close()
+    assert st == 0 and ost == 0
+    assert rel(got, ref) < 1e-10
+
+
+@pytest.mark.parametrize("shape", [(12, 10, 8), (7, 9, 6), (24, 16, 20)])
+def test_move_substances_ragged_grids(shape):
+    g, h, u, v, w, rho, dt = make(*shape, seed=7)
+    g.move_substances_3D(dt, fia.advect_params())
+    got = g.get("density")
+    ref, _ = O.move_substances_3D(shape, h, u, v, w, rho, dt)
+    g.close()
+    assert rel(got, ref) < 1e-10
+
+
+def test_move_substances_cfl4_long_faces():
+    g, h, u, v, w, rho, dt = make(16, 16, 16, seed=9, cfl=4.0)
+    g.move_substances_3D(dt, fia.advect_params())
+    got = g.get("density")
+    faces, pieces = g.pass_counters()
+    ref, _ = O.move_substances_3D((16, 16, 16), h, u, v, w, rho, dt)
+    g.close()
+    assert rel(got, ref) < 1e-10
+    assert pieces > faces  # long faces are split
+
+
+def test_zero_velocity_keeps_interior_constant():
+    n = 12
+    g = fia.Grid3D(n, n, n, 1.0 / n)
+    rho = np.full(n ** 3, 0.7)
+    g.set("density", rho)
+    for c, s in (("u", (n + 1) * n * n), ("v", n * (n + 1) * n), ("w", n * n * (n + 1))):
+        g.set(c, np.zeros(s))
+    g.move_substances_3D(0.01, fia.advect_params())
+    got = g.get("density")
+    z = np.zeros
+    ref, _ = O.move_substances_3D((n, n, n), 1.0 / n, z((n + 1) * n * n), z(n * (n + 1) * n), z(n * n * (n + 1)),
+                                  rho, 0.01)
+    g.close()
+    assert rel(got, ref) < 1e-12
+    assert np.abs(got - 0.7).max() < 1e-12
+
+
+def test_advect_velocity():
+    g, h, u, v, w, rho, dt = make(12, 12, 12, seed=11, cfl=1.5)
+    g.advect_velocity_xyz_flux_advection_3D(dt, fia.advect_params())
+    got = [g.get(c) for c in "uvw"]
+    ou, ov, ow, _ = O.advect_velocity_3D((12, 12, 12), h, u, v, w, dt)
+    g.close()
+    for a, b in zip(got, (ou, ov, ow)):
+        assert rel(a, b) < 1e-10
+
+
+def test_advect_velocity_linear_no_correction():
+    g, h, u, v, w, rho, dt = make(12, 12, 12, seed=13, cfl=1.5)
+    p = fia.advect_params(interpolation_method="linear", enable_eliminate_zero_velocity_false_diffusion=False)
+    g.advect_velocity_xyz_flux_advection_3D(dt, p)
+    got = [g.get(c) for c in "uvw"]
+    ou, ov, ow, _ = O.advect_velocity_3D((12, 12, 12), h, u, v, w, dt, interp=1, correction=0)
+    g.close()
+    for a, b in zip(got, (ou, ov, ow)):
+        assert rel(a, b) < 1e-10
+
+
+def test_pressure_projection():
+    n = 16
+    h = 1.0 / n
+    rng = np.random.default_rng(3)
+    u = rng.normal(size=(n + 1) * n * n); v = rng.normal(size=n * (n + 1) * n); w = rng.normal(size=n * n * (n + 1))
+    # closed walls: zero normal velocity on the boundary faces
+    u.reshape(n + 1, n, n)[[0, -1]] = 0; v.reshape(n, n + 1, n)[:, [0, -1]] = 0; w.reshape(n, n, n + 1)[:, :, [0, -1]] = 0
+    g = fia.Grid3D(n, n, n, h)
+    for name, a in (("u", u), ("v", v), ("w", w)):
+        g.set(name, a)
+    rep = g.calc_pressure_gradient_term_3D(fia.solver_params(tol=1e-12, max_iter=5000))
+    p = g.get("pressure")
+    b = O.pressure_rhs((n, n, n), h, u, v, w)
+    pref, it, rr = O.pressure_solve((n, n, n), b, tol=1e-13)
+    assert rep.rel_residual <= 1e-12
+    assert rel(p, pref) < 1e-9
+    uu, vv, ww = O.subtract_gradient((n, n, n), h, pref, u, v, w)
+    for name, ref in (("u", uu), ("v", vv), ("w", ww)):
+        assert rel(g.get(name), ref) < 1e-9
+    div = scenes.divergence(n, g.get("u"), g.get("v"), g.get("w"))
+    assert np.abs(div).max() < 1e-9
+    g.close()
+
+
+def test_cfl_reduction_and_mass():
+    g, h, u, v, w, rho, dt = make(10, 12, 14, seed=17)
+    assert g.max_abs_velocity() == pytest.approx(O.max_abs_velocity((10, 12, 14), u, v, w), rel=0, abs=0)
+    assert g.total_mass() == pytest.approx(rho.sum() * h ** 3, rel=1e-13)
+    g.close()
+
+
+def test_invalid_arguments_fail_loudly():
+    g = fia.Grid3D(8, 8, 8, 1.0 / 8)
+    with pytest.raises(fia.FiaError):
+        g.move_substances_3D(0.01, fia.advect_params(use_MacCormack_scheme=True))
+    with pytest.raises(fia.FiaError):
+        g.move_substances_3D(0.01, fia.advect_params(num_gauss_quadrature_point_for_integrate_density=2))
+    with pytest.raises(fia.FiaError):
+        g.set("u", np.zeros(5))
+    g.close()

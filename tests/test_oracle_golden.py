@@ -1,0 +1,110 @@
+"""Pins the CPU oracle against outputs of the reference's own code (tests/golden/*.npz,
+written by tests/golden/make_golden.py from the reference translation units).
+
+The reference clips faces in float even in its double build (facecutter.h:33-34), so the
+oracle (double everywhere) agrees with the double build to float-clip precision
+(~1e-6 relative) and with the float build (the reference as shipped) to ~1e-5, except at
+the y walls where the float build's centroid rounding flips its own quadrature branch.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import Oracle
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+O = Oracle()
+
+
+def load(name):
+    return np.load(os.path.join(GOLD, name))
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+KIND = {0: ("c", 0), 1: ("x", 0), 2: ("y", 0), 3: ("z", 0), 4: ("c", 1), 5: ("x", 1), 6: ("y", 1), 7: ("z", 1),
+        8: ("c", 3), 9: ("x", 2), 10: ("y", 2), 11: ("z", 2)}
+OFF = {"c": (0.5, 0.5, 0.5), "x": (0.0, 0.5, 0.5), "y": (0.5, 0.0, 0.5), "z": (0.5, 0.5, 0.0)}
+
+
+@pytest.mark.parametrize("kind", sorted(KIND))
+def test_interpolation_matches_reference(kind):
+    g = load("interp.npz")
+    N = tuple(int(x) for x in g["N"]); h = float(g["h"])
+    arr, method = KIND[kind]
+    M = [N[d] + (("xyz".index(arr) == d) if arr != "c" else 0) for d in range(3)]
+    got = O.interp(g["a_" + arr], M, OFF[arr], h, method, g["pts"])
+    ref = g["interp_%d_double" % kind]
+    assert np.abs(got - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max())
+    reff = g["interp_%d_float" % kind]
+    assert np.abs(got - reff).max() <= 2e-4 * max(1.0, np.abs(ref).max())
+
+
+@pytest.mark.parametrize("key,mode,k", [("psi_0_3_1", 1, 3), ("psi_0_1_1", 1, 1), ("psi_1_1_1", 2, 1),
+                                        ("psi_3_1_0", 0, 1)])
+def test_psi_matches_reference(key, mode, k):
+    g = load("psi.npz")
+    N = tuple(int(x) for x in g["N"]); h = float(g["h"])
+    got = O.psi(g["rho"], N, (0.5, 0.5, 0.5), h, mode, k)
+    assert np.abs(got - g[key + "_double"]).max() < 1e-13
+    assert np.abs(got - g[key + "_float"]).max() < 1e-5
+
+
+@pytest.mark.parametrize("split,off", [(0, (0.5, 0.5)), (1, (0.0, 0.0)), (2, (0.5, 0.0)), (3, (0.0, 0.5))])
+def test_face_clipping_matches_reference(split, off):
+    g = load("split.npz")
+    h = float(g["h"])
+    tot = []
+    for f in g["faces"]:
+        pc, st = O.split_face(f, h, off)
+        assert st == 0
+        tot.append(np.concatenate([pc[:, 3:].sum(0), (pc[:, :3] * pc[:, 4:5]).sum(0)]) if len(pc) else np.zeros(6))
+    tot = np.array(tot)
+    for prec, tol in (("double", 5e-6), ("float", 5e-5)):
+        ref = g["split_%d_%s_totals" % (split, prec)]
+        assert np.abs(tot - ref).max() / (h * h) < tol
+
+
+@pytest.mark.parametrize("name,args", [
+    ("weno6_integral", (0, 1, 1, 0, (0.5, 0.5))),
+    ("weno6_zero_velocity", (0, 0, 0, 1, (0.5, 0.5))),
+    ("error_1dy_linear", (2, 0, 0, 0, (0.0, 0.0))),
+    ("linear_integral", (1, 2, 1, 0, (0.5, 0.5))),
+])
+def test_density_pass_matches_reference(name, args):
+    g = load("density.npz")
+    N = tuple(int(x) for x in g["N"]); h = float(g["h"]); dt = float(g["dt"])
+    interp, psi, integ, zv, co = args
+    got, st, nf, npoly = O.flux_pass(N, h, g["u"], g["v"], g["w"], -1, g["rho"], dt, interp, psi, integ, zv, co, 3)
+    assert st == 0
+    assert rel(got, g["pass_%s_double" % name]) < 5e-6
+    if name == "weno6_zero_velocity":
+        assert rel(got, g["pass_%s_double" % name]) < 1e-13
+    # the float build: interior cells (the y-wall layers carry its centroid-rounding branch flips)
+    ref = g["pass_%s_float" % name].reshape(N)
+    assert rel(got.reshape(N)[:, 1:-1, :], ref[:, 1:-1, :]) < 2e-5
+
+
+def test_move_substances_matches_reference():
+    g = load("density.npz")
+    N = tuple(int(x) for x in g["N"]); h = float(g["h"]); dt = float(g["dt"])
+    got, st = O.move_substances_3D(N, h, g["u"], g["v"], g["w"], g["rho"], dt)
+    assert st == 0
+    assert rel(got, g["move_substances_double"]) < 5e-6
+    ref = g["move_substances_float"].reshape(N)
+    assert rel(got.reshape(N)[:, 1:-1, :], ref[:, 1:-1, :]) < 2e-5
+
+
+@pytest.mark.parametrize("dim", [0, 1, 2])
+def test_velocity_pass_matches_reference(dim):
+    g = load("velocity.npz")
+    N = tuple(int(x) for x in g["N"]); h = float(g["h"]); dt = float(g["dt"])
+    co = [(0.0, 0.5), (0.5, 0.5), (0.5, 0.0)][dim]
+    f = (g["u"], g["v"], g["w"])[dim]
+    got, st, nf, npoly = O.flux_pass(N, h, g["u"], g["v"], g["w"], dim, f, dt, 1, 2, 1, 0, co, 3)
+    assert st == 0
+    assert rel(got, g["vel_%d_double" % dim]) < 5e-6
+    assert rel(got, g["vel_%d_float" % dim]) < 2e-5
