@@ -247,8 +247,9 @@ __device__ __forceinline__ T piece_flux(const PassDesc& d, const FaceGeom<T>& g,
     if (d.use_integral) {
         // polygon_3D.cpp:257-487 with the grid origin shifted by -h/2 along a staggered axis
         const T oy = (d.comp == 1) ? T(-1) * T(0.5) * h : T(0);
-        const int iy0 = (int)floor((cy - oy) / h);
-        const T f = ((cy - oy) / h) - T(iy0);
+        const T ry = snap_int((cy - oy) / h);
+        const int iy0 = (int)floor(ry);
+        const T f = ry - T(iy0);
         if (f < T(0.5)) {
             const T lo = T(iy0) * h + oy, L = cy - lo;
             for (int q = 0; q < d.k; ++q) {
@@ -330,9 +331,12 @@ __device__ T emit_polygon(const PassDesc& d, const FaceGeom<T>& g, const T* px, 
 }
 
 // Clips one face and returns its flux (sum over pieces of the quadrature terms).
+// `multi` is set when some iso-line crosses a piece more than twice: the piece that holds
+// the first vertex then merges several disjoint parts (facecutter.h:163-181), so the
+// partition depends on the vertex order and the two adjacent cells see different pieces.
 template <typename T>
 __device__ T clip_face(const PassDesc& d, const FaceGeom<T>& g, const T* __restrict__ a,
-                       const T* __restrict__ psi, unsigned& st, int& npieces) {
+                       const T* __restrict__ psi, unsigned& st, int& npieces, bool& multi) {
     const T h = T(d.h);
     CV<T> pool[kPool];
     unsigned char sstart[kMaxStack], snum[kMaxStack], sdim[kMaxStack];
@@ -340,8 +344,8 @@ __device__ T clip_face(const PassDesc& d, const FaceGeom<T>& g, const T* __restr
     const T xi[4] = {T(0), T(1), T(1), T(0)}, eta[4] = {T(0), T(0), T(1), T(1)};
     for (int q = 0; q < 4; ++q) {
         pool[q].p0 = xi[q]; pool[q].p1 = eta[q];
-        pool[q].c0 = g.x[q] / h - T(d.color_off[0]);
-        pool[q].c1 = g.z[q] / h - T(d.color_off[1]);
+        pool[q].c0 = snap_int(g.x[q] / h - T(d.color_off[0]));
+        pool[q].c1 = snap_int(g.z[q] / h - T(d.color_off[1]));
     }
     sstart[0] = 0; snum[0] = 4; sdim[0] = 0; sp = 1;
     T F = T(0);
@@ -376,7 +380,7 @@ __device__ T clip_face(const PassDesc& d, const FaceGeom<T>& g, const T* __restr
                     CV<T> X;
                     X.p0 = t0 * poly[n].p0 + t1 * poly[m].p0;
                     X.p1 = t0 * poly[n].p1 + t1 * poly[m].p1;
-                    const T other = t0 * cv_c(poly[n], 1 - dim) + t1 * cv_c(poly[m], 1 - dim);
+                    const T other = snap_int(t0 * cv_c(poly[n], 1 - dim) + t1 * cv_c(poly[m], 1 - dim));
                     if (dim == 0) { X.c0 = iso; X.c1 = other; } else { X.c1 = iso; X.c0 = other; }
                     if (slot == 0) {
                         tmp0[h0++] = X;
@@ -398,6 +402,7 @@ __device__ T clip_face(const PassDesc& d, const FaceGeom<T>& g, const T* __restr
                 if (h0 >= kMaxVerts || h1 >= kMaxVerts || p1start + h1 + 2 >= kPool) bad = true;
             }
             if (bad) { st |= ST_CLIP_OVERFLOW; top = pstart; continue; }
+            if (nchild > 1) multi = true;
             if (cut) {
                 if (slot != 0) { st |= ST_CLIP_ODD_CUT; top = pstart; continue; }
                 if (wpos + h0 >= kPool || sp + nchild + 1 > kMaxStack) { st |= ST_CLIP_OVERFLOW; top = pstart; continue; }
@@ -455,13 +460,13 @@ __device__ __forceinline__ void face_corners(int fam, int i, int j, int k, int* 
 template <typename T>
 __global__ void __launch_bounds__(128) k_faces(PassDesc d, int fam, const T* __restrict__ a,
                                                const T* __restrict__ psi, const T* __restrict__ verts,
-                                               T* __restrict__ flux, unsigned* status,
-                                               unsigned long long* counters) {
+                                               T* __restrict__ flux, T* __restrict__ flux_rev,
+                                               unsigned* status, unsigned long long* counters) {
     const int Fx = d.A.Mx + (fam == 0), Fy = d.A.My + (fam == 1), Fz = d.A.Mz + (fam == 2);
     const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long nface = (long long)Fx * Fy * Fz;
     unsigned st = 0;
-    int npieces = 0;
+    int npieces = 0, nmulti = 0;
     if (id < nface) {
         const int k = (int)(id % Fz);
         const int j = (int)((id / Fz) % Fy);
@@ -480,28 +485,46 @@ __global__ void __launch_bounds__(128) k_faces(PassDesc d, int fam, const T* __r
                 g.x[q] = verts[3 * vid]; g.y[q] = verts[3 * vid + 1]; g.z[q] = verts[3 * vid + 2];
             }
         }
-        T F = clip_face(d, g, a, psi, st, npieces);
-        if (!isfinite(F)) st |= ST_NONFINITE;
+        bool multi = false;
+        const T F = clip_face(d, g, a, psi, st, npieces, multi);
+        T Fr = -F;
+        if (multi) {
+            // the upper cell's own face: vertex order (v0, v3, v2, v1), which is the reference's
+            // x-/y-/z- face order (backtrace_..._for_integrate_density.cpp:77-112)
+            FaceGeom<T> r = g;
+            r.x[1] = g.x[3]; r.y[1] = g.y[3]; r.z[1] = g.z[3];
+            r.x[3] = g.x[1]; r.y[3] = g.y[1]; r.z[3] = g.z[1];
+            int np2 = 0; bool m2 = false;
+            Fr = clip_face(d, r, a, psi, st, np2, m2);
+            ++nmulti;
+        }
+        if (!isfinite(F) || !isfinite(Fr)) st |= ST_NONFINITE;
         flux[id] = F;
+        flux_rev[id] = Fr;
     }
     // warp-aggregated counters and status
     unsigned long long pc = (unsigned long long)npieces;
-    unsigned fc = id < nface ? 1u : 0u;
+    unsigned fc = id < nface ? 1u : 0u, mc = (unsigned)nmulti;
     for (int o = 16; o > 0; o >>= 1) {
         pc += __shfl_down_sync(0xffffffffu, pc, o);
         fc += __shfl_down_sync(0xffffffffu, fc, o);
+        mc += __shfl_down_sync(0xffffffffu, mc, o);
         st |= __shfl_down_sync(0xffffffffu, st, o);
     }
     if ((threadIdx.x & 31) == 0) {
         if (fc) { atomicAdd(&counters[0], (unsigned long long)fc); atomicAdd(&counters[1], pc); }
+        if (mc) atomicAdd(&counters[2], (unsigned long long)mc);
         if (st) atomicOr(status, st);
     }
 }
 
-// rho'(i,j,k) = (Fx(i+1)-Fx(i) + Fy(j+1)-Fy(j) + Fz(k+1)-Fz(k)) / V
+// rho'(i,j,k) = (Fx(i+1) + Rx(i) + Fy(j+1) + Ry(j) + Fz(k+1) + Rz(k)) / V, where F is the
+// flux of a face as the lower cell's face and R as the upper cell's (R = -F unless the
+// clip partition depends on the vertex order).
 template <typename T>
 __global__ void k_gather(PassDesc d, const T* __restrict__ fx, const T* __restrict__ fy,
-                         const T* __restrict__ fz, const T* __restrict__ in, T* __restrict__ out, int mode) {
+                         const T* __restrict__ fz, const T* __restrict__ rx, const T* __restrict__ ry,
+                         const T* __restrict__ rz, const T* __restrict__ in, T* __restrict__ out, int mode) {
     const int Mx = d.A.Mx, My = d.A.My, Mz = d.A.Mz;
     const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= (long long)Mx * My * Mz) return;
@@ -515,7 +538,7 @@ __global__ void k_gather(PassDesc d, const T* __restrict__ fx, const T* __restri
     const long long iy0 = ((long long)i * (My + 1) + j) * Mz + k;       // Mx x (My+1) x Mz
     const long long iy1 = ((long long)i * (My + 1) + j + 1) * Mz + k;
     const long long iz0 = ((long long)i * My + j) * (Mz + 1) + k;       // Mx x My x (Mz+1)
-    const T s = ((fx[ix1] - fx[ix0]) + (fy[iy1] - fy[iy0])) + (fz[iz0 + 1] - fz[iz0]);
+    const T s = ((fx[ix1] + rx[ix0]) + (fy[iy1] + ry[iy0])) + (fz[iz0 + 1] + rz[iz0]);
     const T val = s / V;
     if (mode == 0) out[id] = val;
     else if (mode == 1) out[id] = in[id] - val;
@@ -546,7 +569,10 @@ template <typename T>
 cudaError_t launch_faces(const PassDesc& d, const T* a, const PassWork<T>& w, cudaStream_t s) {
     for (int fam = 0; fam < 3; ++fam) {
         const long long n = (long long)(d.A.Mx + (fam == 0)) * (d.A.My + (fam == 1)) * (d.A.Mz + (fam == 2));
-        k_faces<T><<<blocks_for(n, 128), 128, 0, s>>>(d, fam, a, w.psi, w.verts, w.flux[fam], w.status, w.counters);
+        prof_mark(w, 0, s);
+        k_faces<T><<<blocks_for(n, 128), 128, 0, s>>>(d, fam, a, w.psi, w.verts, w.flux[fam], w.flux_rev[fam],
+                                                      w.status, w.counters);
+        prof_mark(w, 1, s);
     }
     return cudaGetLastError();
 }
@@ -554,7 +580,8 @@ cudaError_t launch_faces(const PassDesc& d, const T* a, const PassWork<T>& w, cu
 template <typename T>
 cudaError_t launch_gather(const PassDesc& d, const PassWork<T>& w, const T* in, T* out, int mode, cudaStream_t s) {
     const long long n = (long long)d.A.Mx * d.A.My * d.A.Mz;
-    k_gather<T><<<blocks_for(n, 256), 256, 0, s>>>(d, w.flux[0], w.flux[1], w.flux[2], in, out, mode);
+    k_gather<T><<<blocks_for(n, 256), 256, 0, s>>>(d, w.flux[0], w.flux[1], w.flux[2], w.flux_rev[0],
+                                                   w.flux_rev[1], w.flux_rev[2], in, out, mode);
     return cudaGetLastError();
 }
 

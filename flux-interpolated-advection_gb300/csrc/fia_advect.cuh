@@ -41,10 +41,23 @@ template <typename T>
 struct PassWork {
     T* psi;            // P.Mx*P.My*P.Mz
     T* verts;          // 3 * (A.Mx+1)(A.My+1)(A.Mz+1)  backtraced vertex positions
-    T* flux[3];        // per face family: (Mx+1)MyMz, Mx(My+1)Mz, MxMy(Mz+1)
+    T* flux[3];        // per face family: (Mx+1)MyMz, Mx(My+1)Mz, MxMy(Mz+1); lower cell's view
+    T* flux_rev[3];    // the same faces seen from the upper cell (its own clip when needed)
     unsigned* status;  // one word
-    unsigned long long* counters;  // [0] faces visited, [1] pieces emitted
+    unsigned long long* counters;  // [0] faces, [1] pieces, [2] faces clipped twice, [3] WENO6 evaluations
+    // optional timing of the face kernels: an event pair is recorded around each launch
+    cudaEvent_t* prof_ev;   // 2 * prof_cap events, or null
+    int* prof_n;            // pairs recorded so far
+    int prof_cap;
 };
+
+// records the opening / closing event of a timed face-kernel launch
+template <typename T>
+inline void prof_mark(const PassWork<T>& w, int closing, cudaStream_t s) {
+    if (!w.prof_ev || *w.prof_n >= w.prof_cap) return;
+    cudaEventRecord(w.prof_ev[2 * *w.prof_n + closing], s);
+    if (closing) ++*w.prof_n;
+}
 
 struct VelocityFields {
     const void* u; const void* v; const void* w;   // T* on the device
@@ -70,5 +83,16 @@ cudaError_t launch_gather(const PassDesc& d, const PassWork<T>& w, const T* in, 
 template <typename T>
 cudaError_t run_pass(const PassDesc& d, const VelocityFields& vel, const T* a, const PassWork<T>& w,
                      const T* in, T* out, int mode, cudaStream_t s);
+
+// The chosen form (fia_advect32.cu): FP32 in local cell coordinates; psi is stored as
+// (hi, lo) float pairs in cell units, fluxes as (flux, y-normal sum) float pairs, vertex
+// displacements in cells.
+template <>
+cudaError_t run_pass<float>(const PassDesc& d, const VelocityFields& vel, const float* a, const PassWork<float>& w,
+                            const float* in, float* out, int mode, cudaStream_t s);
+template <>
+cudaError_t launch_psi<float>(const PassDesc& d, const float* a, float* psi, cudaStream_t s);
+template <>
+cudaError_t launch_backtrace<float>(const PassDesc& d, const VelocityFields& vel, float* verts, cudaStream_t s);
 
 }  // namespace fia

@@ -1,0 +1,507 @@
+// fia_advect32.cu -- the chosen form of the flux pass: FP32 arithmetic in local cell
+// coordinates, double-float psi, compensated face and cell sums.
+//
+// Same kernels as fia_advect.cu (psi column scan, unique-vertex backtrace, unique-face
+// clip + quadrature + WENO6, deterministic gather), with these differences:
+//  * all geometry is in cell units relative to an integer anchor (fia_local.cuh);
+//  * psi is stored as (hi, lo) float pairs in cell units;
+//  * a face interpolates psi - Psi0(f), Psi0(f) = the psi node at the face's anchor, and
+//    stores (Ft, Ny): the compensated flux of psi - Psi0 plus the density terms, and the
+//    sum of the pieces' scaled y-normals;
+//  * the gather forms, per cell c with base node Psi_c,
+//        rho' = sum_f s_f [ Ft(f) + (Psi0(f) - Psi_c) Ny(f) ],
+//    which equals sum_f s_f F(f) - Psi_c sum_f s_f Ny(f); the last sum is the y-component
+//    of the vector area of the closed surface of the backtraced cell, zero in exact
+//    arithmetic, and is dropped so that no O(psi) term survives in FP32.
+#include "fia_advect.cuh"
+#include "fia_local.cuh"
+
+namespace fia {
+
+namespace {
+
+// ---------------------------------------------------------------------------------
+// psi (cell units) as hi/lo pairs, one thread per (x,z) column
+// ---------------------------------------------------------------------------------
+__global__ void k_psi32(PassDesc d, const float* __restrict__ a, float2* __restrict__ psi) {
+    const int Mx = d.A.Mx, My = d.A.My, Mz = d.A.Mz;
+    const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= (long long)Mx * Mz) return;
+    const int i = (int)(col / Mz), k = (int)(col % Mz);
+    const PlainLoad L{a};
+    float hi = 0.f, lo = 0.f;
+    psi[idx3(d.P, i, 0, k)] = make_float2(0.f, 0.f);
+    const float oy = (float)d.A.oy;
+    for (int j = 1; j <= My; ++j) {
+        Kahan inc;
+        if (d.psi_mode == PSI_PLAIN) {
+            inc.add(__ldg(a + idx3(d.A, i, j - 1, k)));
+        } else if (d.psi_mode == PSI_WENO6) {
+            // cell j-1 spans [j-1+oy-.5, j+oy-.5] in cells; anchor (i, j-1, k)
+            const int anc[3] = {i, j - 1, k};
+            for (int half = 0; half < 2; ++half) {
+                const float lo_y = (oy - 0.5f) + 0.5f * float(half);
+                for (int q = 0; q < d.k; ++q) {
+                    const float qq[3] = {(float)d.A.ox, lo_y + 0.25f * (1.0f + (float)d.gx[q]), (float)d.A.oz};
+                    inc.add(weno6_1dy_loc(L, d.A, anc, qq) * 0.5f * (float)d.gw[q]);
+                }
+            }
+        } else {
+            const int anc[3] = {i, j - 1, k};
+            const float q0[3] = {(float)d.A.ox, 0.25f + oy - 0.5f, (float)d.A.oz};
+            const float q1[3] = {(float)d.A.ox, 0.75f + oy - 0.5f, (float)d.A.oz};
+            inc.add(lin3d_loc(L, d.A, anc, q0) * 0.5f);
+            inc.add(lin3d_loc(L, d.A, anc, q1) * 0.5f);
+        }
+        // (hi, lo) += inc
+        float s, e;
+        two_sum(hi, inc.s, s, e);
+        e += lo + inc.c;
+        two_sum(s, e, hi, lo);
+        psi[idx3(d.P, i, j, k)] = make_float2(hi, lo);
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// backtrace: displacement in cells of every unique vertex, clamped to the domain
+// ---------------------------------------------------------------------------------
+__global__ void k_backtrace32(PassDesc d, const float* __restrict__ u, const float* __restrict__ v,
+                              const float* __restrict__ w, NodeField fu, NodeField fv, NodeField fw,
+                              float* __restrict__ disp) {
+    const int Lx = d.A.Mx + 1, Ly = d.A.My + 1, Lz = d.A.Mz + 1;
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= (long long)Lx * Ly * Lz) return;
+    const int k = (int)(id % Lz);
+    const int j = (int)((id / Lz) % Ly);
+    const int i = (int)(id / ((long long)Lz * Ly));
+    const int anc[3] = {i, j, k};
+    float q[3] = {0.f, 0.f, 0.f};
+    if (d.comp >= 0) q[d.comp] = -0.5f;
+    float dx[3] = {0.f, 0.f, 0.f};
+    bool pinned = false;
+    if (d.comp >= 0) {
+        const int vi = anc[d.comp];
+        pinned = (vi <= 1 || vi >= d.N[d.comp]);
+    }
+    if (!pinned) {
+        // dt/h converts the velocity to cells per step
+        const float s = (float)(d.dt / d.h);
+        dx[0] = -interp_loc(d.interp, PlainLoad{u}, fu, anc, q) * s;
+        dx[1] = -interp_loc(d.interp, PlainLoad{v}, fv, anc, q) * s;
+        dx[2] = -interp_loc(d.interp, PlainLoad{w}, fw, anc, q) * s;
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float e = (c == d.comp) ? 0.5f : 0.f;
+        const float rest = float(anc[c]) + q[c];          // exact (small integers and halves)
+        const float lo = -e, hi = float(d.N[c]) + e;
+        if (rest + dx[c] < lo) dx[c] = lo - rest;
+        if (rest + dx[c] > hi) dx[c] = hi - rest;
+    }
+    disp[3 * id + 0] = dx[0]; disp[3 * id + 1] = dx[1]; disp[3 * id + 2] = dx[2];
+}
+
+// ---------------------------------------------------------------------------------
+// faces
+// ---------------------------------------------------------------------------------
+struct CVf { float p0, p1, c0, c1; };
+__device__ __forceinline__ float cvc(const CVf& v, int dim) { return dim ? v.c1 : v.c0; }
+
+__device__ __forceinline__ float bilinf(const float* v, float xi, float eta) {
+    const float a = v[1] - v[0], b = v[3] - v[0], c = (v[0] - v[1]) + (v[2] - v[3]);
+    return v[0] + xi * a + eta * b + (xi * eta) * c;
+}
+
+struct LocalFace {
+    int anc[3];          // lattice index of vertex 0
+    float x[4], y[4], z[4];   // vertex positions in cells relative to the anchor
+};
+
+struct FaceOut { Kahan F; Kahan Ny; int evals = 0; };   // evals: point interpolations made
+
+__device__ __forceinline__ void centroidf(const float* px, const float* py, int num, float& cx, float& cy, float& area) {
+    float a = 0.f, sx = 0.f, sy = 0.f;
+    for (int n = 0; n < num; ++n) {
+        const int m = (n + 1 == num) ? 0 : n + 1;
+        const float c = px[n] * py[m] - px[m] * py[n];
+        a += c; sx += c * (px[n] + px[m]); sy += c * (py[n] + py[m]);
+    }
+    a = fabsf(0.5f * a);
+    if (a != 0.f) { const float s = 1.0f / (6.0f * a); cx = sx * s; cy = sy * s; }
+    else {
+        sx = 0.f; sy = 0.f;
+        for (int n = 0; n < num; ++n) { sx += px[n]; sy += py[n]; }
+        cx = sx / float(num); cy = sy / float(num);
+    }
+    area = a;
+}
+
+__device__ void piece32(const PassDesc& d, const LocalFace& g, const float* px, const float* py, int num,
+                        float cxi, float ceta, const float* __restrict__ a, const float2* __restrict__ psi,
+                        const PsiLoad& pl, FaceOut& out) {
+    const float cx = bilinf(g.x, cxi, ceta), cy = bilinf(g.y, cxi, ceta), cz = bilinf(g.z, cxi, ceta);
+    float ny;
+    if (num == 3) {
+        const float x0 = bilinf(g.x, px[0], py[0]), z0 = bilinf(g.z, px[0], py[0]);
+        const float ax = bilinf(g.x, px[1], py[1]) - x0, az = bilinf(g.z, px[1], py[1]) - z0;
+        const float bx = bilinf(g.x, px[2], py[2]) - x0, bz = bilinf(g.z, px[2], py[2]) - z0;
+        ny = 0.5f * (az * bx - ax * bz);
+    } else {
+        float acc = 0.f;
+        float x0 = bilinf(g.x, px[0], py[0]) - cx, z0 = bilinf(g.z, px[0], py[0]) - cz;
+        const float xs = x0, zs = z0;
+        for (int n = 0; n < num; ++n) {
+            float x1, z1;
+            if (n + 1 == num) { x1 = xs; z1 = zs; }
+            else { x1 = bilinf(g.x, px[n + 1], py[n + 1]) - cx; z1 = bilinf(g.z, px[n + 1], py[n + 1]) - cz; }
+            acc += z0 * x1 - x0 * z1;
+            x0 = x1; z0 = z1;
+        }
+        ny = acc * 0.5f;
+    }
+    if (ny == 0.f) return;
+    out.Ny.add(ny);
+    if (d.interp == INTERP_WENO6)   // WENO6 3D evaluations (the unit of the roofline count)
+        out.evals += d.use_integral ? 1 + d.k * (1 + (int)(snap_int(cy - (d.comp == 1 ? -0.5f : 0.f)) -
+                                                           floorf(snap_int(cy - (d.comp == 1 ? -0.5f : 0.f))) >= 0.5f))
+                                    : 1;
+    const PlainLoad al{a};
+    if (d.use_integral) {
+        const float oy = (d.comp == 1) ? -0.5f : 0.f;
+        const float r = snap_int(cy - oy);
+        const float fl = floorf(r);
+        const float f = r - fl;
+        const float ylo = fl + oy;   // local y of the y-face below the centroid
+        if (f < 0.5f) {
+            const float L = cy - ylo;
+            for (int q = 0; q < d.k; ++q) {
+                const float qq[3] = {cx, (L * 0.5f) * (float)d.gx[q] + (L * 0.5f) + ylo, cz};
+                out.F.add(interp_loc(d.interp, al, d.A, g.anc, qq) * (ny * f * (float)d.gw[q]));
+            }
+        } else {
+            float lo = ylo, L = 0.5f;
+            for (int q = 0; q < d.k; ++q) {
+                const float qq[3] = {cx, (L * 0.5f) * (float)d.gx[q] + (L * 0.5f) + lo, cz};
+                out.F.add(interp_loc(d.interp, al, d.A, g.anc, qq) * (ny * 0.5f * (float)d.gw[q]));
+            }
+            lo = ylo + 0.5f; L = cy - lo;
+            for (int q = 0; q < d.k; ++q) {
+                const float qq[3] = {cx, (L * 0.5f) * (float)d.gx[q] + (L * 0.5f) + lo, cz};
+                out.F.add(interp_loc(d.interp, al, d.A, g.anc, qq) * (ny * (f - 0.5f) * (float)d.gw[q]));
+            }
+        }
+        const float qp[3] = {cx, ylo, cz};
+        out.F.add(interp_loc(d.interp, pl, d.P, g.anc, qp) * ny);
+    } else {
+        const float qp[3] = {cx, cy, cz};
+        out.F.add(interp_loc(d.interp, pl, d.P, g.anc, qp) * ny);
+    }
+}
+
+__device__ void emit32(const PassDesc& d, const LocalFace& g, const float* px, const float* py, int num,
+                       const float* a, const float2* psi, const PsiLoad& pl, unsigned& st, int& npieces,
+                       FaceOut& out) {
+    float cx, cy, area;
+    centroidf(px, py, num, cx, cy, area);
+    const float minA = (float)d.minimal_area;
+    if (!(area > minA)) {
+        if (area != 0.f) { ++npieces; piece32(d, g, px, py, num, cx, cy, a, psi, pl, out); }
+        return;
+    }
+    float tri[24][6];
+    int top = 0;
+    if (num == 3) {
+        tri[0][0] = px[0]; tri[0][1] = py[0]; tri[0][2] = px[1]; tri[0][3] = py[1]; tri[0][4] = px[2]; tri[0][5] = py[2];
+        top = 1;
+    } else {
+        for (int n = num - 1; n >= 0; --n) {
+            const int m = (n + 1 == num) ? 0 : n + 1;
+            if (top >= 24) { st |= ST_SUBDIV_OVERFLOW; return; }
+            tri[top][0] = cx; tri[top][1] = cy; tri[top][2] = px[n]; tri[top][3] = py[n];
+            tri[top][4] = px[m]; tri[top][5] = py[m]; ++top;
+        }
+    }
+    while (top > 0) {
+        --top;
+        float tx[3] = {tri[top][0], tri[top][2], tri[top][4]};
+        float ty[3] = {tri[top][1], tri[top][3], tri[top][5]};
+        float tcx, tcy, ta;
+        centroidf(tx, ty, 3, tcx, tcy, ta);
+        if (ta > minA) {
+            int mi = 0; float ml = -1.f;
+            for (int n = 0; n < 3; ++n) {
+                const int m = (n + 1) % 3;
+                const float len = (tx[n] - tx[m]) * (tx[n] - tx[m]) + (ty[n] - ty[m]) * (ty[n] - ty[m]);
+                if (ml < len) { ml = len; mi = n; }
+            }
+            const int i1 = (mi + 1) % 3, i2 = (mi + 2) % 3;
+            const float mx = 0.5f * (tx[mi] + tx[i1]), my = 0.5f * (ty[mi] + ty[i1]);
+            if (top + 2 > 24) { st |= ST_SUBDIV_OVERFLOW; return; }
+            tri[top][0] = mx; tri[top][1] = my; tri[top][2] = tx[i1]; tri[top][3] = ty[i1]; tri[top][4] = tx[i2]; tri[top][5] = ty[i2]; ++top;
+            tri[top][0] = tx[mi]; tri[top][1] = ty[mi]; tri[top][2] = mx; tri[top][3] = my; tri[top][4] = tx[i2]; tri[top][5] = ty[i2]; ++top;
+        } else if (ta != 0.f) {
+            ++npieces;
+            piece32(d, g, tx, ty, 3, tcx, tcy, a, psi, pl, out);
+        }
+    }
+}
+
+constexpr int kPool32 = 144, kMaxV32 = 32, kStack32 = 48;
+
+// The clipper of fia_advect.cu (facecutter.h:59-224) on local colours.
+__device__ void clip32(const PassDesc& d, const LocalFace& g, const float* a, const float2* psi, const PsiLoad& pl,
+                       unsigned& st, int& npieces, bool& multi, FaceOut& out) {
+    CVf pool[kPool32];
+    unsigned char sstart[kStack32], snum[kStack32], sdim[kStack32];
+    const float xi[4] = {0.f, 1.f, 1.f, 0.f}, eta[4] = {0.f, 0.f, 1.f, 1.f};
+    for (int q = 0; q < 4; ++q) {
+        pool[q].p0 = xi[q]; pool[q].p1 = eta[q];
+        pool[q].c0 = snap_int(g.x[q] - (float)d.color_off[0]);
+        pool[q].c1 = snap_int(g.z[q] - (float)d.color_off[1]);
+    }
+    sstart[0] = 0; snum[0] = 4; sdim[0] = 0;
+    int sp = 1;
+    CVf tmp0[kMaxV32 + 2];
+    while (sp > 0) {
+        --sp;
+        const int pstart = sstart[sp], num = snum[sp], dim = sdim[sp];
+        const CVf* poly = pool + pstart;
+        float mn = cvc(poly[0], dim), mx = mn;
+        for (int n = 1; n < num; ++n) { const float c = cvc(poly[n], dim); mn = fminf(mn, c); mx = fmaxf(mx, c); }
+        int start = (int)ceilf(mn), end = (int)floorf(mx);
+        if (mn - float(start) == 0.f) start += 1;
+        if (mx - float(end) == 0.f) end -= 1;
+        bool cut = false;
+        if (start <= end) {
+            if (pstart + 3 * num + 2 > kPool32) { st |= ST_CLIP_OVERFLOW; continue; }
+            const float iso = float(start);
+            int h0 = 0, h1 = 0, slot = 0, wpos = pstart + num, p1start = wpos, nchild = 0;
+            unsigned char cst[kStack32], cnum[kStack32];
+            tmp0[h0++] = poly[0];
+            bool bad = false;
+            for (int n = 0; n < num && !bad; ++n) {
+                const int m = (n + 1 == num) ? 0 : n + 1;
+                const float v0 = cvc(poly[n], dim) - iso, v1 = cvc(poly[m], dim) - iso;
+                if ((v0 < 0.f) != (v1 < 0.f)) {
+                    const float inv = 1.0f / (v1 - v0);
+                    const float t0 = v1 * inv, t1 = -v0 * inv;
+                    cut = true;
+                    CVf X;
+                    X.p0 = t0 * poly[n].p0 + t1 * poly[m].p0;
+                    X.p1 = t0 * poly[n].p1 + t1 * poly[m].p1;
+                    const float other = snap_int(t0 * cvc(poly[n], 1 - dim) + t1 * cvc(poly[m], 1 - dim));
+                    if (dim == 0) { X.c0 = iso; X.c1 = other; } else { X.c1 = iso; X.c0 = other; }
+                    if (slot == 0) {
+                        tmp0[h0++] = X;
+                        slot = 1; h1 = 0; p1start = wpos;
+                        if (t1 < 1.0f) pool[p1start + h1++] = X;
+                    } else {
+                        pool[p1start + h1++] = X;
+                        if (nchild >= kStack32 - 1) { bad = true; break; }
+                        cst[nchild] = (unsigned char)p1start; cnum[nchild] = (unsigned char)h1; ++nchild;
+                        wpos = p1start + h1;
+                        slot = 0;
+                        if (t1 < 1.0f) tmp0[h0++] = X;
+                    }
+                }
+                if (n < num - 1) {
+                    if (slot == 0) tmp0[h0++] = poly[m];
+                    else pool[p1start + h1++] = poly[m];
+                }
+                if (h0 >= kMaxV32 || h1 >= kMaxV32 || p1start + h1 + 2 >= kPool32) bad = true;
+            }
+            if (bad) { st |= ST_CLIP_OVERFLOW; continue; }
+            if (nchild > 1) multi = true;
+            if (cut) {
+                if (slot != 0) { st |= ST_CLIP_ODD_CUT; continue; }
+                if (wpos + h0 >= kPool32 || sp + nchild + 1 > kStack32) { st |= ST_CLIP_OVERFLOW; continue; }
+                for (int q = 0; q < h0; ++q) pool[wpos + q] = tmp0[q];
+                const int src = pstart + num, len = wpos + h0 - src;
+                for (int q = 0; q < len; ++q) pool[pstart + q] = pool[src + q];
+                for (int c = 0; c < nchild; ++c) {
+                    sstart[sp] = (unsigned char)(cst[c] - num); snum[sp] = cnum[c]; sdim[sp] = (unsigned char)dim; ++sp;
+                }
+                sstart[sp] = (unsigned char)(wpos - num); snum[sp] = (unsigned char)h0; sdim[sp] = (unsigned char)dim; ++sp;
+            }
+        }
+        if (!cut) {
+            if (dim == 0) {
+                sstart[sp] = (unsigned char)pstart; snum[sp] = (unsigned char)num; sdim[sp] = 1; ++sp;
+            } else if (num >= 3) {
+                float px[kMaxV32], py[kMaxV32];
+                for (int q = 0; q < num; ++q) { px[q] = poly[q].p0; py[q] = poly[q].p1; }
+                emit32(d, g, px, py, num, a, psi, pl, st, npieces, out);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void corners(int fam, int i, int j, int k, int* ci, int* cj, int* ck) {
+    if (fam == 0) {
+        ci[0] = i; cj[0] = j; ck[0] = k;   ci[1] = i; cj[1] = j + 1; ck[1] = k;
+        ci[2] = i; cj[2] = j + 1; ck[2] = k + 1;   ci[3] = i; cj[3] = j; ck[3] = k + 1;
+    } else if (fam == 1) {
+        ci[0] = i; cj[0] = j; ck[0] = k;   ci[1] = i; cj[1] = j; ck[1] = k + 1;
+        ci[2] = i + 1; cj[2] = j; ck[2] = k + 1;   ci[3] = i + 1; cj[3] = j; ck[3] = k;
+    } else {
+        ci[0] = i; cj[0] = j; ck[0] = k;   ci[1] = i + 1; cj[1] = j; ck[1] = k;
+        ci[2] = i + 1; cj[2] = j + 1; ck[2] = k;   ci[3] = i; cj[3] = j + 1; ck[3] = k;
+    }
+}
+
+// psi base node of a face / cell anchored at (i,j,k), clamped into the psi array
+__device__ __forceinline__ long long psi_node(const NodeField& P, int i, int j, int k) {
+    return idx3(P, clampi(i, P.Mx - 1), clampi(j, P.My - 1), clampi(k, P.Mz - 1));
+}
+
+__global__ void __launch_bounds__(128) k_faces32(PassDesc d, int fam, const float* __restrict__ a,
+                                                 const float2* __restrict__ psi, const float* __restrict__ disp,
+                                                 float2* __restrict__ flux, float2* __restrict__ flux_rev,
+                                                 unsigned* status, unsigned long long* counters) {
+    const int Fx = d.A.Mx + (fam == 0), Fy = d.A.My + (fam == 1), Fz = d.A.Mz + (fam == 2);
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long nface = (long long)Fx * Fy * Fz;
+    unsigned st = 0;
+    int npieces = 0, nmulti = 0, nevals = 0;
+    if (id < nface) {
+        const int k = (int)(id % Fz);
+        const int j = (int)((id / Fz) % Fy);
+        const int i = (int)(id / ((long long)Fz * Fy));
+        int ci[4], cj[4], ck[4];
+        corners(fam, i, j, k, ci, cj, ck);
+        LocalFace g;
+        g.anc[0] = i; g.anc[1] = j; g.anc[2] = k;
+        const int Ly = d.A.My + 1, Lz = d.A.Mz + 1;
+        const float sx = d.comp == 0 ? -0.5f : 0.f, sy = d.comp == 1 ? -0.5f : 0.f, sz = d.comp == 2 ? -0.5f : 0.f;
+        for (int q = 0; q < 4; ++q) {
+            float dx = 0.f, dy = 0.f, dz = 0.f;
+            if (!d.zero_velocity) {
+                const long long vid = ((long long)ci[q] * Ly + cj[q]) * Lz + ck[q];
+                dx = disp[3 * vid]; dy = disp[3 * vid + 1]; dz = disp[3 * vid + 2];
+            }
+            g.x[q] = float(ci[q] - i) + sx + dx;
+            g.y[q] = float(cj[q] - j) + sy + dy;
+            g.z[q] = float(ck[q] - k) + sz + dz;
+        }
+        const float2 b = __ldg(psi + psi_node(d.P, i, j, k));
+        const PsiLoad pl{psi, b.x, b.y};
+        FaceOut o;
+        bool multi = false;
+        clip32(d, g, a, psi, pl, st, npieces, multi, o);
+        const float F = o.F.value(), N = o.Ny.value();
+        float Fr = -F, Nr = -N;
+        if (multi) {
+            LocalFace r = g;
+            r.x[1] = g.x[3]; r.y[1] = g.y[3]; r.z[1] = g.z[3];
+            r.x[3] = g.x[1]; r.y[3] = g.y[1]; r.z[3] = g.z[1];
+            FaceOut o2;
+            int np2 = 0; bool m2 = false;
+            clip32(d, r, a, psi, pl, st, np2, m2, o2);
+            Fr = o2.F.value(); Nr = o2.Ny.value();
+            ++nmulti;
+            nevals += o2.evals;
+        }
+        nevals += o.evals;
+        if (!isfinite(F) || !isfinite(Fr)) st |= ST_NONFINITE;
+        flux[id] = make_float2(F, N);
+        flux_rev[id] = make_float2(Fr, Nr);
+    }
+    unsigned long long pc = (unsigned long long)npieces, ec = (unsigned long long)nevals;
+    unsigned fc = id < nface ? 1u : 0u, mc = (unsigned)nmulti;
+    for (int o = 16; o > 0; o >>= 1) {
+        pc += __shfl_down_sync(0xffffffffu, pc, o);
+        ec += __shfl_down_sync(0xffffffffu, ec, o);
+        fc += __shfl_down_sync(0xffffffffu, fc, o);
+        mc += __shfl_down_sync(0xffffffffu, mc, o);
+        st |= __shfl_down_sync(0xffffffffu, st, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (fc) { atomicAdd(&counters[0], (unsigned long long)fc); atomicAdd(&counters[1], pc); }
+        if (mc) atomicAdd(&counters[2], (unsigned long long)mc);
+        if (ec) atomicAdd(&counters[3], ec);
+        if (st) atomicOr(status, st);
+    }
+}
+
+// rho'(c) = sum_f s_f [Ft + (Psi0(f) - Psi_c) Ny], compensated
+__global__ void k_gather32(PassDesc d, const float2* __restrict__ fx, const float2* __restrict__ fy,
+                           const float2* __restrict__ fz, const float2* __restrict__ rx,
+                           const float2* __restrict__ ry, const float2* __restrict__ rz,
+                           const float2* __restrict__ psi, const float* __restrict__ in, float* __restrict__ out,
+                           int mode) {
+    const int Mx = d.A.Mx, My = d.A.My, Mz = d.A.Mz;
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= (long long)Mx * My * Mz) return;
+    const int k = (int)(id % Mz);
+    const int j = (int)((id / Mz) % My);
+    const int i = (int)(id / ((long long)Mz * My));
+    const float2 pc = __ldg(psi + psi_node(d.P, i, j, k));
+    auto base_diff = [&](int a, int b, int c) {
+        const float2 p = __ldg(psi + psi_node(d.P, a, b, c));
+        return (p.x - pc.x) + (p.y - pc.y);
+    };
+    // lower faces (anchor = the cell itself): base difference 0
+    const float2 lx = rx[((long long)i * My + j) * Mz + k];
+    const float2 ly = ry[((long long)i * (My + 1) + j) * Mz + k];
+    const float2 lz = rz[((long long)i * My + j) * (Mz + 1) + k];
+    const float2 ux = fx[((long long)(i + 1) * My + j) * Mz + k];
+    const float2 uy = fy[((long long)i * (My + 1) + j + 1) * Mz + k];
+    const float2 uz = fz[((long long)i * My + j) * (Mz + 1) + k + 1];
+    Kahan s;
+    s.add(lx.x); s.add(ly.x); s.add(lz.x);
+    s.add(ux.x); s.add(uy.x); s.add(uz.x);
+    s.add(base_diff(i + 1, j, k) * ux.y);
+    s.add(base_diff(i, j + 1, k) * uy.y);
+    s.add(base_diff(i, j, k + 1) * uz.y);
+    const float val = s.value();
+    if (mode == 0) out[id] = val;
+    else if (mode == 1) out[id] = in[id] - val;
+    else out[id] = out[id] + val;
+}
+
+inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+template <>
+cudaError_t run_pass<float>(const PassDesc& d, const VelocityFields& vel, const float* a, const PassWork<float>& w,
+                            const float* in, float* out, int mode, cudaStream_t s) {
+    float2* psi = (float2*)w.psi;
+    const long long cols = (long long)d.A.Mx * d.A.Mz;
+    k_psi32<<<nblk(cols, 128), 128, 0, s>>>(d, a, psi);
+    if (!d.zero_velocity) {
+        const long long nv = (long long)(d.A.Mx + 1) * (d.A.My + 1) * (d.A.Mz + 1);
+        k_backtrace32<<<nblk(nv, 128), 128, 0, s>>>(d, (const float*)vel.u, (const float*)vel.v, (const float*)vel.w,
+                                                   vel.fu, vel.fv, vel.fw, w.verts);
+    }
+    for (int fam = 0; fam < 3; ++fam) {
+        const long long n = (long long)(d.A.Mx + (fam == 0)) * (d.A.My + (fam == 1)) * (d.A.Mz + (fam == 2));
+        prof_mark(w, 0, s);
+        k_faces32<<<nblk(n, 128), 128, 0, s>>>(d, fam, a, psi, w.verts, (float2*)w.flux[fam], (float2*)w.flux_rev[fam],
+                                               w.status, w.counters);
+        prof_mark(w, 1, s);
+    }
+    const long long nc = (long long)d.A.Mx * d.A.My * d.A.Mz;
+    k_gather32<<<nblk(nc, 256), 256, 0, s>>>(d, (const float2*)w.flux[0], (const float2*)w.flux[1],
+                                             (const float2*)w.flux[2], (const float2*)w.flux_rev[0],
+                                             (const float2*)w.flux_rev[1], (const float2*)w.flux_rev[2], psi, in, out,
+                                             mode);
+    return cudaGetLastError();
+}
+
+template <>
+cudaError_t launch_psi<float>(const PassDesc& d, const float* a, float* psi, cudaStream_t s) {
+    const long long cols = (long long)d.A.Mx * d.A.Mz;
+    k_psi32<<<nblk(cols, 128), 128, 0, s>>>(d, a, (float2*)psi);
+    return cudaGetLastError();
+}
+
+template <>
+cudaError_t launch_backtrace<float>(const PassDesc& d, const VelocityFields& vel, float* verts, cudaStream_t s) {
+    const long long nv = (long long)(d.A.Mx + 1) * (d.A.My + 1) * (d.A.Mz + 1);
+    k_backtrace32<<<nblk(nv, 128), 128, 0, s>>>(d, (const float*)vel.u, (const float*)vel.v, (const float*)vel.w,
+                                               vel.fu, vel.fv, vel.fw, verts);
+    return cudaGetLastError();
+}
+
+}  // namespace fia

@@ -22,13 +22,16 @@ struct fia_session {
     int last_status;
     bool status_pending;
     bool counters_pending;
-    unsigned long long counters_host[2];
+    unsigned long long counters_host[4];
+    unsigned long long launches;   // kernels launched by this session (host-side count)
+    std::vector<cudaEvent_t> prof_ev;   // face-kernel timing (fia_profile_faces)
+    int prof_n;
     double wall_loss[3];
     // device buffers
     void* rho; void* rho_next; void* pres;
     void* vel[3]; void* vel_next[3];
     void* cbuf;                  // correction field (pass 2 result)
-    void* psi; void* verts; void* flux[3];
+    void* psi; void* verts; void* flux[3]; void* flux_rev[3];
     void* pw[5];                 // pressure work vectors r z d q (+ spare)
     double* part; double* scal; double* sums;
     unsigned* status; unsigned long long* counters;
@@ -125,8 +128,12 @@ template <typename T>
 cudaError_t reduce(fia_session* s, const void* a, long long n, int kind, bool accumulate) {
     k_reduce_part<T><<<kRedBlocks, 256, 0, s->stream>>>((const T*)a, n, kind, s->red_part);
     k_reduce_final<<<1, 256, 0, s->stream>>>(s->red_part, kRedBlocks, kind, s->red_out, accumulate ? 1 : 0);
+    s->launches += 2;
     return cudaGetLastError();
 }
+
+// kernels launched by one run_pass: psi, backtrace (moving passes), three face families, gather
+inline unsigned pass_launches(const PassDesc& d) { return d.zero_velocity ? 5u : 6u; }
 
 // Split offsets (colour = pos/h - off) per field for the main and the error-advection pass
 // (move_substances_3d.cpp:189; advect_velocity_flux_advection_3d.cpp:622-628, :721,
@@ -171,8 +178,11 @@ template <typename T>
 PassWork<T> work(fia_session* s) {
     PassWork<T> w;
     w.psi = (T*)s->psi; w.verts = (T*)s->verts;
-    for (int f = 0; f < 3; ++f) w.flux[f] = (T*)s->flux[f];
+    for (int f = 0; f < 3; ++f) { w.flux[f] = (T*)s->flux[f]; w.flux_rev[f] = (T*)s->flux_rev[f]; }
     w.status = s->status; w.counters = s->counters;
+    w.prof_ev = s->prof_ev.empty() ? nullptr : s->prof_ev.data();
+    w.prof_n = &s->prof_n;
+    w.prof_cap = (int)(s->prof_ev.size() / 2);
     return w;
 }
 
@@ -201,23 +211,25 @@ cudaError_t advect_field(fia_session* s, int comp, const T* in, T* out, double d
     d.zero_velocity = 0;
     split_offsets(comp, 0, p->split_method, d.color_off);
     cudaError_t e = run_pass<T>(d, vel, in, w, in, out, 0, s->stream);
+    s->launches += pass_launches(d);
     if (e != cudaSuccess || !p->enable_eliminate_zero_velocity_false_diffusion) return e;
     // pass 2: zero velocity, psi at the piece centroid, plain psi; c = in - A2(in)
     T* c = (T*)s->cbuf;
     d.zero_velocity = 1; d.use_integral = 0; d.psi_mode = PSI_PLAIN;
     e = run_pass<T>(d, vel, in, w, in, c, 1, s->stream);
+    s->launches += pass_launches(d);
     if (e != cudaSuccess) return e;
     // pass 3: advect the error with 1Dy-linear interpolation and the error split
     d.zero_velocity = 0; d.interp = INTERP_1DY_LINEAR;
     split_offsets(comp, 1, p->split_method, d.color_off);
+    s->launches += pass_launches(d);
     return run_pass<T>(d, vel, c, w, nullptr, out, 2, s->stream);
 }
 
+// Status bits are per call; the work counters accumulate over the session's lifetime.
 cudaError_t reset_counters(fia_session* s) {
-    cudaError_t e = cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->stream);
-    if (e != cudaSuccess) return e;
     s->status_pending = true; s->counters_pending = true;
-    return cudaMemsetAsync(s->counters, 0, 2 * sizeof(unsigned long long), s->stream);
+    return cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->stream);
 }
 
 int finish_status(fia_session* s) {
@@ -259,9 +271,11 @@ int pressure(fia_session* s, const fia_solver_params* sp, fia_solver_report* rep
     PressureReport r;
     CK(pressure_solve<T>(W, s->N[0], s->N[1], s->N[2], s->h, (const T*)s->vel[0], (const T*)s->vel[1],
                          (const T*)s->vel[2], sp->tol, sp->max_iter, &r, s->stream));
+    s->launches += 4 + 5ull * (unsigned long long)r.iterations;   // rhs, precondition (+ finals), 5 per CG iteration
     if (subtract) {
         CK(subtract_gradient<T>((const T*)s->pres, (T*)s->vel[0], (T*)s->vel[1], (T*)s->vel[2], s->N[0], s->N[1],
                                 s->N[2], s->h, s->part, s->sums, s->stream));
+        s->launches += 3;
         double loss[3];
         CK(cudaMemcpyAsync(loss, s->sums, 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));
@@ -294,6 +308,33 @@ int debug_flux_pass(fia_session* s, int comp, const double* field, double dt, in
     return finish_status(s);
 }
 
+// FP32 form: vertex displacements in cells -> absolute positions; psi pairs -> psi.
+__global__ void k_disp_to_pos(const float* __restrict__ disp, double* __restrict__ out, int Ly, int Lz, int comp,
+                              double h, long long nv) {
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += (long long)gridDim.x * blockDim.x) {
+        const int idx[3] = {(int)(v / ((long long)Ly * Lz)), (int)((v / Lz) % Ly), (int)(v % Lz)};
+        for (int c = 0; c < 3; ++c)
+            out[3 * v + c] = ((double)idx[c] - (c == comp ? 0.5 : 0.0) + (double)disp[3 * v + c]) * h;
+    }
+}
+__global__ void k_pairs_to_psi(const float2* __restrict__ p, double* __restrict__ out, double h, long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = ((double)p[i].x + (double)p[i].y) * h;
+}
+
+void export_verts(fia_session* s, const PassDesc& d, const double* verts, double* tmp, long long n) {
+    k_convert<double, double><<<256, 256, 0, s->stream>>>(verts, tmp, n);
+}
+void export_verts(fia_session* s, const PassDesc& d, const float* verts, double* tmp, long long n) {
+    k_disp_to_pos<<<256, 256, 0, s->stream>>>(verts, tmp, d.A.My + 1, d.A.Mz + 1, d.comp, s->h, n / 3);
+}
+void export_psi(fia_session* s, const double* psi, double* tmp, long long n) {
+    k_convert<double, double><<<256, 256, 0, s->stream>>>(psi, tmp, n);
+}
+void export_psi(fia_session* s, const float* psi, double* tmp, long long n) {
+    k_pairs_to_psi<<<256, 256, 0, s->stream>>>((const float2*)psi, tmp, s->h, n);
+}
+
 template <typename T>
 int debug_backtrace(fia_session* s, int comp, double dt, int interp, double* out) {
     PassDesc d = base_desc(s, comp, dt);
@@ -302,7 +343,7 @@ int debug_backtrace(fia_session* s, int comp, double dt, int interp, double* out
     CK(launch_backtrace<T>(d, velocity(s, s->vel), (T*)s->verts, s->stream));
     double* tmp = nullptr;
     CK(cudaMallocAsync((void**)&tmp, n * sizeof(double), s->stream));
-    k_convert<double, T><<<256, 256, 0, s->stream>>>((const T*)s->verts, tmp, n);
+    export_verts(s, d, (const T*)s->verts, tmp, n);
     CK(cudaMemcpyAsync(out, tmp, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaFreeAsync(tmp, s->stream));
     CK(cudaStreamSynchronize(s->stream));
@@ -320,17 +361,134 @@ int debug_psi(fia_session* s, int comp, const double* field, int mode, int k, do
     CK(cudaMemcpyAsync(tmp, field, n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
     k_convert<T, double><<<256, 256, 0, s->stream>>>(tmp, (T*)s->cbuf, n);
     CK(launch_psi<T>(d, (const T*)s->cbuf, (T*)s->psi, s->stream));
-    k_convert<double, T><<<256, 256, 0, s->stream>>>((const T*)s->psi, tmp, np);
+    export_psi(s, (const T*)s->psi, tmp, np);
     CK(cudaMemcpyAsync(out, tmp, np * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaFreeAsync(tmp, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return FIA_OK;
 }
 
+// ------------------------------- the smoke step -----------------------------------
+// density = max(density, value) in the cells whose centre lies in the sphere
+template <typename T>
+__global__ void k_source(T* __restrict__ rho, int nx, int ny, int nz, double h, double cx, double cy, double cz,
+                         double r, double value) {
+    const long long n = (long long)nx * ny * nz;
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        const int iz = (int)(c % nz), iy = (int)((c / nz) % ny), ix = (int)(c / ((long long)nz * ny));
+        const double x = (ix + 0.5) * h - cx, y = (iy + 0.5) * h - cy, z = (iz + 0.5) * h - cz;
+        if (x * x + y * y + z * z <= r * r && (double)rho[c] < value) rho[c] = (T)value;
+    }
+}
+
+// v += dt * b * (rho_below + rho_above) / 2 on interior y-faces
+template <typename T>
+__global__ void k_buoyancy(T* __restrict__ v, const T* __restrict__ rho, int nx, int ny, int nz, double a) {
+    const long long n = (long long)nx * (ny + 1) * nz;
+    for (long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x; f < n; f += (long long)gridDim.x * blockDim.x) {
+        const int iz = (int)(f % nz), iy = (int)((f / nz) % (ny + 1)), ix = (int)(f / ((long long)nz * (ny + 1)));
+        if (iy == 0 || iy == ny) continue;
+        const long long c = ((long long)ix * ny + iy) * nz + iz;
+        v[f] = (T)((double)v[f] + a * 0.5 * ((double)rho[c - nz] + (double)rho[c]));
+    }
+}
+
+template <typename T>
+__global__ void k_scale(T* __restrict__ a, long long n, double s) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        a[i] = (T)((double)a[i] * s);
+}
+
+template <typename T>
+int read_reduction(fia_session* s, const void* a, long long n, int kind, double* out) {
+    CK(reduce<T>(s, a, n, kind, false));
+    CK(cudaMemcpyAsync(out, s->red_out, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FIA_OK;
+}
+
+template <typename T>
+int step(fia_session* s, const fia_step_params* p, fia_step_report* rep) {
+    const int nx = s->N[0], ny = s->N[1], nz = s->N[2];
+    const long long nc = (long long)nx * ny * nz;
+    const double V = s->h * s->h * s->h;
+    int status = 0, r;
+    if (p->source) {
+        k_source<T><<<1024, 256, 0, s->stream>>>((T*)s->rho, nx, ny, nz, s->h, p->source_center[0],
+                                                 p->source_center[1], p->source_center[2], p->source_radius,
+                                                 p->source_density);
+        s->launches += 1;
+    }
+    double umax = 0.0, m;
+    for (int c = 0; c < 3; ++c) {
+        if ((r = read_reduction<T>(s, s->vel[c], field_count(s, FIA_FIELD_U + c), 1, &m)) != FIA_OK) return r;
+        umax = std::max(umax, m);
+    }
+    double dt = p->max_dt;
+    if (umax > 0.0) dt = std::min(dt, p->cfl * s->h / umax);
+    if (p->buoyancy != 0.0) {
+        k_buoyancy<T><<<1024, 256, 0, s->stream>>>((T*)s->vel[1], (const T*)s->rho, nx, ny, nz, dt * p->buoyancy);
+        s->launches += 1;
+    }
+    fia_solver_report sr;
+    std::memset(&sr, 0, sizeof(sr));
+    if (p->frame == 0) {
+        if ((r = pressure<T>(s, &p->solver, &sr, true)) < 0) return r;
+        status |= r;
+        if ((r = advect_velocity<T>(s, dt, &p->advect)) < 0) return r;
+    } else {
+        if ((r = advect_velocity<T>(s, dt, &p->advect)) < 0) return r;
+        if ((r = pressure<T>(s, &p->solver, &sr, true)) < 0) return r;
+        status |= r;
+    }
+    status |= finish_status(s);
+    double m0, m1;
+    if ((r = read_reduction<T>(s, s->rho, nc, 0, &m0)) != FIA_OK) return r;
+    if ((r = move_substances<T>(s, dt, &p->advect)) < 0) return r;
+    status |= finish_status(s);
+    if ((r = read_reduction<T>(s, s->rho, nc, 0, &m1)) != FIA_OK) return r;
+    double m2 = m1;
+    if (p->mass_correction && m1 != 0.0 && m0 != 0.0) {
+        k_scale<T><<<1024, 256, 0, s->stream>>>((T*)s->rho, nc, m0 / m1);
+        s->launches += 1;
+        if ((r = read_reduction<T>(s, s->rho, nc, 0, &m2)) != FIA_OK) return r;
+    }
+    if (rep) {
+        rep->dt = dt; rep->max_velocity = umax;
+        rep->mass_before_advection = m0 * V; rep->mass_after_advection = m1 * V; rep->mass_after = m2 * V;
+        rep->solver_iterations = sr.iterations; rep->solver_rel_residual = sr.rel_residual;
+        rep->status = status;
+    }
+    return status;
+}
+
 }  // namespace
 
 // =====================================================================================
 extern "C" {
+
+void fia_default_step_params(fia_step_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    fia_default_advect_params(&p->advect);
+    fia_default_solver_params(&p->solver);
+    p->cfl = 1.0;
+    p->max_dt = 1.0 / 60.0;
+    p->buoyancy = 1.0;
+    p->source = 1;
+    p->source_center[0] = 0.5; p->source_center[1] = 0.15; p->source_center[2] = 0.5;
+    p->source_radius = 0.1;
+    p->source_density = 1.0;
+    p->mass_correction = 1;
+    p->frame = 0;
+}
+
+int fia_step(fia_session* s, const fia_step_params* p, fia_step_report* rep) {
+    if (!s || !p || !(p->cfl > 0.0) || !(p->max_dt > 0.0)) return FIA_ERR_INVALID;
+    const int c = check_params(&p->advect);
+    if (c != FIA_OK) return c;
+    return s->precision == FIA_FP64 ? step<double>(s, p, rep) : step<float>(s, p, rep);
+}
 
 int fia_api_version(void) { return FIA_API_VERSION; }
 
@@ -366,14 +524,14 @@ void fia_default_solver_params(fia_solver_params* p) {
 
 fia_session* fia_create(int nx, int ny, int nz, double cell_length, int precision) {
     if (nx < 2 || ny < 2 || nz < 2 || !(cell_length > 0.0)) { g_last_error = "fia_create: bad grid"; return nullptr; }
-    if (precision != FIA_FP64) { g_last_error = "fia_create: precision not available"; return nullptr; }
+    if (precision != FIA_FP64 && precision != FIA_FP32C) { g_last_error = "fia_create: unknown precision"; return nullptr; }
     if ((long long)(nx + 2) * (ny + 2) * (nz + 2) > (1LL << 31)) { g_last_error = "fia_create: grid too large"; return nullptr; }
     fia_session* s = new fia_session();
     std::memset(s->wall_loss, 0, sizeof(s->wall_loss));
     s->N[0] = nx; s->N[1] = ny; s->N[2] = nz; s->h = cell_length; s->precision = precision;
     s->es = precision == FIA_FP64 ? sizeof(double) : sizeof(float);
-    s->last_status = 0; s->status_pending = false; s->counters_pending = false;
-    s->counters_host[0] = s->counters_host[1] = 0;
+    s->last_status = 0; s->status_pending = false; s->counters_pending = false; s->launches = 0;
+    s->counters_host[0] = s->counters_host[1] = s->counters_host[2] = s->counters_host[3] = 0;
     if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
         g_last_error = "fia_create: stream"; delete s; return nullptr;
     }
@@ -388,8 +546,9 @@ fia_session* fia_create(int nx, int ny, int nz, double cell_length, int precisio
     bool ok = true;
     auto A = [&](void*& dst, size_t bytes) { dst = alloc(bytes); ok = ok && dst != nullptr; };
     const size_t fb = (size_t)big * s->es;
-    A(s->rho, fb); A(s->rho_next, fb); A(s->pres, fb); A(s->cbuf, fb); A(s->psi, fb);
-    for (int c = 0; c < 3; ++c) { A(s->vel[c], fb); A(s->vel_next[c], fb); A(s->flux[c], fb); }
+    const size_t pb = (size_t)big * 8;   // psi and face fluxes: one double or one float pair per node
+    A(s->rho, fb); A(s->rho_next, fb); A(s->pres, fb); A(s->cbuf, (size_t)big * 8); A(s->psi, pb);
+    for (int c = 0; c < 3; ++c) { A(s->vel[c], fb); A(s->vel_next[c], fb); A(s->flux[c], pb); A(s->flux_rev[c], pb); }
     A(s->verts, 3 * fb);
     for (int q = 0; q < 4; ++q) A(s->pw[q], fb);
     s->pw[4] = nullptr;
@@ -410,9 +569,37 @@ fia_session* fia_create(int nx, int ny, int nz, double cell_length, int precisio
     return s;
 }
 
+int fia_profile_faces(fia_session* s, int capacity) {
+    if (!s || capacity < 0) return FIA_ERR_INVALID;
+    CK(cudaStreamSynchronize(s->stream));
+    for (cudaEvent_t e : s->prof_ev) cudaEventDestroy(e);
+    s->prof_ev.assign(2 * (size_t)capacity, nullptr);
+    for (auto& e : s->prof_ev) CK(cudaEventCreate(&e));
+    s->prof_n = 0;
+    return FIA_OK;
+}
+
+int fia_profile_faces_read(fia_session* s, double* total_ms, int* launches) {
+    if (!s || !total_ms || !launches) return FIA_ERR_INVALID;
+    CK(cudaStreamSynchronize(s->stream));
+    double t = 0.0;
+    for (int i = 0; i < s->prof_n; ++i) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, s->prof_ev[2 * i], s->prof_ev[2 * i + 1]));
+        t += ms;
+    }
+    *total_ms = t;
+    *launches = s->prof_n;
+    for (cudaEvent_t e : s->prof_ev) cudaEventDestroy(e);
+    s->prof_ev.clear();
+    s->prof_n = 0;
+    return FIA_OK;
+}
+
 void fia_destroy(fia_session* s) {
     if (!s) return;
     cudaStreamSynchronize(s->stream);
+    for (cudaEvent_t e : s->prof_ev) cudaEventDestroy(e);
     for (void* p : s->allocations) cudaFree(p);
     cudaStreamDestroy(s->stream);
     delete s;
@@ -481,30 +668,33 @@ int fia_move_substances_3D(fia_session* s, double dt, const fia_advect_params* p
     if (!s || !(dt >= 0.0)) return FIA_ERR_INVALID;
     const int c = check_params(p);
     if (c != FIA_OK) return c;
-    return move_substances<double>(s, dt, p);
+    return s->precision == FIA_FP64 ? move_substances<double>(s, dt, p) : move_substances<float>(s, dt, p);
 }
 
 int fia_advect_velocity_xyz(fia_session* s, double dt, const fia_advect_params* p) {
     if (!s || !(dt >= 0.0)) return FIA_ERR_INVALID;
     const int c = check_params(p);
     if (c != FIA_OK) return c;
-    return advect_velocity<double>(s, dt, p);
+    return s->precision == FIA_FP64 ? advect_velocity<double>(s, dt, p) : advect_velocity<float>(s, dt, p);
 }
 
 int fia_calc_pressure_3D(fia_session* s, const fia_solver_params* sp, fia_solver_report* rep) {
     if (!s) return FIA_ERR_INVALID;
-    return pressure<double>(s, sp, rep, false);
+    return s->precision == FIA_FP64 ? pressure<double>(s, sp, rep, false) : pressure<float>(s, sp, rep, false);
 }
 
 int fia_calc_pressure_gradient_term_3D(fia_session* s, const fia_solver_params* sp, fia_solver_report* rep) {
     if (!s) return FIA_ERR_INVALID;
-    return pressure<double>(s, sp, rep, true);
+    return s->precision == FIA_FP64 ? pressure<double>(s, sp, rep, true) : pressure<float>(s, sp, rep, true);
 }
 
 int fia_max_abs_velocity(fia_session* s, double* out) {
     if (!s || !out) return FIA_ERR_INVALID;
     CK(cudaMemsetAsync(s->red_out, 0, sizeof(double), s->stream));
-    for (int c = 0; c < 3; ++c) CK(reduce<double>(s, s->vel[c], field_count(s, FIA_FIELD_U + c), 1, true));
+    for (int c = 0; c < 3; ++c) {
+        const long long n = field_count(s, FIA_FIELD_U + c);
+        CK(s->precision == FIA_FP64 ? reduce<double>(s, s->vel[c], n, 1, true) : reduce<float>(s, s->vel[c], n, 1, true));
+    }
     CK(cudaMemcpyAsync(out, s->red_out, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return FIA_OK;
@@ -512,7 +702,8 @@ int fia_max_abs_velocity(fia_session* s, double* out) {
 
 int fia_total_mass(fia_session* s, double* out) {
     if (!s || !out) return FIA_ERR_INVALID;
-    CK(reduce<double>(s, s->rho, field_count(s, FIA_FIELD_DENSITY), 0, false));
+    const long long n = field_count(s, FIA_FIELD_DENSITY);
+    CK(s->precision == FIA_FP64 ? reduce<double>(s, s->rho, n, 0, false) : reduce<float>(s, s->rho, n, 0, false));
     double m = 0.0;
     CK(cudaMemcpyAsync(&m, s->red_out, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
@@ -526,14 +717,15 @@ int fia_wall_momentum_loss(fia_session* s, double* out3) {
     return FIA_OK;
 }
 
-int fia_pass_counters(fia_session* s, unsigned long long* out2) {
-    if (!s || !out2) return FIA_ERR_INVALID;
+int fia_pass_counters(fia_session* s, unsigned long long* out5) {
+    if (!s || !out5) return FIA_ERR_INVALID;
     if (s->counters_pending) {
-        CK(cudaMemcpyAsync(s->counters_host, s->counters, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaMemcpyAsync(s->counters_host, s->counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));
         s->counters_pending = false;
     }
-    out2[0] = s->counters_host[0]; out2[1] = s->counters_host[1];
+    for (int q = 0; q < 4; ++q) out5[q] = s->counters_host[q];
+    out5[4] = s->launches;
     return FIA_OK;
 }
 
@@ -578,19 +770,24 @@ int fia_debug_flux_pass(fia_session* s, int comp, const double* field, double dt
     if (!s || !field || !out || !co || comp < -1 || comp > 2 || k < 1 || k > kMaxGauss || interp < 0 || interp > 2 ||
         psi_mode < 0 || psi_mode > 2)
         return FIA_ERR_INVALID;
-    return debug_flux_pass<double>(s, comp, field, dt, interp, psi_mode, use_integral, zero_velocity, co, k,
-                                   minimal_area, out);
+    if (s->precision == FIA_FP64)
+        return debug_flux_pass<double>(s, comp, field, dt, interp, psi_mode, use_integral, zero_velocity, co, k,
+                                       minimal_area, out);
+    return debug_flux_pass<float>(s, comp, field, dt, interp, psi_mode, use_integral, zero_velocity, co, k,
+                                  minimal_area, out);
 }
 
 int fia_debug_backtrace(fia_session* s, int comp, double dt, int interp, double* out) {
     if (!s || !out || comp < -1 || comp > 2 || interp < 0 || interp > 2) return FIA_ERR_INVALID;
-    return debug_backtrace<double>(s, comp, dt, interp, out);
+    return s->precision == FIA_FP64 ? debug_backtrace<double>(s, comp, dt, interp, out)
+                                    : debug_backtrace<float>(s, comp, dt, interp, out);
 }
 
 int fia_debug_psi(fia_session* s, int comp, const double* field, int mode, int k, double* out) {
     if (!s || !field || !out || comp < -1 || comp > 2 || mode < 0 || mode > 2 || k < 1 || k > kMaxGauss)
         return FIA_ERR_INVALID;
-    return debug_psi<double>(s, comp, field, mode, k, out);
+    return s->precision == FIA_FP64 ? debug_psi<double>(s, comp, field, mode, k, out)
+                                    : debug_psi<float>(s, comp, field, mode, k, out);
 }
 
 }  // extern "C"

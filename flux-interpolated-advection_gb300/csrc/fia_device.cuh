@@ -20,6 +20,23 @@ __device__ __forceinline__ long long idx3(const NodeField& F, int i, int j, int 
     return (long long)F.Mz * ((long long)F.My * i + j) + k;
 }
 
+// Values within a few units in the last place of an integer are taken as that integer:
+// the discrete decisions of the scheme (iso-line crossings of vertex colours, the cell
+// holding a centroid) are made on integers that exact arithmetic hits exactly (lattice
+// vertices, vertices clamped to a wall) but n*h/h does not when h is not a power of two.
+// Without this, ulp-level differences flip the clipped piece structure.  The oracle
+// applies the same rule.
+__device__ __forceinline__ double snap_int(double x) {
+    const double r = rint(x);
+    const double tol = 8.0 * 2.220446049250313e-16 * fmax(1.0, fabs(x));
+    return fabs(x - r) <= tol ? r : x;
+}
+__device__ __forceinline__ float snap_int(float x) {
+    const float r = rintf(x);
+    const float tol = 8.0f * 1.1920928955078125e-7f * fmaxf(1.0f, fabsf(x));
+    return fabsf(x - r) <= tol ? r : x;
+}
+
 // Read-only load through the non-coherent cache.
 template <typename T> __device__ __forceinline__ T ldg(const T* p) { return __ldg(p); }
 
@@ -123,8 +140,8 @@ __device__ T weno6_3d(const T* __restrict__ a, const NodeField& F, T h, T px, T 
 // (WENO6_interpolation_1d.cpp:315-430).
 template <typename T>
 __device__ T weno6_1dy(const T* __restrict__ a, const NodeField& F, T h, T px, T py, T pz) {
-    const int ix = clampi((int)floor((px - (T(F.ox) * h - T(0.5) * h)) / h), F.Mx - 1);
-    const int iz = clampi((int)floor((pz - (T(F.oz) * h - T(0.5) * h)) / h), F.Mz - 1);
+    const int ix = clampi((int)floor(snap_int((px - (T(F.ox) * h - T(0.5) * h)) / h)), F.Mx - 1);
+    const int iz = clampi((int)floor(snap_int((pz - (T(F.oz) * h - T(0.5) * h)) / h)), F.Mz - 1);
     const int by = (int)floor((py - T(F.oy) * h) / h);
     T t[6], f[6];
 #pragma unroll
@@ -161,8 +178,8 @@ __device__ T lin3d(const T* __restrict__ a, const NodeField& F, T h, T px, T py,
 // Linear along y, nearest cell in x and z (linear_interpolation_1d.cpp:314-374).
 template <typename T>
 __device__ T lin1dy(const T* __restrict__ a, const NodeField& F, T h, T px, T py, T pz) {
-    const int ix = clampi((int)floor((px - (T(F.ox) * h - T(0.5) * h)) / h), F.Mx - 1);
-    const int iz = clampi((int)floor((pz - (T(F.oz) * h - T(0.5) * h)) / h), F.Mz - 1);
+    const int ix = clampi((int)floor(snap_int((px - (T(F.ox) * h - T(0.5) * h)) / h)), F.Mx - 1);
+    const int iz = clampi((int)floor(snap_int((pz - (T(F.oz) * h - T(0.5) * h)) / h)), F.Mz - 1);
     const T oy = T(F.oy) * h;
     const int by = (int)floor((py - oy) / h);
     const T f0 = ldg(a + idx3(F, ix, clampi(by, F.My - 1), iz));

@@ -1,0 +1,161 @@
+// fia_local.cuh -- FP32 building blocks in local cell coordinates (the chosen form).
+//
+// Positions are carried as an integer anchor (a cell-lattice index) plus a small FP32
+// offset q, both in units of the cell length: X = anchor + q.  Every quantity the FP32
+// arithmetic sees is then O(CFL): stencil distances, colours, centroids and normals keep
+// FP32's full relative precision regardless of where in a 256^3 or 384^3 grid the face is.
+// Absolute FP32 coordinates would lose ~1.5e-5 of a cell at 256^3.
+//
+// psi is carried as a double-float pair (hi, lo) in cell units (psi / h).  A face
+// interpolates psi - Psi0 for a base node Psi0 of its own, formed from the pairs as
+// (hi - hi0) + (lo - lo0): WENO6, trilinear and 1Dy-linear interpolation all commute with
+// adding a constant (the smoothness indicators are quadratic forms of differences and the
+// weights sum to one), so this is the same interpolant without FP32 cancellation.
+#pragma once
+#include "fia_device.cuh"
+
+namespace fia {
+
+// error-free sum of two floats (Knuth TwoSum)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// running sum with a compensation term
+struct Kahan {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        float t, e;
+        two_sum(s, x, t, e);
+        s = t;
+        c += e;
+    }
+    __device__ __forceinline__ float value() const { return s + c; }
+};
+
+// Loads node values as floats: plain array, or psi pairs relative to a base pair.
+struct PlainLoad {
+    const float* __restrict__ a;
+    __device__ __forceinline__ float operator()(long long i) const { return __ldg(a + i); }
+};
+struct PsiLoad {
+    const float2* __restrict__ a;
+    float hi0, lo0;
+    __device__ __forceinline__ float operator()(long long i) const {
+        const float2 v = __ldg(a + i);
+        return (v.x - hi0) + (v.y - lo0);
+    }
+};
+
+// stencil base and fractional offset of the local position along one axis
+__device__ __forceinline__ void locate(int anchor, float q, float off, int& base, float& s) {
+    const float r = q - off;
+    const float f = floorf(r);
+    base = anchor + (int)f;
+    s = r - f;
+}
+// the cell holding the local position along one axis (a discrete decision: snapped)
+__device__ __forceinline__ int cell_of(int anchor, float q, float off) {
+    return anchor + (int)floorf(snap_int(q - off));
+}
+
+template <class L>
+__device__ float weno6_3d_loc(const L& load, const NodeField& F, const int* anc, const float* q) {
+    int bx, by, bz;
+    float sx, sy, sz;
+    locate(anc[0], q[0], (float)F.ox, bx, sx);
+    locate(anc[1], q[1], (float)F.oy, by, sy);
+    locate(anc[2], q[2], (float)F.oz, bz, sz);
+    float tx[6], ty[6], tz[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        tx[i] = sx + float(2 - i);
+        ty[i] = sy + float(2 - i);
+        tz[i] = sz + float(2 - i);
+    }
+    const WenoCoef<float> cx = weno_coef(tx), cy = weno_coef(ty), cz = weno_coef(tz);
+    int kk[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) kk[i] = clampi(bz - 2 + i, F.Mz - 1);
+    float yv[6];
+#pragma unroll 1
+    for (int ix = 0; ix < 6; ++ix) {
+        const int ii = clampi(bx - 2 + ix, F.Mx - 1);
+        float zv[6];
+#pragma unroll
+        for (int iy = 0; iy < 6; ++iy) {
+            const int jj = clampi(by - 2 + iy, F.My - 1);
+            const long long row = (long long)F.Mz * ((long long)F.My * ii + jj);
+            float f[6];
+#pragma unroll
+            for (int iz = 0; iz < 6; ++iz) f[iz] = load(row + kk[iz]);
+            zv[iy] = weno6_eval(f, cz);
+        }
+        yv[ix] = weno6_eval(zv, cy);
+    }
+    return weno6_eval(yv, cx);
+}
+
+template <class L>
+__device__ float weno6_1dy_loc(const L& load, const NodeField& F, const int* anc, const float* q) {
+    int by;
+    float sy;
+    const int ix = clampi(cell_of(anc[0], q[0], (float)F.ox - 0.5f), F.Mx - 1);
+    const int iz = clampi(cell_of(anc[2], q[2], (float)F.oz - 0.5f), F.Mz - 1);
+    locate(anc[1], q[1], (float)F.oy, by, sy);
+    float t[6], f[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        t[i] = sy + float(2 - i);
+        f[i] = load(idx3(F, ix, clampi(by - 2 + i, F.My - 1), iz));
+    }
+    return weno6_eval(f, weno_coef(t));
+}
+
+template <class L>
+__device__ float lin3d_loc(const L& load, const NodeField& F, const int* anc, const float* q) {
+    int bx, by, bz;
+    float sx, sy, sz;
+    locate(anc[0], q[0], (float)F.ox, bx, sx);
+    locate(anc[1], q[1], (float)F.oy, by, sy);
+    locate(anc[2], q[2], (float)F.oz, bz, sz);
+    const int k0 = clampi(bz, F.Mz - 1), k1 = clampi(bz + 1, F.Mz - 1);
+    float yv[2];
+#pragma unroll
+    for (int ix = 0; ix < 2; ++ix) {
+        const int ii = clampi(bx + ix, F.Mx - 1);
+        float zv[2];
+#pragma unroll
+        for (int iy = 0; iy < 2; ++iy) {
+            const int jj = clampi(by + iy, F.My - 1);
+            const long long row = (long long)F.Mz * ((long long)F.My * ii + jj);
+            zv[iy] = (1.f - sz) * load(row + k0) + sz * load(row + k1);
+        }
+        yv[ix] = (1.f - sy) * zv[0] + sy * zv[1];
+    }
+    return (1.f - sx) * yv[0] + sx * yv[1];
+}
+
+template <class L>
+__device__ float lin1dy_loc(const L& load, const NodeField& F, const int* anc, const float* q) {
+    int by;
+    float sy;
+    const int ix = clampi(cell_of(anc[0], q[0], (float)F.ox - 0.5f), F.Mx - 1);
+    const int iz = clampi(cell_of(anc[2], q[2], (float)F.oz - 0.5f), F.Mz - 1);
+    locate(anc[1], q[1], (float)F.oy, by, sy);
+    const float f0 = load(idx3(F, ix, clampi(by, F.My - 1), iz));
+    const float f1 = load(idx3(F, ix, clampi(by + 1, F.My - 1), iz));
+    return (1.f - sy) * f0 + sy * f1;
+}
+
+template <class L>
+__device__ __forceinline__ float interp_loc(int method, const L& load, const NodeField& F, const int* anc,
+                                            const float* q) {
+    if (method == INTERP_WENO6) return weno6_3d_loc(load, F, anc, q);
+    if (method == INTERP_LINEAR) return lin3d_loc(load, F, anc, q);
+    return lin1dy_loc(load, F, anc, q);
+}
+
+}  // namespace fia

@@ -278,5 +278,9 @@ template cudaError_t pressure_solve<double>(const PressureWork<double>&, int, in
                                             const double*, double, int, PressureReport*, cudaStream_t);
 template cudaError_t subtract_gradient<double>(const double*, double*, double*, double*, int, int, int, double, double*,
                                                double*, cudaStream_t);
+template cudaError_t pressure_solve<float>(const PressureWork<float>&, int, int, int, double, const float*, const float*,
+                                           const float*, double, int, PressureReport*, cudaStream_t);
+template cudaError_t subtract_gradient<float>(const float*, float*, float*, float*, int, int, int, double, double*,
+                                              double*, cudaStream_t);
 
 }  // namespace fia

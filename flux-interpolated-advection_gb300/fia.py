@@ -24,8 +24,8 @@ REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libfia_%s.so" % platform.machine())
-SOURCES = ["fia_api.cu", "fia_advect.cu", "fia_pressure.cu"]
-HEADERS = ["fia_device.cuh", "fia_advect.cuh", "fia_pressure.cuh"]
+SOURCES = ["fia_api.cu", "fia_advect.cu", "fia_advect32.cu", "fia_pressure.cu"]
+HEADERS = ["fia_device.cuh", "fia_advect.cuh", "fia_local.cuh", "fia_pressure.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 FIA_OK, FIA_ERR_INVALID, FIA_ERR_CUDA, FIA_ERR_UNSUPPORTED, FIA_ERR_NOMEM = 0, -1, -2, -3, -4
@@ -107,6 +107,21 @@ class SolverReport(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("rel_residual", ctypes.c_double), ("status", ctypes.c_int)]
 
 
+class StepParams(ctypes.Structure):
+    """fia_step_params: one smoke step (main.cpp:600-721 order) plus the plume harness."""
+    _fields_ = [("advect", AdvectParams), ("solver", SolverParams), ("cfl", ctypes.c_double),
+                ("max_dt", ctypes.c_double), ("buoyancy", ctypes.c_double), ("source", ctypes.c_int),
+                ("source_center", ctypes.c_double * 3), ("source_radius", ctypes.c_double),
+                ("source_density", ctypes.c_double), ("mass_correction", ctypes.c_int), ("frame", ctypes.c_int)]
+
+
+class StepReport(ctypes.Structure):
+    _fields_ = [("dt", ctypes.c_double), ("max_velocity", ctypes.c_double),
+                ("mass_before_advection", ctypes.c_double), ("mass_after_advection", ctypes.c_double),
+                ("mass_after", ctypes.c_double), ("solver_iterations", ctypes.c_int),
+                ("solver_rel_residual", ctypes.c_double), ("status", ctypes.c_int)]
+
+
 def _declare(lib):
     vp, dp, ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int
     lib.fia_create.restype = vp
@@ -137,6 +152,10 @@ def _declare(lib):
     lib.fia_debug_psi.argtypes = [vp, ip, dp, ip, ip, dp]
     lib.fia_default_advect_params.argtypes = [ctypes.POINTER(AdvectParams)]
     lib.fia_default_solver_params.argtypes = [ctypes.POINTER(SolverParams)]
+    lib.fia_default_step_params.argtypes = [ctypes.POINTER(StepParams)]
+    lib.fia_profile_faces.argtypes = [vp, ip]
+    lib.fia_profile_faces_read.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_int)]
+    lib.fia_step.argtypes = [vp, ctypes.POINTER(StepParams), ctypes.POINTER(StepReport)]
 
 
 def _check(rc, what):
@@ -164,6 +183,22 @@ def advect_params(interpolation_method="WENO6", split_method="xz-CellFaceAligned
 def solver_params(tol=1e-6, max_iter=10000, method=0):
     p = SolverParams()
     p.tol, p.max_iter, p.method = tol, max_iter, method
+    return p
+
+
+def step_params(**kw):
+    """Defaults of fia_default_step_params (the plume), overridden by keyword."""
+    p = StepParams()
+    load().fia_default_step_params(ctypes.byref(p))
+    for k, v in kw.items():
+        if k == "advect" and isinstance(v, dict):
+            p.advect = advect_params(**v)
+        elif k == "solver" and isinstance(v, dict):
+            p.solver = solver_params(**v)
+        elif k == "source_center":
+            p.source_center = (ctypes.c_double * 3)(*v)
+        else:
+            setattr(p, k, v)
     return p
 
 
@@ -248,6 +283,22 @@ class Grid3D:
                                                            ctypes.byref(rep)), "calc_pressure_gradient_term_3D")
         return rep
 
+    def step(self, params=None):
+        """One smoke step (fia_step); returns the StepReport."""
+        rep = StepReport()
+        _check(self.lib.fia_step(self.s, ctypes.byref(params or step_params()), ctypes.byref(rep)), "fia_step")
+        return rep
+
+    def profile_faces(self, capacity):
+        """Start timing each face-kernel launch with CUDA events (see read_face_profile)."""
+        _check(self.lib.fia_profile_faces(self.s, capacity), "fia_profile_faces")
+
+    def read_face_profile(self):
+        """(summed device ms, number of face-kernel launches) since profile_faces."""
+        ms = ctypes.c_double(0); n = ctypes.c_int(0)
+        _check(self.lib.fia_profile_faces_read(self.s, ctypes.byref(ms), ctypes.byref(n)), "fia_profile_faces_read")
+        return ms.value, n.value
+
     def max_abs_velocity(self):
         out = ctypes.c_double(0)
         _check(self.lib.fia_max_abs_velocity(self.s, ctypes.byref(out)), "fia_max_abs_velocity")
@@ -264,9 +315,11 @@ class Grid3D:
         return tuple(out)
 
     def pass_counters(self):
-        out = (ctypes.c_ulonglong * 2)()
+        """Cumulative (faces, pieces, faces clipped from both sides, FP32 point
+        interpolations, kernel launches) since the session was created."""
+        out = (ctypes.c_ulonglong * 5)()
         _check(self.lib.fia_pass_counters(self.s, out), "fia_pass_counters")
-        return int(out[0]), int(out[1])
+        return tuple(int(x) for x in out)
 
     # ---- test hooks ----
     def debug_flux_pass(self, comp, field, dt, interp, psi_mode, use_integral, zero_velocity, color_off, k,

@@ -95,9 +95,44 @@ typedef struct fia_solver_report {
     int status;        /* FIA_STATUS_* bits of the solve */
 } fia_solver_report;
 
+/* One smoke step in the order of the reference's 3D loop (main.cpp:600-721): CFL time
+ * step, body force, velocity update (frame 0: project then advect, afterwards advect then
+ * project; update_fluid_velocity_3d.cpp:116-192), density advection.  The plume source,
+ * the buoyancy force and the mass correction have no counterpart in the reference
+ * (add_force_fluid_3D is commented out at update_fluid_velocity_3d.cpp:109 and
+ * correct_volume_concentration_error.cpp is empty); they are off when zero. */
+typedef struct fia_step_params {
+    fia_advect_params advect;     /* density and velocity flux advection */
+    fia_solver_params solver;     /* pressure projection */
+    double cfl;                   /* dt = cfl * h / max|u|   (calc_time_step_length_from_CFL_number.cpp:119) */
+    double max_dt;                /* cap on dt (the reference caps at the next movie frame, 1/fps) */
+    double buoyancy;              /* upward acceleration per unit density, added to v before advection */
+    int source;                   /* re-inject density in a sphere at the start of the step */
+    double source_center[3];
+    double source_radius;
+    double source_density;
+    int mass_correction;          /* rescale density to its pre-advection mass (FP64 sums) */
+    int frame;                    /* step index i_frame */
+} fia_step_params;
+
+typedef struct fia_step_report {
+    double dt;
+    double max_velocity;
+    double mass_before_advection;
+    double mass_after_advection;  /* before the mass correction */
+    double mass_after;            /* after it */
+    int solver_iterations;
+    double solver_rel_residual;
+    int status;                   /* FIA_STATUS_* bits of the step */
+} fia_step_report;
+
 /* Reference defaults for the flags (main.cpp:48-83) with WENO6, xz-CellFaceAligned, k = 3. */
 void fia_default_advect_params(fia_advect_params* p);
 void fia_default_solver_params(fia_solver_params* p);
+/* The plume of the benchmark configurations: source r = 0.1 at (0.5, 0.15, 0.5) of the unit
+ * box, density 1, buoyancy 1, CFL 1, mass correction on. */
+void fia_default_step_params(fia_step_params* p);
+int fia_step(fia_session* s, const fia_step_params* p, fia_step_report* rep);
 
 int fia_api_version(void);
 const char* fia_error_string(int code);
@@ -131,8 +166,17 @@ int fia_max_abs_velocity(fia_session* s, double* out);
 int fia_total_mass(fia_session* s, double* out);
 /* total_loss_of_momentum_{x,y,z} accumulated by calc_pressure_gradient_term_3D. */
 int fia_wall_momentum_loss(fia_session* s, double* out3);
-/* Faces visited and pieces emitted by the last advection call. */
-int fia_pass_counters(fia_session* s, unsigned long long* out2);
+/* Work counters accumulated since fia_create: [0] faces visited, [1] pieces emitted,
+ * [2] faces clipped from both sides (an iso-line crossed a piece more than twice, so the
+ * two adjacent cells see different pieces; FP32 form only counts [3]), [3] point
+ * interpolations made by the FP32 face kernel, [4] kernels launched. */
+int fia_pass_counters(fia_session* s, unsigned long long* out5);
+
+/* Face-kernel timing: after fia_profile_faces(s, capacity) an event pair is recorded on the
+ * session stream around each face-kernel launch (up to capacity launches);
+ * fia_profile_faces_read returns their summed device time and count, and stops. */
+int fia_profile_faces(fia_session* s, int capacity);
+int fia_profile_faces_read(fia_session* s, double* total_ms, int* launches);
 
 /* Drop-in bodies with host buffers: copy in, run on the device, copy out (synchronous). */
 int fia_move_substances_3D_host(fia_session* s, int host_dtype, void* substance_density, const void* u,

@@ -50,6 +50,19 @@ struct Field {
 inline long idx3(const int* M, int i, int j, int k) { return (long)M[2] * ((long)M[1] * i + j) + k; }
 inline int clampi(int i, int lo, int hi) { return i < lo ? lo : (i > hi ? hi : i); }
 
+// Values within a few units in the last place of an integer are taken as that integer.
+// The scheme makes discrete decisions on exact integers (iso-line crossings of vertex
+// colours, the cell holding a centroid); in exact arithmetic a vertex on the lattice or
+// clamped to a wall has an integer colour, but n*h/h rounds to either side of n when h
+// is not a power of two, and the resulting piece structure then flips under ulp-sized
+// changes (measured: 1e-15 relative velocity noise moved a 9^3 error pass by 1e-6).
+// The GPU library applies the same rule.
+inline real snap_int(real x) {
+    const real r = std::nearbyint(x);
+    const real tol = 8.0 * 2.220446049250313e-16 * std::max(1.0, std::fabs(x));
+    return std::fabs(x - r) <= tol ? r : x;
+}
+
 struct Grid {
     int N[3];
     real h;
@@ -174,8 +187,8 @@ static real weno6_3d(const Field& F, const real* p, real h) {
 // WENO6 along y only; x and z pick the node whose cell holds p
 // (WENO6_interpolation_1d.cpp:315-430:  index_x = floor(p_x/h) for cell centres).
 static real weno6_1dy(const Field& F, const real* p, real h) {
-    int ix = clampi((int)std::floor((p[0] - (F.off[0] * h - 0.5 * h)) / h), 0, F.M[0] - 1);
-    int iz = clampi((int)std::floor((p[2] - (F.off[2] * h - 0.5 * h)) / h), 0, F.M[2] - 1);
+    int ix = clampi((int)std::floor(snap_int((p[0] - (F.off[0] * h - 0.5 * h)) / h)), 0, F.M[0] - 1);
+    int iz = clampi((int)std::floor(snap_int((p[2] - (F.off[2] * h - 0.5 * h)) / h)), 0, F.M[2] - 1);
     int base = (int)std::floor((p[1] - F.off[1] * h) / h);
     real d[6], f[6];
     for (int i = 0; i < 6; ++i) {
@@ -208,8 +221,8 @@ static real lin3d(const Field& F, const real* p, real h) {
 
 // Linear along y, nearest cell in x and z (linear_interpolation_1d.cpp:314-374).
 static real lin1dy(const Field& F, const real* p, real h) {
-    int ix = clampi((int)std::floor((p[0] - (F.off[0] * h - 0.5 * h)) / h), 0, F.M[0] - 1);
-    int iz = clampi((int)std::floor((p[2] - (F.off[2] * h - 0.5 * h)) / h), 0, F.M[2] - 1);
+    int ix = clampi((int)std::floor(snap_int((p[0] - (F.off[0] * h - 0.5 * h)) / h)), 0, F.M[0] - 1);
+    int iz = clampi((int)std::floor(snap_int((p[2] - (F.off[2] * h - 0.5 * h)) / h)), 0, F.M[2] - 1);
     real o = F.off[1] * h;
     int base = (int)std::floor((p[1] - o) / h);
     real f0 = F.a[idx3(F.M, ix, clampi(base, 0, F.M[1] - 1), iz)];
@@ -301,7 +314,7 @@ static void cut_face_rec(const V2* poly, int num, int dim, const std::function<v
                 add.p[0] = t0 * poly[n].p[0] + t1 * poly[m].p[0];
                 add.p[1] = t0 * poly[n].p[1] + t1 * poly[m].p[1];
                 add.c[dim] = iso;
-                add.c[1 - dim] = t0 * poly[n].c[1 - dim] + t1 * poly[m].c[1 - dim];
+                add.c[1 - dim] = snap_int(t0 * poly[n].c[1 - dim] + t1 * poly[m].c[1 - dim]);
                 if (slot == 0) {
                     arr[0][head[0]++] = add;
                     slot = 1; head[1] = 0;
@@ -414,8 +427,8 @@ static int split_face(const real (*v)[3], real h, const real* color_off, real mi
     const real xi[4][2] = {{0.0, 0.0}, {1.0, 0.0}, {1.0, 1.0}, {0.0, 1.0}};
     for (int i = 0; i < 4; ++i) {
         quad[i].p[0] = xi[i][0]; quad[i].p[1] = xi[i][1];
-        quad[i].c[0] = v[i][0] / h - color_off[0];
-        quad[i].c[1] = v[i][2] / h - color_off[1];
+        quad[i].c[0] = snap_int(v[i][0] / h - color_off[0]);
+        quad[i].c[1] = snap_int(v[i][2] / h - color_off[1]);
     }
     ClipStatus st;
     cut_face_rec(quad, 4, 0, [&](const V2* poly, int num) {
@@ -535,8 +548,9 @@ static void pass_range(const Grid& G, const Velocity& vel, const Field& A, const
             for (const SubPoly& sp : polys) {
                 if (P.use_integral) {
                     // polygon_3D.cpp:257-487
-                    int iy0 = (int)std::floor((sp.pos[1] - origin[1]) / h);
-                    real f01 = ((sp.pos[1] - origin[1]) / h) - iy0;
+                    const real ry = snap_int((sp.pos[1] - origin[1]) / h);
+                    int iy0 = (int)std::floor(ry);
+                    real f01 = ry - iy0;
                     real q[3] = {sp.pos[0], 0.0, sp.pos[2]};
                     if (f01 < 0.5) {
                         real a = iy0 * h + origin[1], b = sp.pos[1];

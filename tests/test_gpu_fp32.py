@@ -1,0 +1,105 @@
+"""The chosen form (FP32 advection in local cell coordinates, double-float psi, compensated
+sums) against the FP64 oracle and the FP64 GPU form.
+
+Tolerances: 2e-6 relative L2 for one flux pass (FP32 round-off of O(1) values, with no
+O(psi) cancellation left), and 1e-4 after 40 plume steps at 32^3 against the FP64 form.
+"""
+import numpy as np
+import pytest
+
+import scenes
+from oracle import Oracle
+
+fia = pytest.importorskip("fia")
+
+pytestmark = pytest.mark.gpu
+
+O = Oracle()
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def make(n, precision, seed=1, cfl=2.0):
+    h = 1.0 / n
+    u, v, w = scenes.fourier_velocity(n, seed=seed)
+    rho = scenes.gaussian_blobs(n, seed=seed + 1)
+    g = fia.Grid3D(n, n, n, h, precision=precision)
+    for name, a in (("density", rho), ("u", u), ("v", v), ("w", w)):
+        g.set(name, a)
+    return g, h, u, v, w, rho, cfl * h
+
+
+PASSES = {
+    "weno6_integral": (0, 1, 1, 0, (0.5, 0.5)),
+    "weno6_zero_velocity": (0, 0, 0, 1, (0.5, 0.5)),
+    "error_1dy_linear": (2, 0, 0, 0, (0.0, 0.0)),
+    "linear_integral": (1, 2, 1, 0, (0.5, 0.5)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(PASSES))
+@pytest.mark.parametrize("comp", [-1, 0, 1, 2])
+def test_fp32_flux_pass(name, comp):
+    g, h, u, v, w, rho, dt = make(16, fia.FIA_FP32C)
+    interp, psi_mode, integ, zv, co = PASSES[name]
+    f = rho if comp < 0 else (u, v, w)[comp]
+    ref, _, _, _ = O.flux_pass((16, 16, 16), h, u, v, w, comp, f, dt, interp, psi_mode, integ, zv, co, 3)
+    got, st = g.debug_flux_pass(comp, f, dt, interp, psi_mode, integ, zv, co, 3)
+    g.close()
+    assert st == 0
+    assert rel(got, ref) < 2e-6
+
+
+@pytest.mark.parametrize("mode,k", [(0, 1), (1, 3), (2, 1)])
+def test_fp32_psi(mode, k):
+    g, h, u, v, w, rho, dt = make(16, fia.FIA_FP32C)
+    ref = O.psi(rho, (16, 16, 16), (0.5, 0.5, 0.5), h, mode, k)
+    got = g.debug_psi(-1, rho, mode, k)
+    g.close()
+    assert np.abs(got - ref).max() < 1e-9 * max(1.0, np.abs(ref).max())
+
+
+def test_fp32_backtrace():
+    g, h, u, v, w, rho, dt = make(16, fia.FIA_FP32C)
+    ref = O.backtrace_vertices((16, 16, 16), h, u, v, w, dt, -1, 0)
+    got = g.debug_backtrace(-1, dt, 0)
+    g.close()
+    assert np.abs(got - ref).max() < 1e-6 * h
+
+
+def test_fp32_move_substances():
+    g, h, u, v, w, rho, dt = make(32, fia.FIA_FP32C, seed=3)
+    g.move_substances_3D(dt, fia.advect_params())
+    got = g.get("density")
+    ref, _ = O.move_substances_3D((32, 32, 32), h, u, v, w, rho, dt, nthreads=8)
+    g.close()
+    assert rel(got, ref) < 2e-6
+
+
+def run_plume(n, precision, steps):
+    import scenes as sc
+    g = fia.Grid3D(n, n, n, 1.0 / n, precision=precision)
+    g.set("density", sc.plume_density(n))
+    for c, m in (("u", (n + 1) * n * n), ("v", n * (n + 1) * n), ("w", n * n * (n + 1))):
+        g.set(c, np.zeros(m))
+    sp = fia.step_params(cfl=2.0, solver={"tol": 1e-8, "max_iter": 20000})
+    masses = []
+    for i in range(steps):
+        sp.frame = i
+        rep = g.step(sp)
+        masses.append((rep.mass_before_advection, rep.mass_after))
+    out = g.get("density"), [g.get(c) for c in "uvw"], masses
+    g.close()
+    return out
+
+
+def test_fp32_plume_tracks_fp64():
+    r64, v64, m64 = run_plume(32, fia.FIA_FP64, 40)
+    r32, v32, m32 = run_plume(32, fia.FIA_FP32C, 40)
+    assert rel(r32, r64) < 1e-4
+    for a, b in zip(v32, v64):
+        assert rel(a, b) < 1e-4
+    for before, after in m32:
+        assert abs(after - before) <= 1e-6 * before

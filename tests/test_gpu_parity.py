@@ -122,7 +122,7 @@ def test_move_substances_cfl4_long_faces():
     g, h, u, v, w, rho, dt = make(16, 16, 16, seed=9, cfl=4.0)
     g.move_substances_3D(dt, fia.advect_params())
     got = g.get("density")
-    faces, pieces = g.pass_counters()
+    faces, pieces, both_sides, evals, launches = g.pass_counters()
     ref, _ = O.move_substances_3D((16, 16, 16), h, u, v, w, rho, dt)
     g.close()
     assert rel(got, ref) < 1e-10
