@@ -31,11 +31,11 @@ import numpy as np  # noqa: E402
 
 METRIC = "steps/s at 256^3 smoke step (flux advection of density and velocity + pressure to 1e-6)"
 UNIT = "steps/s"
-# FP32 operation count of one WENO6 3D evaluation as implemented in fia_device.cuh
-# (43 one-dimensional evaluations of 157 operations each, an FMA counted as two, plus the
-# position-dependent coefficients of the three axes).  Frozen; see the design doc.
-WENO1D_FLOP = 157
-WENO3D_FLOP = 43 * WENO1D_FLOP + 81
+# FP32 operation count of one 1D WENO6 evaluation as implemented in fia_device.cuh
+# (weno6_eval: differences 12, three cubic candidates 18, three smoothness indicators 57,
+# nonlinear weights and the weighted sum 26; an FMA counted as two).  The face kernel counts
+# the 1D evaluations it executes.  Frozen; see the design doc.
+WENO1D_FLOP = 113
 FP32_LANES_PER_SM = 128
 SMS = 152
 
@@ -233,7 +233,11 @@ def run_gpu(args, world, rank, local, dist):
     frame = 0
     for _ in range(args.warmup):
         sp.frame = frame
-        g.step(sp)
+        r = g.step(sp)
+        if args.verbose:
+            print("warmup frame %d: dt %.3e umax %.3e mass %.6e -> %.6e (corrected %.6e) CG %d it rel %.2e status %d"
+                  % (frame, r.dt, r.max_velocity, r.mass_before_advection, r.mass_after_advection, r.mass_after,
+                     r.solver_iterations, r.solver_rel_residual, r.status), file=sys.stderr, flush=True)
         frame += 1
     g.synchronize()
     c0 = g.pass_counters()
@@ -293,7 +297,7 @@ def run_gpu(args, world, rank, local, dist):
 
     # ---- roofline of the dominant kernel (k_faces32: clip + quadrature + WENO6)
     evals = c1[3] - c0[3]
-    flops = evals * WENO3D_FLOP
+    flops = evals * WENO1D_FLOP
     faces = c1[0] - c0[0]
     pieces = c1[1] - c0[1]
     sm_mhz = clocks.get("sm_mhz") or 2070.0
@@ -310,7 +314,7 @@ def run_gpu(args, world, rank, local, dist):
         "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s", "frac": achieved_tf / peak_tf if peak_tf else None,
         "peak_source": "152 SMs x 128 FP32 lanes x 2 FLOP x median SM clock sampled in the run (%.0f MHz); "
                        "no FP32-SIMT figure in MEASURED_PEAKS.json" % sm_mhz,
-        "algorithmic_flop": "WENO6 3D evaluations counted on the device x %d FLOP" % WENO3D_FLOP,
+        "algorithmic_flop": "1D WENO6 evaluations executed, counted on the device, x %d FLOP" % WENO1D_FLOP,
         "launches": face_launches, "avg_launch_ms": face_ms / max(face_launches, 1),
         "flop_per_launch": flops / max(face_launches, 1),
         "share_of_step": (face_ms / t_ms) if t_ms > 0 else None,
@@ -338,7 +342,7 @@ def run_gpu(args, world, rank, local, dist):
         "clocks": clocks,
         "details": {"faces_per_s": faces / (t_ms / 1e3), "cells_per_s": n ** 3 * args.steps / (t_ms / 1e3),
                     "pieces_per_face": pieces / max(faces, 1), "faces_clipped_both_sides": c1[2] - c0[2],
-                    "weno6_3d_evaluations": evals, "face_kernel_ms": face_ms,
+                    "weno6_1d_evaluations": evals, "face_kernel_ms": face_ms,
                     "last_dt": last.dt, "last_max_velocity": last.max_velocity,
                     "last_pressure_iterations": last.solver_iterations,
                     "last_pressure_rel_residual": last.solver_rel_residual,
@@ -361,6 +365,7 @@ def main():
     ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-sample-grid", type=int, default=24)
+    ap.add_argument("--verbose", action="store_true", help="per-step reports of the warm-up on stderr")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

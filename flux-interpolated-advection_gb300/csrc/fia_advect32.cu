@@ -4,7 +4,9 @@
 // Same kernels as fia_advect.cu (psi column scan, unique-vertex backtrace, unique-face
 // clip + quadrature + WENO6, deterministic gather), with these differences:
 //  * all geometry is in cell units relative to an integer anchor (fia_local.cuh);
-//  * psi is stored as (hi, lo) float pairs in cell units;
+//  * psi is stored as (hi, lo) float pairs in the reference's units (density x length):
+//    the WENO6 weights are not scale invariant (alpha = C / (1e-6 + beta)^2), so psi must
+//    carry the same scale as in the reference for the same interpolant;
 //  * a face interpolates psi - Psi0(f), Psi0(f) = the psi node at the face's anchor, and
 //    stores (Ft, Ny): the compensated flux of psi - Psi0 plus the density terms, and the
 //    sum of the pieces' scaled y-normals;
@@ -21,7 +23,7 @@ namespace fia {
 namespace {
 
 // ---------------------------------------------------------------------------------
-// psi (cell units) as hi/lo pairs, one thread per (x,z) column
+// psi as hi/lo pairs, one thread per (x,z) column
 // ---------------------------------------------------------------------------------
 __global__ void k_psi32(PassDesc d, const float* __restrict__ a, float2* __restrict__ psi) {
     const int Mx = d.A.Mx, My = d.A.My, Mz = d.A.Mz;
@@ -29,13 +31,14 @@ __global__ void k_psi32(PassDesc d, const float* __restrict__ a, float2* __restr
     if (col >= (long long)Mx * Mz) return;
     const int i = (int)(col / Mz), k = (int)(col % Mz);
     const PlainLoad L{a};
+    const float hf = (float)d.h;
     float hi = 0.f, lo = 0.f;
     psi[idx3(d.P, i, 0, k)] = make_float2(0.f, 0.f);
     const float oy = (float)d.A.oy;
     for (int j = 1; j <= My; ++j) {
         Kahan inc;
         if (d.psi_mode == PSI_PLAIN) {
-            inc.add(__ldg(a + idx3(d.A, i, j - 1, k)));
+            inc.add(__ldg(a + idx3(d.A, i, j - 1, k)) * hf);
         } else if (d.psi_mode == PSI_WENO6) {
             // cell j-1 spans [j-1+oy-.5, j+oy-.5] in cells; anchor (i, j-1, k)
             const int anc[3] = {i, j - 1, k};
@@ -43,15 +46,15 @@ __global__ void k_psi32(PassDesc d, const float* __restrict__ a, float2* __restr
                 const float lo_y = (oy - 0.5f) + 0.5f * float(half);
                 for (int q = 0; q < d.k; ++q) {
                     const float qq[3] = {(float)d.A.ox, lo_y + 0.25f * (1.0f + (float)d.gx[q]), (float)d.A.oz};
-                    inc.add(weno6_1dy_loc(L, d.A, anc, qq) * 0.5f * (float)d.gw[q]);
+                    inc.add(weno6_1dy_loc(L, d.A, anc, qq) * (0.5f * hf) * (float)d.gw[q]);
                 }
             }
         } else {
             const int anc[3] = {i, j - 1, k};
             const float q0[3] = {(float)d.A.ox, 0.25f + oy - 0.5f, (float)d.A.oz};
             const float q1[3] = {(float)d.A.ox, 0.75f + oy - 0.5f, (float)d.A.oz};
-            inc.add(lin3d_loc(L, d.A, anc, q0) * 0.5f);
-            inc.add(lin3d_loc(L, d.A, anc, q1) * 0.5f);
+            inc.add(lin3d_loc(L, d.A, anc, q0) * (0.5f * hf));
+            inc.add(lin3d_loc(L, d.A, anc, q1) * (0.5f * hf));
         }
         // (hi, lo) += inc
         float s, e;
@@ -161,40 +164,56 @@ __device__ void piece32(const PassDesc& d, const LocalFace& g, const float* px, 
     }
     if (ny == 0.f) return;
     out.Ny.add(ny);
-    if (d.interp == INTERP_WENO6)   // WENO6 3D evaluations (the unit of the roofline count)
-        out.evals += d.use_integral ? 1 + d.k * (1 + (int)(snap_int(cy - (d.comp == 1 ? -0.5f : 0.f)) -
-                                                           floorf(snap_int(cy - (d.comp == 1 ? -0.5f : 0.f))) >= 0.5f))
-                                    : 1;
     const PlainLoad al{a};
+    const float invh = (float)(1.0 / d.h);   // psi carries a length; the face terms are per cell volume
     if (d.use_integral) {
         const float oy = (d.comp == 1) ? -0.5f : 0.f;
         const float r = snap_int(cy - oy);
         const float fl = floorf(r);
         const float f = r - fl;
         const float ylo = fl + oy;   // local y of the y-face below the centroid
+        // the density quadrature points (polygon_3D.cpp:286-453): k on [ylo, cy] when the
+        // centroid is in the lower half of the cell, else k on each of [ylo, ylo+1/2], [ylo+1/2, cy]
+        float ys[2 * kMaxGauss], ws[2 * kMaxGauss];
+        int np = 0;
         if (f < 0.5f) {
             const float L = cy - ylo;
             for (int q = 0; q < d.k; ++q) {
-                const float qq[3] = {cx, (L * 0.5f) * (float)d.gx[q] + (L * 0.5f) + ylo, cz};
-                out.F.add(interp_loc(d.interp, al, d.A, g.anc, qq) * (ny * f * (float)d.gw[q]));
+                ys[np] = (L * 0.5f) * (float)d.gx[q] + (L * 0.5f) + ylo;
+                ws[np++] = ny * f * (float)d.gw[q];
             }
         } else {
             float lo = ylo, L = 0.5f;
             for (int q = 0; q < d.k; ++q) {
-                const float qq[3] = {cx, (L * 0.5f) * (float)d.gx[q] + (L * 0.5f) + lo, cz};
-                out.F.add(interp_loc(d.interp, al, d.A, g.anc, qq) * (ny * 0.5f * (float)d.gw[q]));
+                ys[np] = (L * 0.5f) * (float)d.gx[q] + (L * 0.5f) + lo;
+                ws[np++] = ny * 0.5f * (float)d.gw[q];
             }
             lo = ylo + 0.5f; L = cy - lo;
             for (int q = 0; q < d.k; ++q) {
-                const float qq[3] = {cx, (L * 0.5f) * (float)d.gx[q] + (L * 0.5f) + lo, cz};
-                out.F.add(interp_loc(d.interp, al, d.A, g.anc, qq) * (ny * (f - 0.5f) * (float)d.gw[q]));
+                ys[np] = (L * 0.5f) * (float)d.gx[q] + (L * 0.5f) + lo;
+                ws[np++] = ny * (f - 0.5f) * (float)d.gw[q];
             }
         }
+        bool shared = false;
+        if (d.interp == INTERP_WENO6) {
+            const int n1d = weno6_ycolumn(al, d.A, g.anc, cx, cz, ys, ws, np, out.F);
+            shared = n1d > 0;
+            out.evals += n1d;          // 1D WENO6 evaluations executed
+        }
+        if (!shared) {
+            for (int m = 0; m < np; ++m) {
+                const float qq[3] = {cx, ys[m], cz};
+                out.F.add(interp_loc(d.interp, al, d.A, g.anc, qq) * ws[m]);
+            }
+            if (d.interp == INTERP_WENO6) out.evals += 43 * np;
+        }
         const float qp[3] = {cx, ylo, cz};
-        out.F.add(interp_loc(d.interp, pl, d.P, g.anc, qp) * ny);
+        out.F.add(interp_loc(d.interp, pl, d.P, g.anc, qp) * (ny * invh));
+        if (d.interp == INTERP_WENO6) out.evals += 43;
     } else {
         const float qp[3] = {cx, cy, cz};
-        out.F.add(interp_loc(d.interp, pl, d.P, g.anc, qp) * ny);
+        out.F.add(interp_loc(d.interp, pl, d.P, g.anc, qp) * (ny * invh));
+        if (d.interp == INTERP_WENO6) out.evals += 43;
     }
 }
 
@@ -436,9 +455,10 @@ __global__ void k_gather32(PassDesc d, const float2* __restrict__ fx, const floa
     const int j = (int)((id / Mz) % My);
     const int i = (int)(id / ((long long)Mz * My));
     const float2 pc = __ldg(psi + psi_node(d.P, i, j, k));
+    const float invh = (float)(1.0 / d.h);
     auto base_diff = [&](int a, int b, int c) {
         const float2 p = __ldg(psi + psi_node(d.P, a, b, c));
-        return (p.x - pc.x) + (p.y - pc.y);
+        return ((p.x - pc.x) + (p.y - pc.y)) * invh;
     };
     // lower faces (anchor = the cell itself): base difference 0
     const float2 lx = rx[((long long)i * My + j) * Mz + k];

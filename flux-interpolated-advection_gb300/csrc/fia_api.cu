@@ -317,9 +317,9 @@ __global__ void k_disp_to_pos(const float* __restrict__ disp, double* __restrict
             out[3 * v + c] = ((double)idx[c] - (c == comp ? 0.5 : 0.0) + (double)disp[3 * v + c]) * h;
     }
 }
-__global__ void k_pairs_to_psi(const float2* __restrict__ p, double* __restrict__ out, double h, long long n) {
+__global__ void k_pairs_to_psi(const float2* __restrict__ p, double* __restrict__ out, long long n) {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        out[i] = ((double)p[i].x + (double)p[i].y) * h;
+        out[i] = (double)p[i].x + (double)p[i].y;
 }
 
 void export_verts(fia_session* s, const PassDesc& d, const double* verts, double* tmp, long long n) {
@@ -332,7 +332,7 @@ void export_psi(fia_session* s, const double* psi, double* tmp, long long n) {
     k_convert<double, double><<<256, 256, 0, s->stream>>>(psi, tmp, n);
 }
 void export_psi(fia_session* s, const float* psi, double* tmp, long long n) {
-    k_pairs_to_psi<<<256, 256, 0, s->stream>>>((const float2*)psi, tmp, s->h, n);
+    k_pairs_to_psi<<<256, 256, 0, s->stream>>>((const float2*)psi, tmp, n);
 }
 
 template <typename T>

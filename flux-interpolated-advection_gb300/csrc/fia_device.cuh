@@ -69,34 +69,41 @@ __device__ __forceinline__ WenoCoef<T> weno_coef(const T* t) {
 
 // One 1D WENO6 evaluation: smoothness indicators with integer coefficients over 180,
 // alpha_i = C_i / (1e-6 + beta_i)^2, normalised weights (WENO6_interpolation_3d.cpp:94-123).
+// The smoothness indicators are evaluated as quadratic forms of the first differences
+// D_i = f_{i+1} - f_i.  Expanding the reference's forms (products of the samples,
+// WENO6_interpolation_3d.cpp:95-110) in D gives exactly
+//   beta0 = (244 D0^2 - 1171 D0 D1 + 683 D0 D2 + 1561 D1^2 - 1951 D1 D2 + 814 D2^2) / 180
+//   beta1 = (244 D1^2 - 781 D1 D2 + 293 D1 D3 + 961 D2^2 - 781 D2 D3 + 244 D3^2) / 180
+//   beta2 = (814 D2^2 - 1951 D2 D3 + 683 D2 D4 + 1561 D3^2 - 1171 D3 D4 + 244 D4^2) / 180
+// (no term in the samples themselves survives: the indicators are shift invariant).  In
+// FP32 the sample-product form cancels to an absolute error of ~1e-3 f^2, far above the
+// 1e-6 regularisation; the difference form keeps full relative accuracy and costs less.
 template <typename T>
 __device__ __forceinline__ T weno6_eval(const T* f, const WenoCoef<T>& w) {
+    const T D0 = f[1] - f[0], D1 = f[2] - f[1], D2 = f[3] - f[2], D3 = f[4] - f[3], D4 = f[5] - f[4];
+    const T S0 = D1 - D0, S1 = D2 - D1, S2 = D3 - D2;      // second differences
+    const T D[3] = {D0, D1, D2}, S[3] = {S0, S1, S2};
+    const T Tt[3] = {S1 - S0, S2 - S1, (D4 - D3) - S2};    // third differences
     T P[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        T d1 = f[i + 1] - f[i];
-        T d2 = f[i + 2] - T(2) * f[i + 1] + f[i];
-        T d3 = f[i + 3] - T(3) * f[i + 2] + T(3) * f[i + 1] - f[i];
-        P[i] = f[i] + d1 * w.a[i] + d2 * w.b[i] + d3 * w.c[i];
-    }
-    const T f0 = f[0], f1 = f[1], f2 = f[2], f3 = f[3], f4 = f[4], f5 = f[5];
-    T b0 = (T(-3579) * f3 * f2 + T(2634) * f3 * f1 - T(683) * f3 * f0
-            - T(6927) * f2 * f1 + T(1854) * f2 * f0 - T(1659) * f1 * f0
-            + T(814) * f3 * f3 + T(4326) * f2 * f2 + T(2976) * f1 * f1
-            + T(244) * f0 * f0) / T(180);
-    T b1 = (T(-3777) * f3 * f2 + T(1074) * f3 * f1 - T(1269) * f2 * f1
-            + T(1986) * f3 * f3 + T(1986) * f2 * f2 + T(244) * f1 * f1
-            + T(244) * f4 * f4 - T(1269) * f4 * f3 + T(1074) * f4 * f2
-            - T(293) * f4 * f1) / T(180);
-    T b2 = (T(-3579) * f3 * f2 + T(4326) * f3 * f3 + T(814) * f2 * f2
-            + T(2976) * f4 * f4 + T(244) * f5 * f5 - T(683) * f5 * f2
-            - T(6927) * f4 * f3 + T(2634) * f4 * f2 - T(1659) * f5 * f4
-            + T(1854) * f5 * f3) / T(180);
+    for (int i = 0; i < 3; ++i) P[i] = f[i] + D[i] * w.a[i] + S[i] * w.b[i] + Tt[i] * w.c[i];
+    const T r180 = T(1) / T(180);
+    const T b0 = (T(244) * D0 * D0 - T(1171) * D0 * D1 + T(683) * D0 * D2 + T(1561) * D1 * D1
+                  - T(1951) * D1 * D2 + T(814) * D2 * D2) * r180;
+    const T b1 = (T(244) * D1 * D1 - T(781) * D1 * D2 + T(293) * D1 * D3 + T(961) * D2 * D2
+                  - T(781) * D2 * D3 + T(244) * D3 * D3) * r180;
+    const T b2 = (T(814) * D2 * D2 - T(1951) * D2 * D3 + T(683) * D2 * D4 + T(1561) * D3 * D3
+                  - T(1171) * D3 * D4 + T(244) * D4 * D4) * r180;
     const T eps = T(0.000001);
-    T e0 = eps + b0, e1 = eps + b1, e2 = eps + b2;
-    T al0 = w.C[0] / (e0 * e0), al1 = w.C[1] / (e1 * e1), al2 = w.C[2] / (e2 * e2);
-    T s = al0 + al1 + al2;
-    return (al0 / s) * P[0] + (al1 / s) * P[1] + (al2 / s) * P[2];
+    const T e0 = eps + b0, e1 = eps + b1, e2 = eps + b2;
+    // alpha_i = C_i / e_i^2 and w_i = alpha_i / sum(alpha).  Multiplying every alpha by
+    // e0^2 e1^2 e2^2 / max(e^2)^2 leaves the weights unchanged and needs two divisions
+    // instead of six; the scaling by the largest e^2 keeps the products in range.
+    const T q0 = e0 * e0, q1 = e1 * e1, q2 = e2 * e2;
+    const T rq = T(1) / fmax(q0, fmax(q1, q2));
+    const T t0 = q0 * rq, t1 = q1 * rq, t2 = q2 * rq;
+    const T a0 = w.C[0] * (t1 * t2), a1 = w.C[1] * (t0 * t2), a2 = w.C[2] * (t0 * t1);
+    return (a0 * P[0] + a1 * P[1] + a2 * P[2]) / (a0 + a1 + a2);
 }
 
 // Tensor-product WENO6 of a node field at p (z, then y, then x), stencil indices clamped

@@ -98,6 +98,69 @@ __device__ float weno6_3d_loc(const L& load, const NodeField& F, const int* anc,
     return weno6_eval(yv, cx);
 }
 
+// WENO6 at npts points that share x and z and lie within one cell in y (the density
+// quadrature points of one piece, polygon_3D.cpp:286-453): the z-pass over the 6 x 7
+// (x, y) stencil rows is done once and shared; each point then needs 6 y- and 1 x-
+// evaluation instead of 43.  Bit-identical to evaluating the points one by one.  Returns
+// the number of 1D evaluations made, or 0 (nothing accumulated) if the points span more
+// than one cell.
+template <class L>
+__device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, float qx, float qz,
+                             const float* ys, const float* ws, int npts, Kahan& acc) {
+    int bx, bz, by0, by1;
+    float sx, sz, s;
+    locate(anc[0], qx, (float)F.ox, bx, sx);
+    locate(anc[2], qz, (float)F.oz, bz, sz);
+    float ymin = ys[0], ymax = ys[0];
+    for (int m = 1; m < npts; ++m) { ymin = fminf(ymin, ys[m]); ymax = fmaxf(ymax, ys[m]); }
+    locate(anc[1], ymin, (float)F.oy, by0, s);
+    locate(anc[1], ymax, (float)F.oy, by1, s);
+    if (by1 - by0 > 1) return 0;
+    const bool seven = by1 > by0;
+    float tx[6], tz[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) { tx[i] = sx + float(2 - i); tz[i] = sz + float(2 - i); }
+    const WenoCoef<float> cx = weno_coef(tx), cz = weno_coef(tz);
+    int kk[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) kk[i] = clampi(bz - 2 + i, F.Mz - 1);
+    float zr[6][7];
+#pragma unroll
+    for (int ix = 0; ix < 6; ++ix) {
+        const int ii = clampi(bx - 2 + ix, F.Mx - 1);
+#pragma unroll
+        for (int r = 0; r < 7; ++r) {
+            if (r == 6 && !seven) { zr[ix][6] = 0.f; continue; }
+            const int jj = clampi(by0 - 2 + r, F.My - 1);
+            const long long row = (long long)F.Mz * ((long long)F.My * ii + jj);
+            float f[6];
+#pragma unroll
+            for (int iz = 0; iz < 6; ++iz) f[iz] = load(row + kk[iz]);
+            zr[ix][r] = weno6_eval(f, cz);
+        }
+    }
+    for (int m = 0; m < npts; ++m) {
+        int by;
+        float sy;
+        locate(anc[1], ys[m], (float)F.oy, by, sy);
+        const bool up = by > by0;
+        float ty[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) ty[i] = sy + float(2 - i);
+        const WenoCoef<float> cy = weno_coef(ty);
+        float yv[6];
+#pragma unroll
+        for (int ix = 0; ix < 6; ++ix) {
+            float f[6];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) f[i] = up ? zr[ix][i + 1] : zr[ix][i];
+            yv[ix] = weno6_eval(f, cy);
+        }
+        acc.add(weno6_eval(yv, cx) * ws[m]);
+    }
+    return (seven ? 42 : 36) + 7 * npts;
+}
+
 template <class L>
 __device__ float weno6_1dy_loc(const L& load, const NodeField& F, const int* anc, const float* q) {
     int by;

@@ -49,7 +49,9 @@ def test_fp32_flux_pass(name, comp):
     got, st = g.debug_flux_pass(comp, f, dt, interp, psi_mode, integ, zv, co, 3)
     g.close()
     assert st == 0
-    assert rel(got, ref) < 2e-6
+    # the 1Dy-linear error pass picks the nearest cell in x and z (a discontinuous choice),
+    # so FP32 centroids near a cell boundary move a few pieces to the neighbouring column
+    assert rel(got, ref) < (1e-5 if name == "error_1dy_linear" else 2e-6)
 
 
 @pytest.mark.parametrize("mode,k", [(0, 1), (1, 3), (2, 1)])
@@ -58,7 +60,8 @@ def test_fp32_psi(mode, k):
     ref = O.psi(rho, (16, 16, 16), (0.5, 0.5, 0.5), h, mode, k)
     got = g.debug_psi(-1, rho, mode, k)
     g.close()
-    assert np.abs(got - ref).max() < 1e-9 * max(1.0, np.abs(ref).max())
+    # the density itself is rounded to FP32 on upload (6e-8 relative)
+    assert np.abs(got - ref).max() < 2e-7 * np.abs(ref).max()
 
 
 def test_fp32_backtrace():
