@@ -24,7 +24,7 @@ REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libfia_%s.so" % platform.machine())
-SOURCES = ["fia_api.cu", "fia_advect.cu", "fia_advect32.cu", "fia_pressure.cu"]
+SOURCES = ["fia_api.cu", "fia_advect.cu", "fia_advect32.cu", "fia_pressure.cu", "fia_noalloc.cu"]
 HEADERS = ["fia_device.cuh", "fia_advect.cuh", "fia_local.cuh", "fia_pressure.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -188,6 +188,24 @@ int fia_calc_pressure_gradient_term_3D_host(fia_session* s, int host_dtype, void
                                             void* pressure, const fia_solver_params* sp,
                                             fia_solver_report* rep);
 
+/* move_substances_3D (FP64 plain form) on caller-owned DEVICE buffers, allocating nothing.
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc: a host
+ * application that owns all device memory and hands a plug-in only the buffers it may touch
+ * (a renderer or engine integration with a fixed memory budget), or a real-time loop where
+ * an allocation's latency and possible failure are not acceptable.  The scratch of the pass
+ * lives in a static device array of 23.6 MB that every GPU loading the library holds until
+ * the process exits; grids are limited to 64 cells per axis (larger grids return
+ * FIA_ERR_INVALID; fia_noalloc_error_string says why).  density_in and density_out must be
+ * distinct; stream is a cudaStream_t (NULL: the legacy default stream); the call returns
+ * after the pass has finished, with FIA_STATUS_* bits or an error code.  The first call on a
+ * device looks up the scratch's device address (cudaGetSymbolAddress), so make it before any
+ * stream capture.  All calls share the one scratch array: calls that overlap on the GPU
+ * (other streams or host threads) race on it. */
+int fia_move_substances_3D_noalloc(int nx, int ny, int nz, double cell_length, const double* density_in,
+                                   double* density_out, const double* u, const double* v, const double* w,
+                                   double time_step_length, const fia_advect_params* p, void* stream);
+const char* fia_noalloc_error_string(void);
+
 /* Test hooks: single pieces of the path on host data (FP64 buffers), mirroring the oracle. */
 /* one flux pass of a node field (comp -1 density, 0..2 velocity) with the session velocity */
 int fia_debug_flux_pass(fia_session* s, int comp, const double* field, double dt, int interp, int psi_mode,
