@@ -136,11 +136,17 @@ def max_over_ranks(x, dist):
     return float(t.item())
 
 
-def plume_state(n):
+MAX_DT = 1.0 / 60.0   # fia_default_step_params: one step per movie frame at 60 fps
+
+
+def plume_state(n, cfl):
+    """The plume density (sphere r=0.1 at (0.5,0.15,0.5)) in a developed flow: a seeded
+    divergence-free velocity (curl of 16 Fourier modes, wavenumbers 1-8) scaled so that the
+    frame-length step runs at the requested CFL number (max|u| = cfl h / dt)."""
     import scenes
     rho = scenes.plume_density(n)
-    z = np.zeros
-    return rho, z((n + 1) * n * n), z(n * (n + 1) * n), z(n * n * (n + 1))
+    u, v, w = scenes.fourier_velocity(n, seed=1, target_max=cfl * (1.0 / n) / MAX_DT)
+    return rho, u, v, w
 
 
 # ------------------------------------------------------------------------------------
@@ -205,8 +211,8 @@ def run_reference(args, world, rank, dist):
 
 
 def config_of(args, reference=False):
-    return {"workload": "smoke plume %d^3 (sphere source r=0.1 at (0.5,0.15,0.5), buoyancy 1.0, closed box), "
-                        "CFL %g, flux advection of density and velocity (WENO6, k=3, zero-velocity "
+    return {"workload": "smoke plume %d^3 (sphere source r=0.1 at (0.5,0.15,0.5), buoyancy 1.0, closed box) "
+                        "in a developed divergence-free flow (16 seeded Fourier modes) at CFL %g, flux advection of density and velocity (WENO6, k=3, zero-velocity "
                         "correction), pressure Jacobi-PCG to %g relative residual" % (args.grid, args.cfl, args.tol),
             "grid": args.grid, "cfl": args.cfl, "interpolation": "WENO6", "gauss_points": 3,
             "pressure_tol": args.tol, "pressure_solver": "Jacobi-PCG (FP64 dot products)",
@@ -225,10 +231,10 @@ def run_gpu(args, world, rank, local, dist):
     prec = fia.FIA_FP32C if args.precision == "fp32c" else fia.FIA_FP64
     n = args.grid
     g = fia.Grid3D(n, n, n, 1.0 / n, precision=prec)
-    rho, u, v, w = plume_state(n)
+    rho, u, v, w = plume_state(n, args.cfl)
     for name, a in (("density", rho), ("u", u), ("v", v), ("w", w)):
         g.set(name, a)
-    sp = fia.step_params(cfl=args.cfl, solver={"tol": args.tol, "max_iter": 20000})
+    sp = fia.step_params(cfl=args.cfl, max_dt=MAX_DT, solver={"tol": args.tol, "max_iter": 20000})
     stream = torch.cuda.ExternalStream(g.stream())
     frame = 0
     for _ in range(args.warmup):

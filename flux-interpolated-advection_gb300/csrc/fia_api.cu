@@ -35,6 +35,7 @@ struct fia_session {
     void* pw[5];                 // pressure work vectors r z d q (+ spare)
     double* part; double* scal; double* sums;
     unsigned* status; unsigned long long* counters;
+    unsigned* ticket;            // last-block counters of the fused CG kernels
     double* red_part; double* red_out;
     std::vector<void*> allocations;
 };
@@ -260,21 +261,33 @@ int advect_velocity(fia_session* s, double dt, const fia_advect_params* p) {
 }
 
 template <typename T>
+PressureWork<T> pressure_work(fia_session* s) {
+    PressureWork<T> W;
+    W.p = (T*)s->pres; W.r = (T*)s->pw[0]; W.z = (T*)s->pw[1]; W.d = (T*)s->pw[2]; W.q = (T*)s->pw[3];
+    W.d2 = (T*)s->pw[4]; W.ticket = s->ticket;
+    W.part = s->part; W.scal = s->scal; W.sums = s->sums;
+    return W;
+}
+
+PoissonGrid poisson_grid(const fia_session* s) {
+    return PoissonGrid{s->N[0], s->N[1], s->N[2], s->N[0] * s->N[1] * s->N[2] - 1, nullptr};
+}
+
+template <typename T>
 int pressure(fia_session* s, const fia_solver_params* sp, fia_solver_report* rep, bool subtract) {
     fia_solver_params def;
     fia_default_solver_params(&def);
     if (!sp) sp = &def;
     if (sp->method != FIA_SOLVER_PCG_JACOBI) return FIA_ERR_UNSUPPORTED;
-    PressureWork<T> W;
-    W.p = (T*)s->pres; W.r = (T*)s->pw[0]; W.z = (T*)s->pw[1]; W.d = (T*)s->pw[2]; W.q = (T*)s->pw[3];
-    W.part = s->part; W.scal = s->scal; W.sums = s->sums;
+    PressureWork<T> W = pressure_work<T>(s);
+    const PoissonGrid g = poisson_grid(s);
     PressureReport r;
-    CK(pressure_solve<T>(W, s->N[0], s->N[1], s->N[2], s->h, (const T*)s->vel[0], (const T*)s->vel[1],
-                         (const T*)s->vel[2], sp->tol, sp->max_iter, &r, s->stream));
-    s->launches += 4 + 5ull * (unsigned long long)r.iterations;   // rhs, precondition (+ finals), 5 per CG iteration
+    CK(pressure_solve<T>(W, g, s->h, (const T*)s->vel[0], (const T*)s->vel[1], (const T*)s->vel[2], sp->tol,
+                         sp->max_iter, &r, s->stream));
+    s->launches += (unsigned long long)r.launches;
     if (subtract) {
-        CK(subtract_gradient<T>((const T*)s->pres, (T*)s->vel[0], (T*)s->vel[1], (T*)s->vel[2], s->N[0], s->N[1],
-                                s->N[2], s->h, s->part, s->sums, s->stream));
+        CK(subtract_gradient<T>((const T*)s->pres, (T*)s->vel[0], (T*)s->vel[1], (T*)s->vel[2], g, s->h, s->part,
+                                s->sums, s->stream));
         s->launches += 3;
         double loss[3];
         CK(cudaMemcpyAsync(loss, s->sums, 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
@@ -550,8 +563,8 @@ fia_session* fia_create(int nx, int ny, int nz, double cell_length, int precisio
     A(s->rho, fb); A(s->rho_next, fb); A(s->pres, fb); A(s->cbuf, (size_t)big * 8); A(s->psi, pb);
     for (int c = 0; c < 3; ++c) { A(s->vel[c], fb); A(s->vel_next[c], fb); A(s->flux[c], pb); A(s->flux_rev[c], pb); }
     A(s->verts, 3 * fb);
-    for (int q = 0; q < 4; ++q) A(s->pw[q], fb);
-    s->pw[4] = nullptr;
+    for (int q = 0; q < 5; ++q) A(s->pw[q], fb);
+    { void* t2; A(t2, 4 * sizeof(unsigned)); s->ticket = (unsigned*)t2; }
     void* t;
     A(t, pressure_partials() * sizeof(double)); s->part = (double*)t;
     A(t, 8 * sizeof(double)); s->scal = (double*)t;
