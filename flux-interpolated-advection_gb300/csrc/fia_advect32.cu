@@ -373,7 +373,7 @@ __device__ __forceinline__ long long psi_node(const NodeField& P, int i, int j, 
     return idx3(P, clampi(i, P.Mx - 1), clampi(j, P.My - 1), clampi(k, P.Mz - 1));
 }
 
-__global__ void __launch_bounds__(128) k_faces32(PassDesc d, int fam, const float* __restrict__ a,
+__global__ void __launch_bounds__(128, 4) k_faces32(PassDesc d, int fam, const float* __restrict__ a,
                                                  const float2* __restrict__ psi, const float* __restrict__ disp,
                                                  float2* __restrict__ flux, float2* __restrict__ flux_rev,
                                                  unsigned* status, unsigned long long* counters) {

@@ -3,6 +3,7 @@
 #include "../../include/fia.h"
 #include "fia_advect.cuh"
 #include "fia_pressure.cuh"
+#include "fia_unet.cuh"
 
 #include <cstdio>
 #include <cstring>
@@ -38,6 +39,13 @@ struct fia_session {
     unsigned* ticket;            // last-block counters of the fused CG kernels
     double* red_part; double* red_out;
     std::vector<void*> allocations;
+    // solids and the pinned pressure cell
+    unsigned char* solid = nullptr;
+    int pin = 0;
+    long long n_free = 0;
+    // learned preconditioner (created by fia_learned_init / fia_learned_set_weights)
+    unet::Net* net = nullptr;
+    cudaEvent_t pev[2] = {nullptr, nullptr};
 };
 
 namespace {
@@ -270,7 +278,58 @@ PressureWork<T> pressure_work(fia_session* s) {
 }
 
 PoissonGrid poisson_grid(const fia_session* s) {
-    return PoissonGrid{s->N[0], s->N[1], s->N[2], s->N[0] * s->N[1] * s->N[2] - 1, nullptr};
+    return PoissonGrid{s->N[0], s->N[1], s->N[2], s->pin, s->solid};
+}
+
+// Flexible CG with the learned preconditioner (FP32C sessions), Jacobi-PCG after
+// fallback_iter iterations without convergence.
+int pressure_fcg(fia_session* s, const fia_solver_params* sp, PressureReport& r, int& fcg_its, double& pms) {
+    if (!s->net) return FIA_ERR_INVALID;
+    using T = float;
+    PressureWork<T> W = pressure_work<T>(s);
+    const PoissonGrid g = poisson_grid(s);
+    const T *u = (const T*)s->vel[0], *v = (const T*)s->vel[1], *w = (const T*)s->vel[2];
+    double br[2];
+    CK(pressure_rhs<T>(W, g, s->h, u, v, w, false, br, s->stream));
+    s->launches += 2;
+    r.iterations = 0; r.status = 0; r.rel_residual = 0.0; r.launches = 0;
+    fcg_its = 0; pms = 0.0;
+    if (br[0] == 0.0) return FIA_OK;
+    CK(fcg_begin<T>(W, br[0], br[1], sp->tol, s->stream));
+    s->launches += 1;
+    if (!s->pev[0]) { CK(cudaEventCreate(&s->pev[0])); CK(cudaEventCreate(&s->pev[1])); }
+    T* dold = W.d;
+    T* dnew = W.d2;
+    const int cap = std::min(sp->fallback_iter, sp->max_iter);
+    double st[3] = {br[1], br[1] <= sp->tol * sp->tol * br[0] ? 1.0 : 0.0, 0.0};
+    int it = 0;
+    while (it < cap && st[1] == 0.0) {
+        CK(cudaEventRecord(s->pev[0], s->stream));
+        CK(unet::net_apply(s->net, g, W.r, W.z, W.scal + kScalRR, (double)s->n_free, s->stream));
+        CK(cudaEventRecord(s->pev[1], s->stream));
+        CK(fcg_iteration<T>(W, g, it == 0, dold, dnew, s->stream));
+        std::swap(dold, dnew);
+        s->launches += (unsigned long long)unet::net_launches(s->net) + 3;
+        CK(solver_state(W.scal, st, s->stream));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, s->pev[0], s->pev[1]));
+        pms += ms;
+        ++it;
+    }
+    fcg_its = it;
+    r.iterations = it;
+    r.rel_residual = std::sqrt(st[0] / br[0]);
+    if (st[1] != 0.0) return FIA_OK;
+    // fallback: Jacobi-PCG from the current pressure
+    double br2[2];
+    CK(pressure_rhs<T>(W, g, s->h, u, v, w, true, br2, s->stream));
+    PressureReport r2;
+    CK(pressure_pcg<T>(W, g, br[0], br2[1], sp->tol, std::max(0, sp->max_iter - it), &r2, s->stream));
+    s->launches += 2 + (unsigned long long)r2.launches;
+    r.iterations = it + r2.iterations;
+    r.rel_residual = r2.rel_residual;
+    r.status = r2.status;
+    return FIA_STATUS_SOLVER_FALLBACK;
 }
 
 template <typename T>
@@ -278,13 +337,25 @@ int pressure(fia_session* s, const fia_solver_params* sp, fia_solver_report* rep
     fia_solver_params def;
     fia_default_solver_params(&def);
     if (!sp) sp = &def;
-    if (sp->method != FIA_SOLVER_PCG_JACOBI) return FIA_ERR_UNSUPPORTED;
+    if (sp->method != FIA_SOLVER_PCG_JACOBI && sp->method != FIA_SOLVER_FCG_LEARNED) return FIA_ERR_INVALID;
+    if (!(sp->tol > 0.0) || sp->max_iter < 1) return FIA_ERR_INVALID;
     PressureWork<T> W = pressure_work<T>(s);
     const PoissonGrid g = poisson_grid(s);
     PressureReport r;
-    CK(pressure_solve<T>(W, g, s->h, (const T*)s->vel[0], (const T*)s->vel[1], (const T*)s->vel[2], sp->tol,
-                         sp->max_iter, &r, s->stream));
-    s->launches += (unsigned long long)r.launches;
+    int extra = 0, fcg_its = 0;
+    double pms = 0.0;
+    if (sp->method == FIA_SOLVER_FCG_LEARNED) {
+        if (s->precision != FIA_FP32C) return FIA_ERR_UNSUPPORTED;
+        if (!s->net) return FIA_ERR_INVALID;
+        if (sp->fallback_iter < 1) return FIA_ERR_INVALID;
+        const int rc = pressure_fcg(s, sp, r, fcg_its, pms);
+        if (rc < 0) return rc;
+        extra = rc;
+    } else {
+        CK(pressure_solve<T>(W, g, s->h, (const T*)s->vel[0], (const T*)s->vel[1], (const T*)s->vel[2], sp->tol,
+                             sp->max_iter, &r, s->stream));
+        s->launches += (unsigned long long)r.launches;
+    }
     if (subtract) {
         CK(subtract_gradient<T>((const T*)s->pres, (T*)s->vel[0], (T*)s->vel[1], (T*)s->vel[2], g, s->h, s->part,
                                 s->sums, s->stream));
@@ -294,9 +365,40 @@ int pressure(fia_session* s, const fia_solver_params* sp, fia_solver_report* rep
         CK(cudaStreamSynchronize(s->stream));
         for (int c = 0; c < 3; ++c) s->wall_loss[c] += loss[c];
     }
-    int status = r.status ? FIA_STATUS_SOLVER_CAP : 0;
-    if (rep) { rep->iterations = r.iterations; rep->rel_residual = r.rel_residual; rep->status = status; }
+    const int status = (r.status ? FIA_STATUS_SOLVER_CAP : 0) | extra;
+    if (rep) {
+        rep->iterations = r.iterations; rep->rel_residual = r.rel_residual; rep->status = status;
+        rep->fcg_iterations = fcg_its; rep->precond_ms = pms;
+    }
     return status;
+}
+
+// Solves the projection of the current velocity to tol with Jacobi-PCG (pressure untouched)
+// and keeps (r = -div(u) h, p) as a training pair of the learned preconditioner.
+int capture_pair(fia_session* s, double tol) {
+    if (s->precision != FIA_FP32C || !s->net) return FIA_ERR_INVALID;
+    using T = float;
+    PressureWork<T> W = pressure_work<T>(s);
+    const PoissonGrid g = poisson_grid(s);
+    // the solve runs on a copy of the pressure so that the session's pressure is kept
+    PressureWork<T> C = W;
+    const long long nc = (long long)s->N[0] * s->N[1] * s->N[2];
+    T* pkeep = (T*)s->cbuf;
+    CK(cudaMemcpyAsync(pkeep, s->pres, nc * sizeof(T), cudaMemcpyDeviceToDevice, s->stream));
+    PressureReport r;
+    CK(pressure_solve<T>(C, g, s->h, (const T*)s->vel[0], (const T*)s->vel[1], (const T*)s->vel[2], tol, 100000, &r,
+                         s->stream));
+    s->launches += (unsigned long long)r.launches;
+    // r = -b into W.z (its pressure argument W.q is a scratch that gets zeroed)
+    PressureWork<T> R = W;
+    R.r = W.z; R.p = W.q;
+    double br[2];
+    CK(pressure_rhs<T>(R, g, s->h, (const T*)s->vel[0], (const T*)s->vel[1], (const T*)s->vel[2], false, br,
+                       s->stream));
+    const int id = unet::net_add_pair(s->net, g, W.z, (const float*)s->pres, s->stream);
+    CK(cudaMemcpyAsync(s->pres, pkeep, nc * sizeof(T), cudaMemcpyDeviceToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return id < 0 ? FIA_ERR_CUDA : FIA_OK;
 }
 
 template <typename T>
@@ -385,24 +487,59 @@ int debug_psi(fia_session* s, int comp, const double* field, int mode, int k, do
 // density = max(density, value) in the cells whose centre lies in the sphere
 template <typename T>
 __global__ void k_source(T* __restrict__ rho, int nx, int ny, int nz, double h, double cx, double cy, double cz,
-                         double r, double value) {
+                         double r, double value, const unsigned char* __restrict__ solid) {
     const long long n = (long long)nx * ny * nz;
     for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
         const int iz = (int)(c % nz), iy = (int)((c / nz) % ny), ix = (int)(c / ((long long)nz * ny));
         const double x = (ix + 0.5) * h - cx, y = (iy + 0.5) * h - cy, z = (iz + 0.5) * h - cz;
+        if (solid && solid[c]) continue;
         if (x * x + y * y + z * z <= r * r && (double)rho[c] < value) rho[c] = (T)value;
     }
 }
 
-// v += dt * b * (rho_below + rho_above) / 2 on interior y-faces
+// v += dt * b * (rho_below + rho_above) / 2 on interior y-faces between fluid cells
 template <typename T>
-__global__ void k_buoyancy(T* __restrict__ v, const T* __restrict__ rho, int nx, int ny, int nz, double a) {
+__global__ void k_buoyancy(T* __restrict__ v, const T* __restrict__ rho, int nx, int ny, int nz, double a,
+                           const unsigned char* __restrict__ solid) {
     const long long n = (long long)nx * (ny + 1) * nz;
     for (long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x; f < n; f += (long long)gridDim.x * blockDim.x) {
         const int iz = (int)(f % nz), iy = (int)((f / nz) % (ny + 1)), ix = (int)(f / ((long long)nz * (ny + 1)));
         if (iy == 0 || iy == ny) continue;
         const long long c = ((long long)ix * ny + iy) * nz + iz;
+        if (solid && (solid[c] || solid[c - nz])) continue;
         v[f] = (T)((double)v[f] + a * 0.5 * ((double)rho[c - nz] + (double)rho[c]));
+    }
+}
+
+// density = 0 in solid cells
+template <typename T>
+__global__ void k_clear_solid(T* __restrict__ rho, long long n, const unsigned char* __restrict__ solid) {
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        if (solid[c]) rho[c] = (T)0;
+}
+
+// zero velocity on faces touching a solid cell (all three families)
+template <typename T>
+__global__ void k_solid_faces(T* __restrict__ u, T* __restrict__ v, T* __restrict__ w, int nx, int ny, int nz,
+                              const unsigned char* __restrict__ solid) {
+    const long long nu = (long long)(nx + 1) * ny * nz, nv = (long long)nx * (ny + 1) * nz;
+    const long long nw = (long long)nx * ny * (nz + 1);
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nu + nv + nw; t += (long long)gridDim.x * blockDim.x) {
+        if (t < nu) {
+            const int iz = (int)(t % nz), iy = (int)((t / nz) % ny), ix = (int)(t / ((long long)nz * ny));
+            const long long c = ((long long)ix * ny + iy) * nz + iz, sx = (long long)ny * nz;
+            if ((ix < nx && solid[c]) || (ix > 0 && solid[c - sx])) u[t] = (T)0;
+        } else if (t < nu + nv) {
+            const long long f = t - nu;
+            const int iz = (int)(f % nz), iy = (int)((f / nz) % (ny + 1)), ix = (int)(f / ((long long)nz * (ny + 1)));
+            const long long c = ((long long)ix * ny + iy) * nz + iz;
+            if ((iy < ny && solid[c]) || (iy > 0 && solid[c - nz])) v[f] = (T)0;
+        } else {
+            const long long f = t - nu - nv;
+            const int iz = (int)(f % (nz + 1)), iy = (int)((f / (nz + 1)) % ny), ix = (int)(f / ((long long)(nz + 1) * ny));
+            const long long c = ((long long)ix * ny + iy) * nz + iz;
+            if ((iz < nz && solid[c]) || (iz > 0 && solid[c - 1])) w[f] = (T)0;
+        }
     }
 }
 
@@ -429,7 +566,7 @@ int step(fia_session* s, const fia_step_params* p, fia_step_report* rep) {
     if (p->source) {
         k_source<T><<<1024, 256, 0, s->stream>>>((T*)s->rho, nx, ny, nz, s->h, p->source_center[0],
                                                  p->source_center[1], p->source_center[2], p->source_radius,
-                                                 p->source_density);
+                                                 p->source_density, s->solid);
         s->launches += 1;
     }
     double umax = 0.0, m;
@@ -440,18 +577,26 @@ int step(fia_session* s, const fia_step_params* p, fia_step_report* rep) {
     double dt = p->max_dt;
     if (umax > 0.0) dt = std::min(dt, p->cfl * s->h / umax);
     if (p->buoyancy != 0.0) {
-        k_buoyancy<T><<<1024, 256, 0, s->stream>>>((T*)s->vel[1], (const T*)s->rho, nx, ny, nz, dt * p->buoyancy);
+        k_buoyancy<T><<<1024, 256, 0, s->stream>>>((T*)s->vel[1], (const T*)s->rho, nx, ny, nz, dt * p->buoyancy,
+                                                   s->solid);
         s->launches += 1;
     }
     fia_solver_report sr;
     std::memset(&sr, 0, sizeof(sr));
+    auto project = [&]() -> int {
+        if (p->capture_pair) {
+            const int c = capture_pair(s, p->capture_tol);
+            if (c < 0) return c;
+        }
+        return pressure<T>(s, &p->solver, &sr, true);
+    };
     if (p->frame == 0) {
-        if ((r = pressure<T>(s, &p->solver, &sr, true)) < 0) return r;
+        if ((r = project()) < 0) return r;
         status |= r;
         if ((r = advect_velocity<T>(s, dt, &p->advect)) < 0) return r;
     } else {
         if ((r = advect_velocity<T>(s, dt, &p->advect)) < 0) return r;
-        if ((r = pressure<T>(s, &p->solver, &sr, true)) < 0) return r;
+        if ((r = project()) < 0) return r;
         status |= r;
     }
     status |= finish_status(s);
@@ -459,6 +604,10 @@ int step(fia_session* s, const fia_step_params* p, fia_step_report* rep) {
     if ((r = read_reduction<T>(s, s->rho, nc, 0, &m0)) != FIA_OK) return r;
     if ((r = move_substances<T>(s, dt, &p->advect)) < 0) return r;
     status |= finish_status(s);
+    if (s->solid) {
+        k_clear_solid<T><<<1024, 256, 0, s->stream>>>((T*)s->rho, nc, s->solid);
+        s->launches += 1;
+    }
     if ((r = read_reduction<T>(s, s->rho, nc, 0, &m1)) != FIA_OK) return r;
     double m2 = m1;
     if (p->mass_correction && m1 != 0.0 && m0 != 0.0) {
@@ -471,6 +620,8 @@ int step(fia_session* s, const fia_step_params* p, fia_step_report* rep) {
         rep->mass_before_advection = m0 * V; rep->mass_after_advection = m1 * V; rep->mass_after = m2 * V;
         rep->solver_iterations = sr.iterations; rep->solver_rel_residual = sr.rel_residual;
         rep->status = status;
+        rep->solver_fcg_iterations = sr.fcg_iterations;
+        rep->precond_ms = sr.precond_ms;
     }
     return status;
 }
@@ -494,6 +645,8 @@ void fia_default_step_params(fia_step_params* p) {
     p->source_density = 1.0;
     p->mass_correction = 1;
     p->frame = 0;
+    p->capture_pair = 0;
+    p->capture_tol = 1e-10;
 }
 
 int fia_step(fia_session* s, const fia_step_params* p, fia_step_report* rep) {
@@ -533,6 +686,7 @@ void fia_default_solver_params(fia_solver_params* p) {
     p->tol = 1e-6;
     p->max_iter = 10000;
     p->method = FIA_SOLVER_PCG_JACOBI;
+    p->fallback_iter = 200;
 }
 
 fia_session* fia_create(int nx, int ny, int nz, double cell_length, int precision) {
@@ -545,6 +699,8 @@ fia_session* fia_create(int nx, int ny, int nz, double cell_length, int precisio
     s->es = precision == FIA_FP64 ? sizeof(double) : sizeof(float);
     s->last_status = 0; s->status_pending = false; s->counters_pending = false; s->launches = 0;
     s->counters_host[0] = s->counters_host[1] = s->counters_host[2] = s->counters_host[3] = 0;
+    s->pin = nx * ny * nz - 1;
+    s->n_free = (long long)nx * ny * nz - 1;
     if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
         g_last_error = "fia_create: stream"; delete s; return nullptr;
     }
@@ -613,6 +769,9 @@ void fia_destroy(fia_session* s) {
     if (!s) return;
     cudaStreamSynchronize(s->stream);
     for (cudaEvent_t e : s->prof_ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : s->pev) if (e) cudaEventDestroy(e);
+    unet::net_destroy(s->net);
+    if (s->solid) cudaFree(s->solid);
     for (void* p : s->allocations) cudaFree(p);
     cudaStreamDestroy(s->stream);
     delete s;
@@ -801,6 +960,197 @@ int fia_debug_psi(fia_session* s, int comp, const double* field, int mode, int k
         return FIA_ERR_INVALID;
     return s->precision == FIA_FP64 ? debug_psi<double>(s, comp, field, mode, k, out)
                                     : debug_psi<float>(s, comp, field, mode, k, out);
+}
+
+// ------------------------------- solids -------------------------------------------
+int fia_set_solid_spheres(fia_session* s, int count, const double* centers, const double* radii) {
+    if (!s || count < 0 || (count > 0 && (!centers || !radii))) return FIA_ERR_INVALID;
+    const int nx = s->N[0], ny = s->N[1], nz = s->N[2];
+    const long long nc = (long long)nx * ny * nz;
+    CK(cudaStreamSynchronize(s->stream));
+    if (count == 0) {
+        if (s->solid) CK(cudaFree(s->solid));
+        s->solid = nullptr;
+        s->pin = (int)(nc - 1);
+        s->n_free = nc - 1;
+        return FIA_OK;
+    }
+    std::vector<unsigned char> m(nc, 0);
+    long long nsolid = 0;
+    for (int ix = 0; ix < nx; ++ix)
+        for (int iy = 0; iy < ny; ++iy)
+            for (int iz = 0; iz < nz; ++iz) {
+                const double x = (ix + 0.5) * s->h, y = (iy + 0.5) * s->h, z = (iz + 0.5) * s->h;
+                for (int k = 0; k < count; ++k) {
+                    const double dx = x - centers[3 * k], dy = y - centers[3 * k + 1], dz = z - centers[3 * k + 2];
+                    if (dx * dx + dy * dy + dz * dz <= radii[k] * radii[k]) {
+                        m[((long long)ix * ny + iy) * nz + iz] = 1;
+                        ++nsolid;
+                        break;
+                    }
+                }
+            }
+    long long pin = nc - 1;
+    while (pin >= 0 && m[pin]) --pin;
+    if (pin < 0) return FIA_ERR_INVALID;   // no fluid cell left
+    if (!s->solid) CK(cudaMalloc(&s->solid, nc));
+    CK(cudaMemcpy(s->solid, m.data(), nc, cudaMemcpyHostToDevice));
+    s->pin = (int)pin;
+    s->n_free = nc - nsolid - 1;
+    // no velocity through solid faces, no density inside
+    if (s->precision == FIA_FP64) {
+        k_solid_faces<double><<<1024, 256, 0, s->stream>>>((double*)s->vel[0], (double*)s->vel[1], (double*)s->vel[2],
+                                                           nx, ny, nz, s->solid);
+        k_clear_solid<double><<<1024, 256, 0, s->stream>>>((double*)s->rho, nc, s->solid);
+    } else {
+        k_solid_faces<float><<<1024, 256, 0, s->stream>>>((float*)s->vel[0], (float*)s->vel[1], (float*)s->vel[2], nx,
+                                                          ny, nz, s->solid);
+        k_clear_solid<float><<<1024, 256, 0, s->stream>>>((float*)s->rho, nc, s->solid);
+    }
+    s->launches += 2;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s->stream));
+    return FIA_OK;
+}
+
+int fia_get_solid_mask(fia_session* s, unsigned char* out) {
+    if (!s || !out) return FIA_ERR_INVALID;
+    const long long nc = (long long)s->N[0] * s->N[1] * s->N[2];
+    if (!s->solid) { std::memset(out, 0, nc); return FIA_OK; }
+    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaMemcpy(out, s->solid, nc, cudaMemcpyDeviceToHost));
+    return FIA_OK;
+}
+
+// ------------------------------- learned preconditioner ---------------------------
+static int ensure_net(fia_session* s) {
+    if (s->precision != FIA_FP32C) return FIA_ERR_UNSUPPORTED;
+    if (!s->net) {
+        s->net = unet::net_create(s->N[0], s->N[1], s->N[2], s->stream);
+        if (!s->net) { g_last_error = "fia_learned: device allocation failed"; return FIA_ERR_NOMEM; }
+    }
+    return FIA_OK;
+}
+
+long long fia_learned_num_parameters(void) { return unet::num_parameters(); }
+
+int fia_learned_init(fia_session* s, unsigned long long seed) {
+    if (!s) return FIA_ERR_INVALID;
+    int r = ensure_net(s);
+    if (r != FIA_OK) return r;
+    CK(unet::net_init(s->net, seed));
+    return FIA_OK;
+}
+
+int fia_learned_set_weights(fia_session* s, const float* w, long long count) {
+    if (!s || !w || count != unet::num_parameters()) return FIA_ERR_INVALID;
+    int r = ensure_net(s);
+    if (r != FIA_OK) return r;
+    CK(unet::net_set_weights(s->net, w, count));
+    return FIA_OK;
+}
+
+int fia_learned_get_weights(fia_session* s, float* w, long long count) {
+    if (!s || !w || !s->net || count != unet::num_parameters()) return FIA_ERR_INVALID;
+    CK(unet::net_get_weights(s->net, w, count));
+    return FIA_OK;
+}
+
+int fia_learned_add_pair(fia_session* s, const float* r, const float* p) {
+    if (!s || !r || !p || !s->net) return FIA_ERR_INVALID;
+    const long long nc = (long long)s->N[0] * s->N[1] * s->N[2];
+    float *dr = (float*)s->pw[0], *dp = (float*)s->pw[1];
+    CK(cudaMemcpyAsync(dr, r, nc * 4, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(dp, p, nc * 4, cudaMemcpyHostToDevice, s->stream));
+    const int id = unet::net_add_pair(s->net, poisson_grid(s), dr, dp, s->stream);
+    return id < 0 ? FIA_ERR_INVALID : FIA_OK;
+}
+
+int fia_learned_num_pairs(fia_session* s) {
+    if (!s || !s->net) return 0;
+    return unet::net_num_pairs(s->net);
+}
+
+int fia_learned_loss(fia_session* s, int pair, double* loss) {
+    if (!s || !s->net || !loss || pair < 0 || pair >= unet::net_num_pairs(s->net)) return FIA_ERR_INVALID;
+    CK(unet::net_loss(s->net, poisson_grid(s), pair, false, loss, s->stream));
+    return FIA_OK;
+}
+
+int fia_learned_calibrate(fia_session* s, int pair) {
+    if (!s || !s->net || pair < 0 || pair >= unet::net_num_pairs(s->net)) return FIA_ERR_INVALID;
+    CK(unet::net_calibrate(s->net, poisson_grid(s), pair, s->stream));
+    return FIA_OK;
+}
+
+int fia_learned_train_step(fia_session* s, const int* pairs, int batch, double lr, double* losses) {
+    if (!s || !s->net || !pairs || batch < 1 || !(lr > 0.0)) return FIA_ERR_INVALID;
+    const int np = unet::net_num_pairs(s->net);
+    for (int i = 0; i < batch; ++i)
+        if (pairs[i] < 0 || pairs[i] >= np) return FIA_ERR_INVALID;
+    const PoissonGrid g = poisson_grid(s);
+    for (int i = 0; i < batch; ++i) {
+        double l = 0.0;
+        CK(unet::net_loss(s->net, g, pairs[i], true, &l, s->stream));
+        if (losses) losses[i] = l;
+    }
+    CK(unet::net_adam_step(s->net, lr, batch, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FIA_OK;
+}
+
+int fia_learned_level_dims(fia_session* s, int level, int* dims3) {
+    if (!s || !dims3 || level < 0 || level > 3) return FIA_ERR_INVALID;
+    int r = ensure_net(s);
+    if (r != FIA_OK) return r;
+    unet::net_level_dims(s->net, level, dims3);
+    return FIA_OK;
+}
+
+int fia_debug_unet_forward(fia_session* s, const float* x0, float* y) {
+    if (!s || !s->net || !x0 || !y) return FIA_ERR_INVALID;
+    int d[3];
+    unet::net_level_dims(s->net, 0, d);
+    const long long n = (long long)d[0] * d[1] * d[2];
+    float *dx = (float*)s->pw[0], *dy = (float*)s->pw[1];
+    CK(cudaMemcpyAsync(dx, x0, n * 4, cudaMemcpyHostToDevice, s->stream));
+    CK(unet::net_forward_level0(s->net, dx, dy, s->stream));
+    CK(cudaMemcpyAsync(y, dy, n * 4, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FIA_OK;
+}
+
+int fia_debug_unet_backward(fia_session* s, const float* x0, const float* gy, float* grads) {
+    if (!s || !s->net || !x0 || !gy || !grads) return FIA_ERR_INVALID;
+    int d[3];
+    unet::net_level_dims(s->net, 0, d);
+    const long long n = (long long)d[0] * d[1] * d[2];
+    float *dx = (float*)s->pw[0], *dg = (float*)s->pw[1];
+    CK(cudaMemcpyAsync(dx, x0, n * 4, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(dg, gy, n * 4, cudaMemcpyHostToDevice, s->stream));
+    CK(unet::net_zero_grad(s->net, s->stream));
+    CK(unet::net_forward_level0(s->net, dx, nullptr, s->stream));
+    CK(unet::net_backward_level0(s->net, dg, s->stream));
+    CK(unet::net_get_grads(s->net, grads, unet::num_parameters()));
+    CK(unet::net_zero_grad(s->net, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FIA_OK;
+}
+
+int fia_debug_precondition(fia_session* s, const float* r, float* z) {
+    if (!s || !s->net || !r || !z) return FIA_ERR_INVALID;
+    const long long nc = (long long)s->N[0] * s->N[1] * s->N[2];
+    float *dr = (float*)s->pw[0], *dz = (float*)s->pw[1];
+    CK(cudaMemcpyAsync(dr, r, nc * 4, cudaMemcpyHostToDevice, s->stream));
+    // r.r into the solver scalar the preconditioner reads
+    std::vector<float> h(r, r + nc);
+    double rr = 0.0;
+    for (long long i = 0; i < nc; ++i) rr += (double)h[i] * h[i];
+    CK(cudaMemcpyAsync(s->scal + kScalRR, &rr, sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    CK(unet::net_apply(s->net, poisson_grid(s), dr, dz, s->scal + kScalRR, (double)s->n_free, s->stream));
+    CK(cudaMemcpyAsync(z, dz, nc * 4, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FIA_OK;
 }
 
 }  // extern "C"

@@ -16,6 +16,17 @@
 
 namespace fia {
 
+// One 1D WENO6 evaluation as a real call.  Inlined, the face kernel held some sixty copies
+// of weno6_eval (the unrolled z-passes of a stencil), more code than the instruction cache
+// holds; ncu showed most warps waiting on instruction fetch.  Arguments travel in registers.
+__device__ __noinline__ float weno6_f(float f0, float f1, float f2, float f3, float f4, float f5, WenoCoef<float> w) {
+    const float f[6] = {f0, f1, f2, f3, f4, f5};
+    return weno6_eval(f, w);
+}
+__device__ __forceinline__ float weno6_call(const float* f, const WenoCoef<float>& w) {
+    return weno6_f(f[0], f[1], f[2], f[3], f[4], f[5], w);
+}
+
 // error-free sum of two floats (Knuth TwoSum)
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     s = a + b;
@@ -91,11 +102,11 @@ __device__ float weno6_3d_loc(const L& load, const NodeField& F, const int* anc,
             float f[6];
 #pragma unroll
             for (int iz = 0; iz < 6; ++iz) f[iz] = load(row + kk[iz]);
-            zv[iy] = weno6_eval(f, cz);
+            zv[iy] = weno6_call(f, cz);
         }
-        yv[ix] = weno6_eval(zv, cy);
+        yv[ix] = weno6_call(zv, cy);
     }
-    return weno6_eval(yv, cx);
+    return weno6_call(yv, cx);
 }
 
 // WENO6 at npts points that share x and z and lie within one cell in y (the density
@@ -136,7 +147,7 @@ __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, 
             float f[6];
 #pragma unroll
             for (int iz = 0; iz < 6; ++iz) f[iz] = load(row + kk[iz]);
-            zr[ix][r] = weno6_eval(f, cz);
+            zr[ix][r] = weno6_call(f, cz);
         }
     }
     for (int m = 0; m < npts; ++m) {
@@ -154,9 +165,9 @@ __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, 
             float f[6];
 #pragma unroll
             for (int i = 0; i < 6; ++i) f[i] = up ? zr[ix][i + 1] : zr[ix][i];
-            yv[ix] = weno6_eval(f, cy);
+            yv[ix] = weno6_call(f, cy);
         }
-        acc.add(weno6_eval(yv, cx) * ws[m]);
+        acc.add(weno6_call(yv, cx) * ws[m]);
     }
     return (seven ? 42 : 36) + 7 * npts;
 }
@@ -174,7 +185,7 @@ __device__ float weno6_1dy_loc(const L& load, const NodeField& F, const int* anc
         t[i] = sy + float(2 - i);
         f[i] = load(idx3(F, ix, clampi(by - 2 + i, F.My - 1), iz));
     }
-    return weno6_eval(f, weno_coef(t));
+    return weno6_call(f, weno_coef(t));
 }
 
 template <class L>

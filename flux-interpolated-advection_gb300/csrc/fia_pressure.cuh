@@ -14,6 +14,9 @@ struct PoissonGrid {
     const unsigned char* solid;
 };
 
+// index of r.r in PressureWork::scal (read by the learned preconditioner)
+constexpr int kScalRR = 3;
+
 template <typename T>
 struct PressureWork {
     T *p, *r, *z, *d, *d2, *q;  // N^3 each; p is the pressure

@@ -24,8 +24,8 @@ REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libfia_%s.so" % platform.machine())
-SOURCES = ["fia_api.cu", "fia_advect.cu", "fia_advect32.cu", "fia_pressure.cu", "fia_noalloc.cu"]
-HEADERS = ["fia_device.cuh", "fia_advect.cuh", "fia_local.cuh", "fia_pressure.cuh"]
+SOURCES = ["fia_api.cu", "fia_advect.cu", "fia_advect32.cu", "fia_pressure.cu", "fia_noalloc.cu", "fia_unet.cu"]
+HEADERS = ["fia_device.cuh", "fia_advect.cuh", "fia_local.cuh", "fia_pressure.cuh", "fia_unet.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 FIA_OK, FIA_ERR_INVALID, FIA_ERR_CUDA, FIA_ERR_UNSUPPORTED, FIA_ERR_NOMEM = 0, -1, -2, -3, -4
@@ -100,11 +100,13 @@ class AdvectParams(ctypes.Structure):
 
 
 class SolverParams(ctypes.Structure):
-    _fields_ = [("tol", ctypes.c_double), ("max_iter", ctypes.c_int), ("method", ctypes.c_int)]
+    _fields_ = [("tol", ctypes.c_double), ("max_iter", ctypes.c_int), ("method", ctypes.c_int),
+                ("fallback_iter", ctypes.c_int)]
 
 
 class SolverReport(ctypes.Structure):
-    _fields_ = [("iterations", ctypes.c_int), ("rel_residual", ctypes.c_double), ("status", ctypes.c_int)]
+    _fields_ = [("iterations", ctypes.c_int), ("rel_residual", ctypes.c_double), ("status", ctypes.c_int),
+                ("fcg_iterations", ctypes.c_int), ("precond_ms", ctypes.c_double)]
 
 
 class StepParams(ctypes.Structure):
@@ -112,14 +114,16 @@ class StepParams(ctypes.Structure):
     _fields_ = [("advect", AdvectParams), ("solver", SolverParams), ("cfl", ctypes.c_double),
                 ("max_dt", ctypes.c_double), ("buoyancy", ctypes.c_double), ("source", ctypes.c_int),
                 ("source_center", ctypes.c_double * 3), ("source_radius", ctypes.c_double),
-                ("source_density", ctypes.c_double), ("mass_correction", ctypes.c_int), ("frame", ctypes.c_int)]
+                ("source_density", ctypes.c_double), ("mass_correction", ctypes.c_int), ("frame", ctypes.c_int),
+                ("capture_pair", ctypes.c_int), ("capture_tol", ctypes.c_double)]
 
 
 class StepReport(ctypes.Structure):
     _fields_ = [("dt", ctypes.c_double), ("max_velocity", ctypes.c_double),
                 ("mass_before_advection", ctypes.c_double), ("mass_after_advection", ctypes.c_double),
                 ("mass_after", ctypes.c_double), ("solver_iterations", ctypes.c_int),
-                ("solver_rel_residual", ctypes.c_double), ("status", ctypes.c_int)]
+                ("solver_rel_residual", ctypes.c_double), ("status", ctypes.c_int),
+                ("solver_fcg_iterations", ctypes.c_int), ("precond_ms", ctypes.c_double)]
 
 
 def _declare(lib):
@@ -156,6 +160,23 @@ def _declare(lib):
     lib.fia_profile_faces.argtypes = [vp, ip]
     lib.fia_profile_faces_read.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_int)]
     lib.fia_step.argtypes = [vp, ctypes.POINTER(StepParams), ctypes.POINTER(StepReport)]
+    fp = ctypes.POINTER(ctypes.c_float)
+    lib.fia_set_solid_spheres.argtypes = [vp, ip, dp, dp]
+    lib.fia_get_solid_mask.argtypes = [vp, vp]
+    lib.fia_learned_num_parameters.restype = ctypes.c_longlong
+    lib.fia_learned_num_parameters.argtypes = []
+    lib.fia_learned_init.argtypes = [vp, ctypes.c_ulonglong]
+    lib.fia_learned_set_weights.argtypes = [vp, fp, ctypes.c_longlong]
+    lib.fia_learned_get_weights.argtypes = [vp, fp, ctypes.c_longlong]
+    lib.fia_learned_add_pair.argtypes = [vp, fp, fp]
+    lib.fia_learned_num_pairs.argtypes = [vp]
+    lib.fia_learned_loss.argtypes = [vp, ip, dp]
+    lib.fia_learned_calibrate.argtypes = [vp, ip]
+    lib.fia_learned_train_step.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ip, ctypes.c_double, dp]
+    lib.fia_learned_level_dims.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_int)]
+    lib.fia_debug_unet_forward.argtypes = [vp, fp, fp]
+    lib.fia_debug_unet_backward.argtypes = [vp, fp, fp, fp]
+    lib.fia_debug_precondition.argtypes = [vp, fp, fp]
 
 
 def _check(rc, what):
@@ -180,9 +201,13 @@ def advect_params(interpolation_method="WENO6", split_method="xz-CellFaceAligned
     return p
 
 
-def solver_params(tol=1e-6, max_iter=10000, method=0):
+FIA_SOLVER_PCG_JACOBI, FIA_SOLVER_FCG_LEARNED = 0, 1
+FIA_STATUS_SOLVER_CAP, FIA_STATUS_SOLVER_FALLBACK = 16, 32
+
+
+def solver_params(tol=1e-6, max_iter=10000, method=0, fallback_iter=200):
     p = SolverParams()
-    p.tol, p.max_iter, p.method = tol, max_iter, method
+    p.tol, p.max_iter, p.method, p.fallback_iter = tol, max_iter, method, fallback_iter
     return p
 
 
@@ -204,6 +229,14 @@ def step_params(**kw):
 
 def _dp(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _fp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def num_learned_parameters():
+    return int(load().fia_learned_num_parameters())
 
 
 class Grid3D:
@@ -320,6 +353,80 @@ class Grid3D:
         out = (ctypes.c_ulonglong * 5)()
         _check(self.lib.fia_pass_counters(self.s, out), "fia_pass_counters")
         return tuple(int(x) for x in out)
+
+    # ---- solids ----
+    def set_solid_spheres(self, centers, radii):
+        """Solid spheres (physical centres, radii); an empty list removes them."""
+        c = np.ascontiguousarray(centers, dtype=np.float64).reshape(-1)
+        r = np.ascontiguousarray(radii, dtype=np.float64).reshape(-1)
+        if c.size != 3 * r.size:
+            raise FiaError("set_solid_spheres: %d centre values for %d radii" % (c.size, r.size))
+        _check(self.lib.fia_set_solid_spheres(self.s, r.size, _dp(c), _dp(r)), "fia_set_solid_spheres")
+
+    def solid_mask(self):
+        m = np.empty(self.sizes()["density"], dtype=np.uint8)
+        _check(self.lib.fia_get_solid_mask(self.s, m.ctypes.data), "fia_get_solid_mask")
+        return m
+
+    # ---- learned preconditioner ----
+    def learned_init(self, seed=1):
+        _check(self.lib.fia_learned_init(self.s, seed), "fia_learned_init")
+
+    def learned_set_weights(self, w):
+        a = np.ascontiguousarray(w, dtype=np.float32)
+        _check(self.lib.fia_learned_set_weights(self.s, _fp(a), a.size), "fia_learned_set_weights")
+
+    def learned_get_weights(self):
+        a = np.empty(num_learned_parameters(), dtype=np.float32)
+        _check(self.lib.fia_learned_get_weights(self.s, _fp(a), a.size), "fia_learned_get_weights")
+        return a
+
+    def learned_add_pair(self, r, p):
+        a = np.ascontiguousarray(r, dtype=np.float32)
+        b = np.ascontiguousarray(p, dtype=np.float32)
+        _check(self.lib.fia_learned_add_pair(self.s, _fp(a), _fp(b)), "fia_learned_add_pair")
+
+    def learned_num_pairs(self):
+        return self.lib.fia_learned_num_pairs(self.s)
+
+    def learned_loss(self, pair):
+        out = ctypes.c_double(0)
+        _check(self.lib.fia_learned_loss(self.s, pair, ctypes.byref(out)), "fia_learned_loss")
+        return out.value
+
+    def learned_calibrate(self, pair=0):
+        _check(self.lib.fia_learned_calibrate(self.s, pair), "fia_learned_calibrate")
+
+    def learned_train_step(self, pairs, lr):
+        idx = (ctypes.c_int * len(pairs))(*[int(i) for i in pairs])
+        losses = np.zeros(len(pairs))
+        _check(self.lib.fia_learned_train_step(self.s, idx, len(pairs), ctypes.c_double(lr), _dp(losses)),
+               "fia_learned_train_step")
+        return losses
+
+    def learned_level_dims(self, level):
+        d = (ctypes.c_int * 3)()
+        _check(self.lib.fia_learned_level_dims(self.s, level, d), "fia_learned_level_dims")
+        return tuple(d)
+
+    def debug_unet_forward(self, x0):
+        a = np.ascontiguousarray(x0, dtype=np.float32).ravel()
+        y = np.empty_like(a)
+        _check(self.lib.fia_debug_unet_forward(self.s, _fp(a), _fp(y)), "fia_debug_unet_forward")
+        return y
+
+    def debug_unet_backward(self, x0, gy):
+        a = np.ascontiguousarray(x0, dtype=np.float32).ravel()
+        g = np.ascontiguousarray(gy, dtype=np.float32).ravel()
+        out = np.empty(num_learned_parameters(), dtype=np.float32)
+        _check(self.lib.fia_debug_unet_backward(self.s, _fp(a), _fp(g), _fp(out)), "fia_debug_unet_backward")
+        return out
+
+    def debug_precondition(self, r):
+        a = np.ascontiguousarray(r, dtype=np.float32).ravel()
+        z = np.empty_like(a)
+        _check(self.lib.fia_debug_precondition(self.s, _fp(a), _fp(z)), "fia_debug_precondition")
+        return z
 
     # ---- test hooks ----
     def debug_flux_pass(self, comp, field, dt, interp, psi_mode, use_integral, zero_velocity, color_off, k,

@@ -67,6 +67,8 @@ extern "C" {
 
 /* pressure solvers */
 #define FIA_SOLVER_PCG_JACOBI 0
+#define FIA_SOLVER_FCG_LEARNED 1   /* flexible CG around the learned two-level preconditioner (FP32C
+                                      sessions); Jacobi-PCG takes over after fallback_iter iterations */
 
 typedef struct fia_session fia_session;
 
@@ -87,12 +89,15 @@ typedef struct fia_solver_params {
     double tol;        /* relative residual |b - A p| / |b| */
     int max_iter;
     int method;        /* FIA_SOLVER_* */
+    int fallback_iter; /* FIA_SOLVER_FCG_LEARNED: FCG iterations before the Jacobi-PCG fallback */
 } fia_solver_params;
 
 typedef struct fia_solver_report {
-    int iterations;
+    int iterations;    /* all iterations (FCG + fallback PCG) */
     double rel_residual;
     int status;        /* FIA_STATUS_* bits of the solve */
+    int fcg_iterations;        /* of which flexible-CG iterations with the learned preconditioner */
+    double precond_ms;         /* device time in the preconditioner (0 unless profiled) */
 } fia_solver_report;
 
 /* One smoke step in the order of the reference's 3D loop (main.cpp:600-721): CFL time
@@ -113,6 +118,9 @@ typedef struct fia_step_params {
     double source_density;
     int mass_correction;          /* rescale density to its pre-advection mass (FP64 sums) */
     int frame;                    /* step index i_frame */
+    int capture_pair;             /* before the projection, solve it to capture_tol with Jacobi-PCG and
+                                     keep (rhs, pressure) as a training pair of the learned preconditioner */
+    double capture_tol;
 } fia_step_params;
 
 typedef struct fia_step_report {
@@ -124,6 +132,8 @@ typedef struct fia_step_report {
     int solver_iterations;
     double solver_rel_residual;
     int status;                   /* FIA_STATUS_* bits of the step */
+    int solver_fcg_iterations;    /* flexible-CG iterations of the learned solver */
+    double precond_ms;            /* device time in the learned preconditioner */
 } fia_step_report;
 
 /* Reference defaults for the flags (main.cpp:48-83) with WENO6, xz-CellFaceAligned, k = 3. */
@@ -205,6 +215,45 @@ int fia_move_substances_3D_noalloc(int nx, int ny, int nz, double cell_length, c
                                    double* density_out, const double* u, const double* v, const double* w,
                                    double time_step_length, const fia_advect_params* p, void* stream);
 const char* fia_noalloc_error_string(void);
+
+/* Solid spheres (no counterpart in the reference, whose 3D scenes have only the box walls):
+ * cells whose centre lies inside a sphere are solid.  The projection treats them like walls
+ * (zero-flux faces, the pressure unknowns removed; if the pinned last cell is solid the last
+ * fluid cell is pinned instead), faces touching a solid cell get zero velocity, and density
+ * is neither injected into nor kept in solid cells.  centers: 3*count doubles (physical
+ * coordinates, origin at the box corner); count 0 removes all solids. */
+int fia_set_solid_spheres(fia_session* s, int count, const double* centers, const double* radii);
+/* the solid mask (1 byte per cell, reference cell order) */
+int fia_get_solid_mask(fia_session* s, unsigned char* out);
+
+/* Learned pressure preconditioner (no counterpart in the reference, which uses amgcl):
+ * z = omega D^-1 r + P net(R r) with a 3D U-Net of 4 levels (16/32/48/64 channels,
+ * 3x3x3 convolutions, BF16 weights, FP32 accumulation) on the half-resolution grid, used by
+ * FIA_SOLVER_FCG_LEARNED.  The weights are one float array of fia_learned_num_parameters()
+ * values: each layer's [tap][in][out] block in layer order, then omega. */
+long long fia_learned_num_parameters(void);
+int fia_learned_init(fia_session* s, unsigned long long seed);
+int fia_learned_set_weights(fia_session* s, const float* w, long long count);
+int fia_learned_get_weights(fia_session* s, float* w, long long count);
+/* Training pairs B p = r (B = -A, r = -div(u) h) kept on the device, normalised to rms(r) = 1:
+ * from host arrays of nx*ny*nz floats, or captured by fia_step (capture_pair). */
+int fia_learned_add_pair(fia_session* s, const float* r, const float* p);
+int fia_learned_num_pairs(fia_session* s);
+/* Energy-norm loss (z - p)^T B (z - p) / p^T B p of the preconditioner on pair i. */
+int fia_learned_loss(fia_session* s, int pair, double* loss);
+/* Scales the output layer so that the preconditioner's output best fits pair i (least squares
+ * in the energy norm); used once after fia_learned_init. */
+int fia_learned_calibrate(fia_session* s, int pair);
+/* One Adam step on the mean gradient over pairs[0..batch); losses[i] receives each pair's loss. */
+int fia_learned_train_step(fia_session* s, const int* pairs, int batch, double lr, double* losses);
+/* Network dimensions: level 0 .. 3 grid sizes (dims3 out). */
+int fia_learned_level_dims(fia_session* s, int level, int* dims3);
+/* Test hooks: the network alone on a level-0 scalar input (host floats, level-0 size),
+ * its gradient with respect to all parameters for a given dL/dy (host floats), and the
+ * preconditioner applied to a fine-grid residual. */
+int fia_debug_unet_forward(fia_session* s, const float* x0, float* y);
+int fia_debug_unet_backward(fia_session* s, const float* x0, const float* gy, float* grads);
+int fia_debug_precondition(fia_session* s, const float* r, float* z);
 
 /* Test hooks: single pieces of the path on host data (FP64 buffers), mirroring the oracle. */
 /* one flux pass of a node field (comp -1 density, 0..2 velocity) with the session velocity */
