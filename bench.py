@@ -49,8 +49,9 @@ def read_peaks():
 
 
 def traffic_from_profile():
-    """dram bytes per face-kernel launch from the committed ncu summary, if present."""
-    path = os.path.join(ROOT, "profiles", "k_faces32_plume.md")
+    """dram bytes per k_quad32 launch at 256^3 from the committed ncu summary (measured on a
+    smaller plume and scaled by the pieces processed), if present."""
+    path = os.path.join(ROOT, "profiles", "k_quad32_plume.md")
     try:
         for line in open(path):
             if line.strip().startswith("traffic_bytes_per_launch_256:"):
@@ -213,9 +214,13 @@ def run_reference(args, world, rank, dist):
 def config_of(args, reference=False):
     return {"workload": "smoke plume %d^3 (sphere source r=0.1 at (0.5,0.15,0.5), buoyancy 1.0, closed box) "
                         "in a developed divergence-free flow (16 seeded Fourier modes) at CFL %g, flux advection of density and velocity (WENO6, k=3, zero-velocity "
-                        "correction), pressure Jacobi-PCG to %g relative residual" % (args.grid, args.cfl, args.tol),
+                        "correction), pressure solved to %g relative residual" % (args.grid, args.cfl, args.tol),
             "grid": args.grid, "cfl": args.cfl, "interpolation": "WENO6", "gauss_points": 3,
-            "pressure_tol": args.tol, "pressure_solver": "Jacobi-PCG (FP64 dot products)",
+            "pressure_tol": args.tol,
+            "pressure_solver": ("flexible CG with the learned two-level preconditioner (BF16 U-Net), Jacobi-PCG "
+                                "fallback after %d iterations" % args.fallback_iter
+                                if (args.solver == "learned" and args.precision == "fp32c" and not reference)
+                                else "Jacobi-PCG (FP64 dot products)"),
             "precision": "fp64 oracle" if reference else args.precision,
             "l2": "inputs larger than L2 (fields of %d^3, working set above 1 GB)" % args.grid,
             "parallelism": "replicas"}
@@ -224,6 +229,35 @@ def config_of(args, reference=False):
 # ------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------
+def fp64_plain_arm(args):
+    """The plain form (FP64 throughout, Jacobi-PCG) on the same initial plume: one untimed
+    step, then args.fp64_steps timed steps (device events)."""
+    import torch
+    import fia
+    n = args.grid
+    g = fia.Grid3D(n, n, n, 1.0 / n, precision=fia.FIA_FP64)
+    rho, u, v, w = plume_state(n, args.cfl)
+    for name, a in (("density", rho), ("u", u), ("v", v), ("w", w)):
+        g.set(name, a)
+    sp = fia.step_params(cfl=args.cfl, max_dt=MAX_DT, solver={"tol": args.tol, "max_iter": 20000})
+    sp.frame = 0
+    g.step(sp)
+    stream = torch.cuda.ExternalStream(g.stream())
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    reps = []
+    for i in range(args.fp64_steps):
+        sp.frame = 1 + i
+        reps.append(g.step(sp))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.fp64_steps
+    g.close()
+    return {"steps_per_s": 1e3 / ms, "ms_per_step": ms, "steps": args.fp64_steps,
+            "pressure_iterations": reps[-1].solver_iterations,
+            "pressure_rel_residual": reps[-1].solver_rel_residual}
+
 def run_gpu(args, world, rank, local, dist):
     import torch
     import fia
@@ -234,7 +268,13 @@ def run_gpu(args, world, rank, local, dist):
     rho, u, v, w = plume_state(n, args.cfl)
     for name, a in (("density", rho), ("u", u), ("v", v), ("w", w)):
         g.set(name, a)
-    sp = fia.step_params(cfl=args.cfl, max_dt=MAX_DT, solver={"tol": args.tol, "max_iter": 20000})
+    solver = {"tol": args.tol, "max_iter": 20000}
+    weights_used = None
+    if args.solver == "learned" and prec == fia.FIA_FP32C:
+        g.learned_set_weights(np.fromfile(args.weights, dtype="<f4"))
+        solver.update(method=fia.FIA_SOLVER_FCG_LEARNED, fallback_iter=args.fallback_iter)
+        weights_used = os.path.relpath(args.weights, ROOT)
+    sp = fia.step_params(cfl=args.cfl, max_dt=MAX_DT, solver=solver)
     stream = torch.cuda.ExternalStream(g.stream())
     frame = 0
     for _ in range(args.warmup):
@@ -301,7 +341,7 @@ def run_gpu(args, world, rank, local, dist):
                "d2h_bytes_per_step": nbytes, "steps": args.e2e_steps,
                "path": "fia_set_field x4 (pinned FP32 host) + fia_step + fia_get_field x4"}
 
-    # ---- roofline of the dominant kernel (k_faces32: clip + quadrature + WENO6)
+    # ---- roofline of the dominant kernel (k_quad32: per-piece quadrature + WENO6)
     evals = c1[3] - c0[3]
     flops = evals * WENO1D_FLOP
     faces = c1[0] - c0[0]
@@ -311,21 +351,23 @@ def run_gpu(args, world, rank, local, dist):
     achieved_tf = flops / (face_ms / 1e3) / 1e12 if face_ms > 0 else 0.0
     traffic = traffic_from_profile()
     peaks = read_peaks()
-    # algorithmic bytes of one face launch (one family of ~n^3 faces): density/velocity values
-    # (4 B per node), psi pairs (8 B), vertex displacements (12 B), two flux pairs written (16 B)
-    alg_bytes = 40.0 * n ** 3
+    # algorithmic bytes of one k_quad32 launch (one pass, all three face families): per piece
+    # its record (16 B) and face tag (4 B) read and its flux (4 B) written, plus the advected
+    # field (4 B per node) and psi (8 B per node) read once
+    launches = max(face_launches, 1)
+    alg_bytes = (24.0 * pieces + 12.0 * n ** 3 * launches) / launches
     roofline = {
         "bound": "fp32-simt",
-        "kernel": "k_faces32",
+        "kernel": "k_quad32",
         "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s", "frac": achieved_tf / peak_tf if peak_tf else None,
         "peak_source": "152 SMs x 128 FP32 lanes x 2 FLOP x median SM clock sampled in the run (%.0f MHz); "
                        "no FP32-SIMT figure in MEASURED_PEAKS.json" % sm_mhz,
         "algorithmic_flop": "1D WENO6 evaluations executed, counted on the device, x %d FLOP" % WENO1D_FLOP,
-        "launches": face_launches, "avg_launch_ms": face_ms / max(face_launches, 1),
-        "flop_per_launch": flops / max(face_launches, 1),
+        "launches": face_launches, "avg_launch_ms": face_ms / launches,
+        "flop_per_launch": flops / launches,
         "share_of_step": (face_ms / t_ms) if t_ms > 0 else None,
         "traffic": traffic,
-        "hbm": {"achieved": alg_bytes / (face_ms / max(face_launches, 1) / 1e3) / 1e9 if face_ms > 0 else None,
+        "hbm": {"achieved": alg_bytes / (face_ms / launches / 1e3) / 1e9 if face_ms > 0 else None,
                 "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                 "bytes_per_launch": alg_bytes},
     }
@@ -340,6 +382,7 @@ def run_gpu(args, world, rank, local, dist):
                          "(x n for the pressure)" % (det["sample_grid"], args.cfl, det["advection_s"],
                                                      det["pressure_s"], det["pressure_iters"], n)}
     last = reps[-1]
+    fp64 = fp64_plain_arm(args) if (rank == 0 and args.fp64_steps > 0 and prec == fia.FIA_FP32C) else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -352,7 +395,13 @@ def run_gpu(args, world, rank, local, dist):
                     "last_dt": last.dt, "last_max_velocity": last.max_velocity,
                     "last_pressure_iterations": last.solver_iterations,
                     "last_pressure_rel_residual": last.solver_rel_residual,
-                    "mass_after_correction": last.mass_after, "frames_run": frame},
+                    "mass_after_correction": last.mass_after, "frames_run": frame,
+                    "pressure_fcg_iterations": last.solver_fcg_iterations,
+                    "precond_ms_last_step": last.precond_ms,
+                    "pressure_status_bits": last.status & 48,
+                    "weights": weights_used,
+                    "fp64_plain": fp64,
+                    "speedup_vs_fp64_plain": (value / fp64["steps_per_s"]) if fp64 else None},
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -372,9 +421,19 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-sample-grid", type=int, default=24)
     ap.add_argument("--verbose", action="store_true", help="per-step reports of the warm-up on stderr")
+    ap.add_argument("--solver", default="learned", choices=["learned", "pcg"],
+                    help="pressure solver of the FP32 form: flexible CG with the learned preconditioner "
+                         "(Jacobi-PCG fallback) or Jacobi-PCG")
+    ap.add_argument("--weights", default=os.path.join(PKG, "weights", "unet_precond.f32"))
+    ap.add_argument("--fallback-iter", type=int, default=200)
+    ap.add_argument("--fp64-steps", type=int, default=1,
+                    help="steps of the plain FP64 form on the same state, timed after the main arm")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
+    if args.solver == "learned" and not os.path.exists(args.weights):
+        print("bench: no preconditioner weights at %s; using Jacobi-PCG" % args.weights, file=sys.stderr)
+        args.solver = "pcg"
     world, rank, local, dist = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank, dist)

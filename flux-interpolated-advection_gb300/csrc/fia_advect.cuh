@@ -36,6 +36,20 @@ enum StatusBits : unsigned {
     ST_SUBDIV_OVERFLOW = 8u,    // triangle subdivision stack exhausted
 };
 
+// Pieces of the FP32 face pipeline (clip -> per-piece quadrature -> per-face sum): the
+// clipped pieces of every face of a pass, contiguous per face, and per face its range.
+struct PieceStore {
+    float4* rec = nullptr;       // (cx, cy, cz, ny): centroid in cells relative to the face anchor, y-normal
+    int* face = nullptr;         // family << 29 | face index
+    float* flux = nullptr;       // flux of each piece
+    int2* range[3] = {nullptr, nullptr, nullptr};   // per face: start, nfwd | nrev << 15 | multi << 30
+    unsigned* count = nullptr;   // device counter of pieces
+    long long cap = 0;           // pieces the buffers hold
+};
+// (re)allocates the piece buffers for at least `pieces` pieces; ranges for `faces` per family
+cudaError_t piece_store_reserve(PieceStore& p, long long pieces, long long faces_per_family);
+void piece_store_free(PieceStore& p);
+
 // Workspace owned by the caller (device pointers).
 template <typename T>
 struct PassWork {
@@ -49,6 +63,7 @@ struct PassWork {
     cudaEvent_t* prof_ev;   // 2 * prof_cap events, or null
     int* prof_n;            // pairs recorded so far
     int prof_cap;
+    PieceStore* pieces = nullptr;   // FP32 form only
 };
 
 // records the opening / closing event of a timed face-kernel launch

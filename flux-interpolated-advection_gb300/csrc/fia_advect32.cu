@@ -18,6 +18,8 @@
 #include "fia_advect.cuh"
 #include "fia_local.cuh"
 
+#include <algorithm>
+
 namespace fia {
 
 namespace {
@@ -120,7 +122,20 @@ struct LocalFace {
     float x[4], y[4], z[4];   // vertex positions in cells relative to the anchor
 };
 
-struct FaceOut { Kahan F; Kahan Ny; int evals = 0; };   // evals: point interpolations made
+constexpr int kMaxPieces32 = 64;   // pieces of one face, both clips (CFL 4 needs about 36 per clip)
+
+// Pieces emitted by the clipper of one face: centroid (cells, relative to the face anchor)
+// and scaled y-normal, collected in order; the y-normals are summed here.
+struct PieceSink {
+    float4 p[kMaxPieces32];
+    int n = 0;
+    Kahan ny;
+    __device__ __forceinline__ void add(float cx, float cy, float cz, float nyv, unsigned& st) {
+        ny.add(nyv);
+        if (n >= kMaxPieces32) { st |= ST_CLIP_OVERFLOW; return; }
+        p[n++] = make_float4(cx, cy, cz, nyv);
+    }
+};
 
 __device__ __forceinline__ void centroidf(const float* px, const float* py, int num, float& cx, float& cy, float& area) {
     float a = 0.f, sx = 0.f, sy = 0.f;
@@ -139,9 +154,10 @@ __device__ __forceinline__ void centroidf(const float* px, const float* py, int 
     area = a;
 }
 
-__device__ void piece32(const PassDesc& d, const LocalFace& g, const float* px, const float* py, int num,
-                        float cxi, float ceta, const float* __restrict__ a, const float2* __restrict__ psi,
-                        const PsiLoad& pl, FaceOut& out) {
+// 3D centroid and scaled y-normal of a piece (split_face_3D.cpp:67-93), emitted to the sink
+// unless the normal vanishes.
+__device__ void piece_geom32(const LocalFace& g, const float* px, const float* py, int num, float cxi, float ceta,
+                             PieceSink& sink, unsigned& st) {
     const float cx = bilinf(g.x, cxi, ceta), cy = bilinf(g.y, cxi, ceta), cz = bilinf(g.z, cxi, ceta);
     float ny;
     if (num == 3) {
@@ -163,9 +179,16 @@ __device__ void piece32(const PassDesc& d, const LocalFace& g, const float* px, 
         ny = acc * 0.5f;
     }
     if (ny == 0.f) return;
-    out.Ny.add(ny);
+    sink.add(cx, cy, cz, ny, st);
+}
+
+// The quadrature of one piece (polygon_3D.cpp:257-487): density points on the y-interval
+// below the centroid and one psi point; returns the number of 1D WENO6 evaluations.
+__device__ int piece_quad32(const PassDesc& d, const int* anc, float cx, float cy, float cz, float ny,
+                            const float* __restrict__ a, const PsiLoad& pl, Kahan& F) {
     const PlainLoad al{a};
     const float invh = (float)(1.0 / d.h);   // psi carries a length; the face terms are per cell volume
+    int evals = 0;
     if (d.use_integral) {
         const float oy = (d.comp == 1) ? -0.5f : 0.f;
         const float r = snap_int(cy - oy);
@@ -196,35 +219,34 @@ __device__ void piece32(const PassDesc& d, const LocalFace& g, const float* px, 
         }
         bool shared = false;
         if (d.interp == INTERP_WENO6) {
-            const int n1d = weno6_ycolumn(al, d.A, g.anc, cx, cz, ys, ws, np, out.F);
+            const int n1d = weno6_ycolumn(al, d.A, anc, cx, cz, ys, ws, np, F);
             shared = n1d > 0;
-            out.evals += n1d;          // 1D WENO6 evaluations executed
+            evals += n1d;          // 1D WENO6 evaluations executed
         }
         if (!shared) {
             for (int m = 0; m < np; ++m) {
                 const float qq[3] = {cx, ys[m], cz};
-                out.F.add(interp_loc(d.interp, al, d.A, g.anc, qq) * ws[m]);
+                F.add(interp_loc(d.interp, al, d.A, anc, qq) * ws[m]);
             }
-            if (d.interp == INTERP_WENO6) out.evals += 43 * np;
+            if (d.interp == INTERP_WENO6) evals += 43 * np;
         }
         const float qp[3] = {cx, ylo, cz};
-        out.F.add(interp_loc(d.interp, pl, d.P, g.anc, qp) * (ny * invh));
-        if (d.interp == INTERP_WENO6) out.evals += 43;
+        F.add(interp_loc(d.interp, pl, d.P, anc, qp) * (ny * invh));
     } else {
         const float qp[3] = {cx, cy, cz};
-        out.F.add(interp_loc(d.interp, pl, d.P, g.anc, qp) * (ny * invh));
-        if (d.interp == INTERP_WENO6) out.evals += 43;
+        F.add(interp_loc(d.interp, pl, d.P, anc, qp) * (ny * invh));
     }
+    if (d.interp == INTERP_WENO6) evals += 43;
+    return evals;
 }
 
 __device__ void emit32(const PassDesc& d, const LocalFace& g, const float* px, const float* py, int num,
-                       const float* a, const float2* psi, const PsiLoad& pl, unsigned& st, int& npieces,
-                       FaceOut& out) {
+                       unsigned& st, int& npieces, PieceSink& sink) {
     float cx, cy, area;
     centroidf(px, py, num, cx, cy, area);
     const float minA = (float)d.minimal_area;
     if (!(area > minA)) {
-        if (area != 0.f) { ++npieces; piece32(d, g, px, py, num, cx, cy, a, psi, pl, out); }
+        if (area != 0.f) { ++npieces; piece_geom32(g, px, py, num, cx, cy, sink, st); }
         return;
     }
     float tri[24][6];
@@ -260,7 +282,7 @@ __device__ void emit32(const PassDesc& d, const LocalFace& g, const float* px, c
             tri[top][0] = tx[mi]; tri[top][1] = ty[mi]; tri[top][2] = mx; tri[top][3] = my; tri[top][4] = tx[i2]; tri[top][5] = ty[i2]; ++top;
         } else if (ta != 0.f) {
             ++npieces;
-            piece32(d, g, tx, ty, 3, tcx, tcy, a, psi, pl, out);
+            piece_geom32(g, tx, ty, 3, tcx, tcy, sink, st);
         }
     }
 }
@@ -268,8 +290,8 @@ __device__ void emit32(const PassDesc& d, const LocalFace& g, const float* px, c
 constexpr int kPool32 = 144, kMaxV32 = 32, kStack32 = 48;
 
 // The clipper of fia_advect.cu (facecutter.h:59-224) on local colours.
-__device__ void clip32(const PassDesc& d, const LocalFace& g, const float* a, const float2* psi, const PsiLoad& pl,
-                       unsigned& st, int& npieces, bool& multi, FaceOut& out) {
+__device__ void clip32(const PassDesc& d, const LocalFace& g, unsigned& st, int& npieces, bool& multi,
+                       PieceSink& sink) {
     CVf pool[kPool32];
     unsigned char sstart[kStack32], snum[kStack32], sdim[kStack32];
     const float xi[4] = {0.f, 1.f, 1.f, 0.f}, eta[4] = {0.f, 0.f, 1.f, 1.f};
@@ -349,7 +371,7 @@ __device__ void clip32(const PassDesc& d, const LocalFace& g, const float* a, co
             } else if (num >= 3) {
                 float px[kMaxV32], py[kMaxV32];
                 for (int q = 0; q < num; ++q) { px[q] = poly[q].p0; py[q] = poly[q].p1; }
-                emit32(d, g, px, py, num, a, psi, pl, st, npieces, out);
+                emit32(d, g, px, py, num, st, npieces, sink);
             }
         }
     }
@@ -373,19 +395,35 @@ __device__ __forceinline__ long long psi_node(const NodeField& P, int i, int j, 
     return idx3(P, clampi(i, P.Mx - 1), clampi(j, P.My - 1), clampi(k, P.Mz - 1));
 }
 
-__global__ void __launch_bounds__(128, 4) k_faces32(PassDesc d, int fam, const float* __restrict__ a,
-                                                 const float2* __restrict__ psi, const float* __restrict__ disp,
-                                                 float2* __restrict__ flux, float2* __restrict__ flux_rev,
-                                                 unsigned* status, unsigned long long* counters) {
+// Face pipeline of the chosen form, three kernels per pass:
+//  k_clip32     one thread per unique face: backtraced corners, clip (twice when an iso-line
+//               crosses a piece more than twice), pieces appended contiguously per face
+//               (warp prefix sum + one atomic per warp), y-normal sums;
+//  k_quad32     one thread per piece: quadrature + WENO6 (uniform work per thread, no clip
+//               code, so fewer registers and no divergence from the piece count);
+//  k_facesum32  one thread per face: compensated sum of its pieces in emission order.
+__device__ __forceinline__ void face_of(int fam, const NodeField& A, long long id, int& i, int& j, int& k) {
+    const int Fy = A.My + (fam == 1), Fz = A.Mz + (fam == 2);
+    k = (int)(id % Fz);
+    j = (int)((id / Fz) % Fy);
+    i = (int)(id / ((long long)Fz * Fy));
+}
+
+__global__ void __launch_bounds__(128) k_clip32(PassDesc d, int fam, const float* __restrict__ disp,
+                                                float2* __restrict__ flux, float2* __restrict__ flux_rev,
+                                                PieceStore ps, unsigned* status, unsigned long long* counters) {
     const int Fx = d.A.Mx + (fam == 0), Fy = d.A.My + (fam == 1), Fz = d.A.Mz + (fam == 2);
     const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long nface = (long long)Fx * Fy * Fz;
+    const int lane = threadIdx.x & 31;
     unsigned st = 0;
-    int npieces = 0, nmulti = 0, nevals = 0;
+    int npieces = 0, nmulti = 0;
+    PieceSink sink;
+    int nfwd = 0;
+    bool multi = false;
     if (id < nface) {
-        const int k = (int)(id % Fz);
-        const int j = (int)((id / Fz) % Fy);
-        const int i = (int)(id / ((long long)Fz * Fy));
+        int i, j, k;
+        face_of(fam, d.A, id, i, j, k);
         int ci[4], cj[4], ck[4];
         corners(fam, i, j, k, ci, cj, ck);
         LocalFace g;
@@ -402,44 +440,94 @@ __global__ void __launch_bounds__(128, 4) k_faces32(PassDesc d, int fam, const f
             g.y[q] = float(cj[q] - j) + sy + dy;
             g.z[q] = float(ck[q] - k) + sz + dz;
         }
-        const float2 b = __ldg(psi + psi_node(d.P, i, j, k));
-        const PsiLoad pl{psi, b.x, b.y};
-        FaceOut o;
-        bool multi = false;
-        clip32(d, g, a, psi, pl, st, npieces, multi, o);
-        const float F = o.F.value(), N = o.Ny.value();
-        float Fr = -F, Nr = -N;
+        clip32(d, g, st, npieces, multi, sink);
+        nfwd = sink.n;
+        const float N = sink.ny.value();
+        float Nr = -N;
         if (multi) {
+            // the upper cell's vertex order (v0, v3, v2, v1): its own pieces follow
             LocalFace r = g;
             r.x[1] = g.x[3]; r.y[1] = g.y[3]; r.z[1] = g.z[3];
             r.x[3] = g.x[1]; r.y[3] = g.y[1]; r.z[3] = g.z[1];
-            FaceOut o2;
             int np2 = 0; bool m2 = false;
-            clip32(d, r, a, psi, pl, st, np2, m2, o2);
-            Fr = o2.F.value(); Nr = o2.Ny.value();
+            sink.ny = Kahan();
+            clip32(d, r, st, np2, m2, sink);
+            Nr = sink.ny.value();
             ++nmulti;
-            nevals += o2.evals;
         }
-        nevals += o.evals;
-        if (!isfinite(F) || !isfinite(Fr)) st |= ST_NONFINITE;
-        flux[id] = make_float2(F, N);
-        flux_rev[id] = make_float2(Fr, Nr);
+        flux[id].y = N;
+        flux_rev[id].y = Nr;
     }
-    unsigned long long pc = (unsigned long long)npieces, ec = (unsigned long long)nevals;
+    // contiguous slots for this thread's pieces: warp prefix sum, one atomic per warp
+    const int cnt = sink.n;
+    int pre = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, pre, o);
+        if (lane >= o) pre += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, pre, 31);
+    unsigned base = 0;
+    if (lane == 31 && total > 0) base = atomicAdd(ps.count, (unsigned)total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    const long long start = (long long)base + pre - cnt;
+    if (id < nface) {
+        if (start + cnt <= ps.cap) {
+            const int tag = (fam << 29) | (int)id;
+            for (int q = 0; q < cnt; ++q) { ps.rec[start + q] = sink.p[q]; ps.face[start + q] = tag; }
+        }
+        // a range beyond the capacity is kept as it is: the host sees the count, grows the
+        // store and runs the pass again
+        ps.range[fam][id] = make_int2((int)start, nfwd | ((cnt - nfwd) << 15) | ((multi ? 1 : 0) << 30));
+    }
+    unsigned long long pc = (unsigned long long)npieces;
     unsigned fc = id < nface ? 1u : 0u, mc = (unsigned)nmulti;
     for (int o = 16; o > 0; o >>= 1) {
         pc += __shfl_down_sync(0xffffffffu, pc, o);
-        ec += __shfl_down_sync(0xffffffffu, ec, o);
         fc += __shfl_down_sync(0xffffffffu, fc, o);
         mc += __shfl_down_sync(0xffffffffu, mc, o);
         st |= __shfl_down_sync(0xffffffffu, st, o);
     }
-    if ((threadIdx.x & 31) == 0) {
+    if (lane == 0) {
         if (fc) { atomicAdd(&counters[0], (unsigned long long)fc); atomicAdd(&counters[1], pc); }
         if (mc) atomicAdd(&counters[2], (unsigned long long)mc);
-        if (ec) atomicAdd(&counters[3], ec);
         if (st) atomicOr(status, st);
     }
+}
+
+__global__ void __launch_bounds__(128) k_quad32(PassDesc d, const float* __restrict__ a, const float2* __restrict__ psi,
+                                                PieceStore ps, long long npc, unsigned long long* counters) {
+    unsigned long long ec = 0;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < npc; t += (long long)gridDim.x * blockDim.x) {
+        const float4 p = ps.rec[t];
+        const int tag = ps.face[t];
+        const int fam = tag >> 29;
+        int anc[3];
+        face_of(fam, d.A, tag & ((1 << 29) - 1), anc[0], anc[1], anc[2]);
+        const float2 b = __ldg(psi + psi_node(d.P, anc[0], anc[1], anc[2]));
+        const PsiLoad pl{psi, b.x, b.y};
+        Kahan F;
+        ec += (unsigned long long)piece_quad32(d, anc, p.x, p.y, p.z, p.w, a, pl, F);
+        ps.flux[t] = F.value();
+    }
+    for (int o = 16; o > 0; o >>= 1) ec += __shfl_down_sync(0xffffffffu, ec, o);
+    if ((threadIdx.x & 31) == 0 && ec) atomicAdd(&counters[3], ec);
+}
+
+__global__ void k_facesum32(PassDesc d, int fam, PieceStore ps, float2* __restrict__ flux, float2* __restrict__ flux_rev,
+                            unsigned* status) {
+    const long long nface = (long long)(d.A.Mx + (fam == 0)) * (d.A.My + (fam == 1)) * (d.A.Mz + (fam == 2));
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= nface) return;
+    const int2 r = ps.range[fam][id];
+    const int nf = r.y & 0x7fff, nr = (r.y >> 15) & 0x7fff;
+    const bool multi = (r.y >> 30) & 1;
+    Kahan F, Fr;
+    for (int q = 0; q < nf; ++q) F.add(ps.flux[(long long)r.x + q]);
+    for (int q = 0; q < nr; ++q) Fr.add(ps.flux[(long long)r.x + nf + q]);
+    const float f = F.value(), fr = multi ? Fr.value() : -f;
+    flux[id].x = f;
+    flux_rev[id].x = fr;
+    if (!isfinite(f) || !isfinite(fr)) atomicOr(status, (unsigned)ST_NONFINITE);
 }
 
 // rho'(c) = sum_f s_f [Ft + (Psi0(f) - Psi_c) Ny], compensated
@@ -494,19 +582,71 @@ cudaError_t run_pass<float>(const PassDesc& d, const VelocityFields& vel, const 
         k_backtrace32<<<nblk(nv, 128), 128, 0, s>>>(d, (const float*)vel.u, (const float*)vel.v, (const float*)vel.w,
                                                    vel.fu, vel.fv, vel.fw, w.verts);
     }
-    for (int fam = 0; fam < 3; ++fam) {
-        const long long n = (long long)(d.A.Mx + (fam == 0)) * (d.A.My + (fam == 1)) * (d.A.Mz + (fam == 2));
+    PieceStore& ps = *w.pieces;
+    long long nface[3];
+    for (int fam = 0; fam < 3; ++fam)
+        nface[fam] = (long long)(d.A.Mx + (fam == 0)) * (d.A.My + (fam == 1)) * (d.A.Mz + (fam == 2));
+    if (std::max(nface[0], std::max(nface[1], nface[2])) >= (1LL << 29)) return cudaErrorInvalidValue;
+    unsigned npc = 0;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        cudaMemsetAsync(ps.count, 0, sizeof(unsigned), s);
+        for (int fam = 0; fam < 3; ++fam)
+            k_clip32<<<nblk(nface[fam], 128), 128, 0, s>>>(d, fam, w.verts, (float2*)w.flux[fam],
+                                                           (float2*)w.flux_rev[fam], ps, w.status, w.counters);
+        cudaError_t e = cudaMemcpyAsync(&npc, ps.count, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return e;
+        if ((long long)npc <= ps.cap) break;
+        // more pieces than the store holds: grow it and clip again (counters of the first
+        // attempt stay counted)
+        e = piece_store_reserve(ps, (long long)npc + npc / 4 + 1024, std::max(nface[0], std::max(nface[1], nface[2])));
+        if (e != cudaSuccess) return e;
+    }
+    if ((long long)npc > ps.cap) return cudaErrorMemoryAllocation;
+    if (npc > 0) {
         prof_mark(w, 0, s);
-        k_faces32<<<nblk(n, 128), 128, 0, s>>>(d, fam, a, psi, w.verts, (float2*)w.flux[fam], (float2*)w.flux_rev[fam],
-                                               w.status, w.counters);
+        k_quad32<<<152 * 8, 128, 0, s>>>(d, a, psi, ps, (long long)npc, w.counters);
         prof_mark(w, 1, s);
     }
+    for (int fam = 0; fam < 3; ++fam)
+        k_facesum32<<<nblk(nface[fam], 256), 256, 0, s>>>(d, fam, ps, (float2*)w.flux[fam], (float2*)w.flux_rev[fam],
+                                                          w.status);
     const long long nc = (long long)d.A.Mx * d.A.My * d.A.Mz;
     k_gather32<<<nblk(nc, 256), 256, 0, s>>>(d, (const float2*)w.flux[0], (const float2*)w.flux[1],
                                              (const float2*)w.flux[2], (const float2*)w.flux_rev[0],
                                              (const float2*)w.flux_rev[1], (const float2*)w.flux_rev[2], psi, in, out,
                                              mode);
     return cudaGetLastError();
+}
+
+cudaError_t piece_store_reserve(PieceStore& p, long long pieces, long long faces_per_family) {
+    cudaDeviceSynchronize();
+    if (pieces > p.cap) {
+        cudaFree(p.rec); cudaFree(p.face); cudaFree(p.flux);
+        p.rec = nullptr; p.face = nullptr; p.flux = nullptr; p.cap = 0;
+        cudaError_t e = cudaMalloc(&p.rec, pieces * sizeof(float4));
+        if (e == cudaSuccess) e = cudaMalloc(&p.face, pieces * sizeof(int));
+        if (e == cudaSuccess) e = cudaMalloc(&p.flux, pieces * sizeof(float));
+        if (e != cudaSuccess) return e;
+        p.cap = pieces;
+    }
+    if (!p.count) {
+        cudaError_t e = cudaMalloc(&p.count, sizeof(unsigned));
+        if (e != cudaSuccess) return e;
+    }
+    if (!p.range[0]) {
+        for (int f = 0; f < 3; ++f) {
+            cudaError_t e = cudaMalloc(&p.range[f], faces_per_family * sizeof(int2));
+            if (e != cudaSuccess) return e;
+        }
+    }
+    return cudaSuccess;
+}
+
+void piece_store_free(PieceStore& p) {
+    cudaFree(p.rec); cudaFree(p.face); cudaFree(p.flux); cudaFree(p.count);
+    for (int f = 0; f < 3; ++f) cudaFree(p.range[f]);
+    p = PieceStore();
 }
 
 template <>

@@ -46,6 +46,12 @@ struct fia_session {
     // learned preconditioner (created by fia_learned_init / fia_learned_set_weights)
     unet::Net* net = nullptr;
     cudaEvent_t pev[2] = {nullptr, nullptr};
+    // clipped pieces of a pass (FP32 form)
+    PieceStore pieces;
+    // flexible-CG direction ring (allocated on first use)
+    FcgBuffers<float> fcg{};
+    bool fcg_ready = false;
+    double* p64 = nullptr;       // FP32 form: pressure accumulated in FP64 by the refinement
 };
 
 namespace {
@@ -192,6 +198,7 @@ PassWork<T> work(fia_session* s) {
     w.prof_ev = s->prof_ev.empty() ? nullptr : s->prof_ev.data();
     w.prof_n = &s->prof_n;
     w.prof_cap = (int)(s->prof_ev.size() / 2);
+    w.pieces = &s->pieces;
     return w;
 }
 
@@ -282,39 +289,57 @@ PoissonGrid poisson_grid(const fia_session* s) {
 }
 
 // Flexible CG with the learned preconditioner (FP32C sessions), Jacobi-PCG after
-// fallback_iter iterations without convergence.
-int pressure_fcg(fia_session* s, const fia_solver_params* sp, PressureReport& r, int& fcg_its, double& pms) {
+// fallback_iter iterations, or earlier when 20 iterations reduced the best |r| by less than 1%.
+// The right-hand side is -div(u) h of the session velocity, or rhs (device, B p = rhs).
+int pressure_fcg(fia_session* s, const fia_solver_params* sp, PressureReport& r, int& fcg_its, double& pms,
+                 const float* rhs = nullptr) {
     if (!s->net) return FIA_ERR_INVALID;
     using T = float;
     PressureWork<T> W = pressure_work<T>(s);
     const PoissonGrid g = poisson_grid(s);
     const T *u = (const T*)s->vel[0], *v = (const T*)s->vel[1], *w = (const T*)s->vel[2];
+    const long long nc = (long long)s->N[0] * s->N[1] * s->N[2];
     double br[2];
-    CK(pressure_rhs<T>(W, g, s->h, u, v, w, false, br, s->stream));
+    if (rhs) {
+        CK(cudaMemsetAsync(W.p, 0, nc * sizeof(T), s->stream));
+        CK(pressure_residual<T>(W, g, rhs, &br[1], s->stream));
+        br[0] = br[1];
+    } else {
+        CK(pressure_rhs<T>(W, g, s->h, u, v, w, false, br, s->stream));
+    }
     s->launches += 2;
-    r.iterations = 0; r.status = 0; r.rel_residual = 0.0; r.launches = 0;
+    r.iterations = 0; r.status = 0; r.rel_residual = 0.0; r.launches = 0; r.bb = br[0];
     fcg_its = 0; pms = 0.0;
     if (br[0] == 0.0) return FIA_OK;
     CK(fcg_begin<T>(W, br[0], br[1], sp->tol, s->stream));
     s->launches += 1;
     if (!s->pev[0]) { CK(cudaEventCreate(&s->pev[0])); CK(cudaEventCreate(&s->pev[1])); }
-    T* dold = W.d;
-    T* dnew = W.d2;
+    if (!s->fcg_ready) {
+        for (int j = 0; j <= kFcgMaxDirs; ++j) {
+            CK(cudaMalloc(&s->fcg.d[j], nc * sizeof(T)));
+            CK(cudaMalloc(&s->fcg.q[j], nc * sizeof(T)));
+        }
+        s->fcg_ready = true;
+    }
     const int cap = std::min(sp->fallback_iter, sp->max_iter);
     double st[3] = {br[1], br[1] <= sp->tol * sp->tol * br[0] ? 1.0 : 0.0, 0.0};
+    // stalled: the best |r| of the last 20 iterations is not 1% below the best before them
+    std::vector<double> best(1, br[1]);
     int it = 0;
-    while (it < cap && st[1] == 0.0) {
+    bool stalled = false;
+    while (it < cap && st[1] == 0.0 && !stalled) {
         CK(cudaEventRecord(s->pev[0], s->stream));
         CK(unet::net_apply(s->net, g, W.r, W.z, W.scal + kScalRR, (double)s->n_free, s->stream));
         CK(cudaEventRecord(s->pev[1], s->stream));
-        CK(fcg_iteration<T>(W, g, it == 0, dold, dnew, s->stream));
-        std::swap(dold, dnew);
+        CK(fcg_iteration<T>(W, g, s->fcg, it, kFcgMaxDirs, s->stream));
         s->launches += (unsigned long long)unet::net_launches(s->net) + 3;
         CK(solver_state(W.scal, st, s->stream));
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, s->pev[0], s->pev[1]));
         pms += ms;
         ++it;
+        best.push_back(std::min(best.back(), st[0]));
+        if (it >= 20 && best[it] > 0.9801 * best[it - 20]) stalled = true;
     }
     fcg_its = it;
     r.iterations = it;
@@ -322,7 +347,8 @@ int pressure_fcg(fia_session* s, const fia_solver_params* sp, PressureReport& r,
     if (st[1] != 0.0) return FIA_OK;
     // fallback: Jacobi-PCG from the current pressure
     double br2[2];
-    CK(pressure_rhs<T>(W, g, s->h, u, v, w, true, br2, s->stream));
+    if (rhs) CK(pressure_residual<T>(W, g, rhs, &br2[1], s->stream));
+    else CK(pressure_rhs<T>(W, g, s->h, u, v, w, true, br2, s->stream));
     PressureReport r2;
     CK(pressure_pcg<T>(W, g, br[0], br2[1], sp->tol, std::max(0, sp->max_iter - it), &r2, s->stream));
     s->launches += 2 + (unsigned long long)r2.launches;
@@ -330,6 +356,61 @@ int pressure_fcg(fia_session* s, const fia_solver_params* sp, PressureReport& r,
     r.rel_residual = r2.rel_residual;
     r.status = r2.status;
     return FIA_STATUS_SOLVER_FALLBACK;
+}
+
+// FP32 form: the FP32 solve is followed by FP64 residual refinement.  The true residual
+// -b - B p is formed in FP64 with the pressure accumulated in FP64; while it is above the
+// tolerance, B e = r is solved in FP32 from e = 0 (same solver) and p += e.  The reported
+// residual is this FP64 residual, so both precision forms stop at the same true residual.
+constexpr int kMaxRefinements = 4;
+
+int refine_fp32(fia_session* s, const fia_solver_params* sp, PressureReport& r, int& fcg_its, double& pms,
+                int& extra) {
+    using T = float;
+    PressureWork<T> W = pressure_work<T>(s);
+    const PoissonGrid g = poisson_grid(s);
+    const T *u = (const T*)s->vel[0], *v = (const T*)s->vel[1], *w = (const T*)s->vel[2];
+    const long long nc = (long long)s->N[0] * s->N[1] * s->N[2];
+    const double bb = r.bb;
+    if (!(bb > 0.0)) return FIA_OK;
+    if (!s->p64) CK(cudaMalloc(&s->p64, nc * sizeof(double)));
+    CK(widen(W.p, s->p64, nc, false, s->stream));
+    double rr = 0.0;
+    CK(true_residual(W, g, s->h, u, v, w, s->p64, &rr, s->stream));
+    s->launches += 3;
+    int used = r.iterations;
+    for (int k = 0; k < kMaxRefinements && rr > sp->tol * sp->tol * bb && used < sp->max_iter; ++k) {
+        fia_solver_params in = *sp;
+        in.tol = std::min(0.5, std::max(1e-5, 0.3 * sp->tol * std::sqrt(bb / rr)));
+        in.max_iter = sp->max_iter - used;
+        PressureReport r2;
+        if (sp->method == FIA_SOLVER_FCG_LEARNED) {
+            float* rhs = (float*)s->cbuf;
+            CK(cudaMemcpyAsync(rhs, W.r, nc * sizeof(T), cudaMemcpyDeviceToDevice, s->stream));
+            int its2 = 0;
+            double pms2 = 0.0;
+            in.fallback_iter = std::min(in.fallback_iter, in.max_iter);
+            const int rc = pressure_fcg(s, &in, r2, its2, pms2, rhs);
+            if (rc < 0) return rc;
+            extra |= rc;
+            fcg_its += its2;
+            pms += pms2;
+        } else {
+            CK(cudaMemsetAsync(W.p, 0, nc * sizeof(T), s->stream));
+            CK(pressure_pcg<T>(W, g, rr, rr, in.tol, in.max_iter, &r2, s->stream));
+            s->launches += (unsigned long long)r2.launches + 1;
+        }
+        used += r2.iterations;
+        CK(widen(W.p, s->p64, nc, true, s->stream));
+        CK(true_residual(W, g, s->h, u, v, w, s->p64, &rr, s->stream));
+        s->launches += 3;
+    }
+    CK(narrow(s->p64, W.p, nc, s->stream));
+    s->launches += 1;
+    r.iterations = used;
+    r.rel_residual = std::sqrt(rr / bb);
+    r.status = rr > sp->tol * sp->tol * bb ? 1 : 0;
+    return FIA_OK;
 }
 
 template <typename T>
@@ -356,9 +437,18 @@ int pressure(fia_session* s, const fia_solver_params* sp, fia_solver_report* rep
                              sp->max_iter, &r, s->stream));
         s->launches += (unsigned long long)r.launches;
     }
+    const bool refined = s->precision == FIA_FP32C && r.bb > 0.0;
+    if (refined) {
+        const int rc = refine_fp32(s, sp, r, fcg_its, pms, extra);
+        if (rc < 0) return rc;
+    }
     if (subtract) {
-        CK(subtract_gradient<T>((const T*)s->pres, (T*)s->vel[0], (T*)s->vel[1], (T*)s->vel[2], g, s->h, s->part,
-                                s->sums, s->stream));
+        if (refined)
+            CK(subtract_gradient_p64(s->p64, (float*)s->vel[0], (float*)s->vel[1], (float*)s->vel[2], g, s->h, s->part,
+                                     s->sums, s->stream));
+        else
+            CK(subtract_gradient<T>((const T*)s->pres, (T*)s->vel[0], (T*)s->vel[1], (T*)s->vel[2], g, s->h, s->part,
+                                    s->sums, s->stream));
         s->launches += 3;
         double loss[3];
         CK(cudaMemcpyAsync(loss, s->sums, 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
@@ -723,12 +813,17 @@ fia_session* fia_create(int nx, int ny, int nz, double cell_length, int precisio
     { void* t2; A(t2, 4 * sizeof(unsigned)); s->ticket = (unsigned*)t2; }
     void* t;
     A(t, pressure_partials() * sizeof(double)); s->part = (double*)t;
-    A(t, 8 * sizeof(double)); s->scal = (double*)t;
+    A(t, kScalDoubles * sizeof(double)); s->scal = (double*)t;
     A(t, 8 * sizeof(double)); s->sums = (double*)t;
     A(t, sizeof(unsigned)); s->status = (unsigned*)t;
     A(t, 4 * sizeof(unsigned long long)); s->counters = (unsigned long long*)t;
     A(t, kRedBlocks * sizeof(double)); s->red_part = (double*)t;
     A(t, 4 * sizeof(double)); s->red_out = (double*)t;
+    if (ok && precision == FIA_FP32C) {
+        // about 2.8 pieces per face at CFL 2, three face families per pass; grown on demand
+        // faces of one family of any (staggered) field fit in (nx+2)(ny+2)(nz+2)
+        ok = piece_store_reserve(s->pieces, 10 * big + 1024, big) == cudaSuccess;
+    }
     if (!ok) {
         g_last_error = "fia_create: device allocation failed";
         fia_destroy(s);
@@ -770,7 +865,11 @@ void fia_destroy(fia_session* s) {
     cudaStreamSynchronize(s->stream);
     for (cudaEvent_t e : s->prof_ev) cudaEventDestroy(e);
     for (cudaEvent_t e : s->pev) if (e) cudaEventDestroy(e);
+    if (s->fcg_ready)
+        for (int j = 0; j <= kFcgMaxDirs; ++j) { cudaFree(s->fcg.d[j]); cudaFree(s->fcg.q[j]); }
     unet::net_destroy(s->net);
+    piece_store_free(s->pieces);
+    if (s->p64) cudaFree(s->p64);
     if (s->solid) cudaFree(s->solid);
     for (void* p : s->allocations) cudaFree(p);
     cudaStreamDestroy(s->stream);
@@ -1135,6 +1234,61 @@ int fia_debug_unet_backward(fia_session* s, const float* x0, const float* gy, fl
     CK(unet::net_zero_grad(s->net, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return FIA_OK;
+}
+
+int fia_debug_learned_grad(fia_session* s, int pair, float* grads, double* loss) {
+    if (!s || !s->net || !grads || pair < 0 || pair >= unet::net_num_pairs(s->net)) return FIA_ERR_INVALID;
+    CK(unet::net_zero_grad(s->net, s->stream));
+    double l = 0.0;
+    CK(unet::net_loss(s->net, poisson_grid(s), pair, true, &l, s->stream));
+    CK(unet::net_get_grads(s->net, grads, unet::num_parameters()));
+    CK(unet::net_zero_grad(s->net, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    if (loss) *loss = l;
+    return FIA_OK;
+}
+
+int fia_debug_set_piece_capacity(fia_session* s, long long pieces) {
+    if (!s || s->precision != FIA_FP32C || pieces < 1) return FIA_ERR_INVALID;
+    CK(cudaStreamSynchronize(s->stream));
+    const long long big = (long long)(s->N[0] + 2) * (s->N[1] + 2) * (s->N[2] + 2);
+    piece_store_free(s->pieces);
+    CK(piece_store_reserve(s->pieces, pieces, big));
+    return FIA_OK;
+}
+
+long long fia_debug_piece_capacity(fia_session* s) { return s ? s->pieces.cap : -1; }
+
+int fia_debug_solve_rhs(fia_session* s, const float* rhs, float* x, const fia_solver_params* sp,
+                        fia_solver_report* rep) {
+    if (!s || !rhs || !x || !sp || s->precision != FIA_FP32C) return FIA_ERR_INVALID;
+    const long long nc = (long long)s->N[0] * s->N[1] * s->N[2];
+    float* drhs = (float*)s->cbuf;
+    CK(cudaMemcpyAsync(drhs, rhs, nc * 4, cudaMemcpyHostToDevice, s->stream));
+    PressureReport r;
+    int fcg_its = 0, extra = 0;
+    double pms = 0.0;
+    if (sp->method == FIA_SOLVER_FCG_LEARNED) {
+        if (!s->net) return FIA_ERR_INVALID;
+        const int rc = pressure_fcg(s, sp, r, fcg_its, pms, drhs);
+        if (rc < 0) return rc;
+        extra = rc;
+    } else {
+        PressureWork<float> W = pressure_work<float>(s);
+        const PoissonGrid g = poisson_grid(s);
+        double rr;
+        CK(cudaMemsetAsync(W.p, 0, nc * 4, s->stream));
+        CK(pressure_residual<float>(W, g, drhs, &rr, s->stream));
+        CK(pressure_pcg<float>(W, g, rr, rr, sp->tol, sp->max_iter, &r, s->stream));
+    }
+    CK(cudaMemcpyAsync(x, s->pres, nc * 4, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    const int status = (r.status ? FIA_STATUS_SOLVER_CAP : 0) | extra;
+    if (rep) {
+        rep->iterations = r.iterations; rep->rel_residual = r.rel_residual; rep->status = status;
+        rep->fcg_iterations = fcg_its; rep->precond_ms = pms;
+    }
+    return status;
 }
 
 int fia_debug_precondition(fia_session* s, const float* r, float* z) {

@@ -18,12 +18,16 @@
 
 namespace fia {
 
-constexpr int kRedBlocks = 152 * 4;
+constexpr int kRedBlocks = 152 * 6;
 constexpr int kRedThreads = 256;
 constexpr int kCgBatch = 16;
 
 // scal layout
-enum : int { S_ALPHA = 0, S_BETA = 1, S_RZ = 2, S_RR = 3, S_THRESH = 4, S_DONE = 5, S_ITERS = 6, S_DQ = 7 };
+enum : int {
+    S_ALPHA = 0, S_BETA = 1, S_RZ = 2, S_RR = 3, S_THRESH = 4, S_DONE = 5, S_ITERS = 6, S_DQ = 7,
+    S_BETAJ = 8,    // flexible CG: beta of direction slot j
+    S_DQJ = 16      // flexible CG: d.q of direction slot j
+};
 
 // ---------------------------------------------------------------------------------
 // per-thread dot accumulators
@@ -237,68 +241,223 @@ __global__ void __launch_bounds__(kRedThreads) k_pcg_init(PoissonGrid g, const T
     }
 }
 
-// d_new = z + beta d_old (d_new = z on the first iteration);  q = B d_new;  alpha = rz / (d_new.q)
-template <typename T>
+// ---------------------------------------------------------------------------------
+// per-iteration kernels, W consecutive cells of a z-line per thread and loop trip
+// (float4 / double2 loads when nz is a multiple of W; W = 1 otherwise)
+// ---------------------------------------------------------------------------------
+template <typename T, int W>
+__device__ __forceinline__ void ldv(const T* __restrict__ p, T (&v)[W]) {
+    if constexpr (W == 4) {
+        const float4 t = *reinterpret_cast<const float4*>(p);
+        v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+    } else if constexpr (W == 2) {
+        const double2 t = *reinterpret_cast<const double2*>(p);
+        v[0] = t.x; v[1] = t.y;
+    } else {
+        v[0] = p[0];
+    }
+}
+template <typename T, int W>
+__device__ __forceinline__ void stv(T* __restrict__ p, const T (&v)[W]) {
+    if constexpr (W == 4) *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    else if constexpr (W == 2) *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+    else p[0] = v[0];
+}
+
+// warp sum of a float-float accumulator; lane 0 holds the total
+__device__ __forceinline__ double warp_total(const DotAcc<float>& a) {
+    float hi = a.hi, lo = a.lo;
+    for (int o = 16; o > 0; o >>= 1) {
+        const float h2 = __shfl_down_sync(0xffffffffu, hi, o), l2 = __shfl_down_sync(0xffffffffu, lo, o);
+        const float s = __fadd_rn(hi, h2);
+        const float bb = __fsub_rn(s, hi);
+        const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(h2, bb));
+        hi = s;
+        lo = __fadd_rn(__fadd_rn(lo, l2), e);
+    }
+    return (double)hi + (double)lo;
+}
+__device__ __forceinline__ double warp_total(const DotAcc<double>& a) { return warp_sum(a.s); }
+
+// block sums of NV accumulators into part[b + nb*q] (FP64 conversions only per warp)
+template <typename T, int NV>
+__device__ __forceinline__ void block_dots(const DotAcc<T> (&acc)[NV], double* part) {
+    __shared__ double sh[NV][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        const double t = warp_total(acc[q]);
+        if (lane == 0) sh[q][wid] = t;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            double v = lane < nw ? sh[q][lane] : 0.0;
+            v = warp_sum(v);
+            if (lane == 0) part[blockIdx.x + gridDim.x * q] = v;
+        }
+    }
+}
+
+// diagonal of B at cell c0 + e of a group (walls and solid neighbours removed)
+template <int W>
+__device__ __forceinline__ int diag_at(const PoissonGrid& g, unsigned c0, const Cell& k, int e) {
+    const unsigned sx = (unsigned)g.ny * g.nz, sy = (unsigned)g.nz, c = c0 + e;
+    int d = 0;
+    auto nb = [&](bool ok, unsigned o) { if (ok && !(g.solid && g.solid[o])) ++d; };
+    nb(k.ix > 0, c - sx);
+    nb(k.ix < g.nx - 1, c + sx);
+    nb(k.iy > 0, c - sy);
+    nb(k.iy < g.ny - 1, c + sy);
+    nb(e > 0 || k.iz > 0, c - 1);
+    nb(e < W - 1 || k.iz + W < g.nz, c + 1);
+    return d;
+}
+
+// d_new = z + beta d_old (d_new = z on the first iteration);  q = B d_new;
+// alpha = rz / (d_new.q), or (d_new.r) / (d_new.q) when r is given (flexible CG: exact line
+// search along d whatever the preconditioner did)
+template <typename T, int W>
 __global__ void __launch_bounds__(kRedThreads) k_cg_direction_apply(PoissonGrid g, double* __restrict__ scal,
                                                                      const T* __restrict__ z, const T* __restrict__ dold,
                                                                      T* __restrict__ dnew, T* __restrict__ q, int first,
-                                                                     double* part, unsigned* ticket) {
+                                                                     const T* __restrict__ rres, double* part,
+                                                                     unsigned* ticket) {
     if (scal[S_DONE] != 0.0) return;
-    const unsigned n = (unsigned)g.nx * g.ny * g.nz;
+    const unsigned n = (unsigned)g.nx * g.ny * g.nz, ngr = n / W;
+    const unsigned sx = (unsigned)g.ny * g.nz, sy = (unsigned)g.nz;
     const T beta = (T)scal[S_BETA];
-    auto dval = [&](unsigned o) -> T { return first ? z[o] : z[o] + beta * dold[o]; };
-    DotAcc<T> dq;
-    for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
-        const T dc = dval(c);
-        T qc = T(0);
-        if (!excluded(g, c)) {
-            T s = T(0);
-            const int diag = for_neighbours(g, c, decode(c, g.ny, g.nz), [&](unsigned o) { s += dval(o); });
-            qc = T(diag) * dc - s;
+    auto dvec = [&](unsigned o0, T (&o)[W]) {
+        ldv<T, W>(z + o0, o);
+        if (!first) {
+            T b[W];
+            ldv<T, W>(dold + o0, b);
+#pragma unroll
+            for (int e = 0; e < W; ++e) o[e] += beta * b[e];
         }
-        dnew[c] = dc;
-        q[c] = qc;
-        dq.add(dc, qc);
+    };
+    auto d1 = [&](unsigned o) -> T { return first ? z[o] : z[o] + beta * dold[o]; };
+    DotAcc<T> acc[2];
+    for (unsigned gi = blockIdx.x * blockDim.x + threadIdx.x; gi < ngr; gi += gridDim.x * blockDim.x) {
+        const unsigned c0 = gi * W;
+        const Cell k = decode(c0, g.ny, g.nz);
+        T dc[W], s[W];
+        int dg[W];
+        dvec(c0, dc);
+#pragma unroll
+        for (int e = 0; e < W; ++e) { s[e] = T(0); dg[e] = 0; }
+        auto side = [&](bool ok, unsigned o0) {
+            if (!ok) return;
+            T nv[W];
+            dvec(o0, nv);
+#pragma unroll
+            for (int e = 0; e < W; ++e) {
+                const unsigned o = o0 + e;
+                if (g.solid && g.solid[o]) continue;
+                ++dg[e];
+                if ((int)o != g.pin) s[e] += nv[e];
+            }
+        };
+        side(k.ix > 0, c0 - sx);
+        side(k.ix < g.nx - 1, c0 + sx);
+        side(k.iy > 0, c0 - sy);
+        side(k.iy < g.ny - 1, c0 + sy);
+#pragma unroll
+        for (int e = 0; e < W; ++e) {
+            const unsigned c = c0 + e;
+            if (e > 0 || k.iz > 0) {
+                const unsigned o = c - 1;
+                if (!(g.solid && g.solid[o])) { ++dg[e]; if ((int)o != g.pin) s[e] += e > 0 ? dc[e - 1] : d1(o); }
+            }
+            if (e < W - 1 || k.iz + W < g.nz) {
+                const unsigned o = c + 1;
+                if (!(g.solid && g.solid[o])) { ++dg[e]; if ((int)o != g.pin) s[e] += e < W - 1 ? dc[e + 1] : d1(o); }
+            }
+        }
+        T qv[W];
+#pragma unroll
+        for (int e = 0; e < W; ++e) {
+            qv[e] = excluded(g, c0 + e) ? T(0) : T(dg[e]) * dc[e] - s[e];
+            acc[0].add(dc[e], qv[e]);
+        }
+        stv<T, W>(dnew + c0, dc);
+        stv<T, W>(q + c0, qv);
+        if (rres) {
+            T rv[W];
+            ldv<T, W>(rres + c0, rv);
+#pragma unroll
+            for (int e = 0; e < W; ++e) acc[1].add(dc[e], rv[e]);
+        }
     }
-    const double acc[1] = {dq.value()};
-    block_sums<1>(acc, part);
+    block_dots<T, 2>(acc, part);
     if (last_block(ticket)) {
         const double t = block_total(part, gridDim.x, 0);
+        const double tr = rres ? block_total(part, gridDim.x, 1) : 0.0;
         if (threadIdx.x == 0) {
-            scal[S_ALPHA] = t != 0.0 ? scal[S_RZ] / t : 0.0;
+            const double num = rres ? tr : scal[S_RZ];
+            scal[S_ALPHA] = t != 0.0 ? num / t : 0.0;
             scal[S_DQ] = t;
             *ticket = 0;
         }
     }
 }
 
-// x += alpha d; r -= alpha q; rr; with jacobi: z = r / diag, rz, beta = rz_new / rz_old.
+// r = rhs - B p on the free cells; partials |r|^2
 template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_residual(PoissonGrid g, const T* __restrict__ rhs,
+                                                           const T* __restrict__ p, T* __restrict__ r, double* part) {
+    const unsigned n = (unsigned)g.nx * g.ny * g.nz;
+    DotAcc<T> rr;
+    for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        T rc = T(0);
+        if (!excluded(g, c)) {
+            T s = T(0);
+            const int diag = for_neighbours(g, c, decode(c, g.ny, g.nz), [&](unsigned o) { s += p[o]; });
+            rc = rhs[c] - (T(diag) * p[c] - s);
+        }
+        r[c] = rc;
+        rr.add(rc, rc);
+    }
+    const double acc[1] = {rr.value()};
+    block_sums<1>(acc, part);
+}
+
+// x += alpha d; r -= alpha q; rr; with jacobi: z = r / diag, rz, beta = rz_new / rz_old.
+template <typename T, int W>
 __global__ void __launch_bounds__(kRedThreads) k_cg_update(PoissonGrid g, double* __restrict__ scal, T* __restrict__ x,
                                                             T* __restrict__ r, const T* __restrict__ d,
                                                             const T* __restrict__ q, T* __restrict__ z, int jacobi,
                                                             double* part, unsigned* ticket) {
     if (scal[S_DONE] != 0.0) return;
-    const unsigned n = (unsigned)g.nx * g.ny * g.nz;
+    const unsigned n = (unsigned)g.nx * g.ny * g.nz, ngr = n / W;
     const T a = (T)scal[S_ALPHA];
-    DotAcc<T> rz, rr;
-    for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
-        x[c] = x[c] + a * d[c];
-        const T rc = r[c] - a * q[c];
-        r[c] = rc;
-        rr.add(rc, rc);
+    DotAcc<T> acc[2];   // rz, rr
+    for (unsigned gi = blockIdx.x * blockDim.x + threadIdx.x; gi < ngr; gi += gridDim.x * blockDim.x) {
+        const unsigned c0 = gi * W;
+        T xv[W], dv[W], rv[W], qv[W];
+        ldv<T, W>(x + c0, xv); ldv<T, W>(d + c0, dv); ldv<T, W>(r + c0, rv); ldv<T, W>(q + c0, qv);
+#pragma unroll
+        for (int e = 0; e < W; ++e) {
+            xv[e] += a * dv[e];
+            rv[e] -= a * qv[e];
+            acc[1].add(rv[e], rv[e]);
+        }
+        stv<T, W>(x + c0, xv);
+        stv<T, W>(r + c0, rv);
         if (jacobi) {
-            T zc = T(0);
-            if (!excluded(g, c)) {
-                const int diag = for_neighbours(g, c, decode(c, g.ny, g.nz), [](unsigned) {});
-                zc = rc * inv_count<T>(diag);
+            const Cell k = decode(c0, g.ny, g.nz);
+            T zv[W];
+#pragma unroll
+            for (int e = 0; e < W; ++e) {
+                zv[e] = excluded(g, c0 + e) ? T(0) : rv[e] * inv_count<T>(diag_at<W>(g, c0, k, e));
+                acc[0].add(rv[e], zv[e]);
             }
-            z[c] = zc;
-            rz.add(rc, zc);
+            stv<T, W>(z + c0, zv);
         }
     }
-    const double acc[2] = {rz.value(), rr.value()};
-    block_sums<2>(acc, part);
+    block_dots<T, 2>(acc, part);
     if (last_block(ticket)) {
         const double trz = block_total(part, gridDim.x, 0);
         const double trr = block_total(part, gridDim.x, 1);
@@ -315,26 +474,136 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_update(PoissonGrid g, double
     }
 }
 
-// flexible CG: beta = -(z.q_old)/(d_old.q_old) (first: 0); rz = z.r
+// flexible CG with m kept directions (Notay's FCG(m)):
+//   beta_j = -(z.q_j)/(d_j.q_j) for the kept directions j;  d = z + sum_j beta_j d_j;
+//   q = B d;  alpha = (d.r)/(d.q)
 template <typename T>
-__global__ void __launch_bounds__(kRedThreads) k_fcg_dots(unsigned n, double* __restrict__ scal, const T* __restrict__ z,
-                                                           const T* __restrict__ qold, const T* __restrict__ r, int first,
-                                                           double* part, unsigned* ticket) {
+struct DirSet {
+    const T* v[kFcgMaxDirs];
+    int slot[kFcgMaxDirs];
+    int n;
+};
+
+template <typename T, int W>
+__global__ void __launch_bounds__(kRedThreads) k_fcgm_dots(unsigned n, double* __restrict__ scal, const T* __restrict__ z,
+                                                            const T* __restrict__ r, DirSet<T> qs, double* part,
+                                                            unsigned* ticket) {
     if (scal[S_DONE] != 0.0) return;
-    DotAcc<T> zq, zr;
-    for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
-        const T zc = z[c];
-        if (!first) zq.add(zc, qold[c]);
-        zr.add(zc, r[c]);
+    const unsigned ngr = n / W;
+    DotAcc<T> acc[kFcgMaxDirs + 1];   // z.q_j, then z.r
+    for (unsigned gi = blockIdx.x * blockDim.x + threadIdx.x; gi < ngr; gi += gridDim.x * blockDim.x) {
+        const unsigned c0 = gi * W;
+        T zv[W], v[W];
+        ldv<T, W>(z + c0, zv);
+        ldv<T, W>(r + c0, v);
+#pragma unroll
+        for (int e = 0; e < W; ++e) acc[kFcgMaxDirs].add(zv[e], v[e]);
+#pragma unroll
+        for (int j = 0; j < kFcgMaxDirs; ++j) {
+            if (j >= qs.n) break;
+            ldv<T, W>(qs.v[j] + c0, v);
+#pragma unroll
+            for (int e = 0; e < W; ++e) acc[j].add(zv[e], v[e]);
+        }
     }
-    const double acc[2] = {zq.value(), zr.value()};
-    block_sums<2>(acc, part);
+    block_dots<T, kFcgMaxDirs + 1>(acc, part);
     if (last_block(ticket)) {
-        const double tzq = block_total(part, gridDim.x, 0);
-        const double tzr = block_total(part, gridDim.x, 1);
+        double t[kFcgMaxDirs + 1];
+        for (int j = 0; j <= kFcgMaxDirs; ++j) t[j] = (j < qs.n || j == kFcgMaxDirs) ? block_total(part, gridDim.x, j) : 0.0;
         if (threadIdx.x == 0) {
-            scal[S_BETA] = (first || scal[S_DQ] == 0.0) ? 0.0 : -tzq / scal[S_DQ];
-            scal[S_RZ] = tzr;
+            for (int j = 0; j < qs.n; ++j) {
+                const double dq = scal[S_DQJ + qs.slot[j]];
+                scal[S_BETAJ + qs.slot[j]] = dq != 0.0 ? -t[j] / dq : 0.0;
+            }
+            scal[S_RZ] = t[kFcgMaxDirs];
+            *ticket = 0;
+        }
+    }
+}
+
+template <typename T, int W>
+__global__ void __launch_bounds__(kRedThreads) k_fcgm_direction(PoissonGrid g, double* __restrict__ scal,
+                                                                 const T* __restrict__ z, DirSet<T> ds,
+                                                                 T* __restrict__ dnew, T* __restrict__ qnew, int newslot,
+                                                                 const T* __restrict__ rres, double* part,
+                                                                 unsigned* ticket) {
+    if (scal[S_DONE] != 0.0) return;
+    const unsigned n = (unsigned)g.nx * g.ny * g.nz, ngr = n / W;
+    const unsigned sx = (unsigned)g.ny * g.nz, sy = (unsigned)g.nz;
+    T beta[kFcgMaxDirs];
+#pragma unroll
+    for (int j = 0; j < kFcgMaxDirs; ++j) beta[j] = j < ds.n ? (T)scal[S_BETAJ + ds.slot[j]] : T(0);
+    auto dvec = [&](unsigned o0, T (&o)[W]) {
+        ldv<T, W>(z + o0, o);
+#pragma unroll
+        for (int j = 0; j < kFcgMaxDirs; ++j) {
+            if (j >= ds.n) break;
+            T b[W];
+            ldv<T, W>(ds.v[j] + o0, b);
+#pragma unroll
+            for (int e = 0; e < W; ++e) o[e] += beta[j] * b[e];
+        }
+    };
+    auto d1 = [&](unsigned o) -> T {
+        T v = z[o];
+        for (int j = 0; j < ds.n; ++j) v += beta[j] * ds.v[j][o];
+        return v;
+    };
+    DotAcc<T> acc[2];
+    for (unsigned gi = blockIdx.x * blockDim.x + threadIdx.x; gi < ngr; gi += gridDim.x * blockDim.x) {
+        const unsigned c0 = gi * W;
+        const Cell k = decode(c0, g.ny, g.nz);
+        T dc[W], s[W];
+        int dg[W];
+        dvec(c0, dc);
+#pragma unroll
+        for (int e = 0; e < W; ++e) { s[e] = T(0); dg[e] = 0; }
+        auto side = [&](bool ok, unsigned o0) {
+            if (!ok) return;
+            T nv[W];
+            dvec(o0, nv);
+#pragma unroll
+            for (int e = 0; e < W; ++e) {
+                const unsigned o = o0 + e;
+                if (g.solid && g.solid[o]) continue;
+                ++dg[e];
+                if ((int)o != g.pin) s[e] += nv[e];
+            }
+        };
+        side(k.ix > 0, c0 - sx);
+        side(k.ix < g.nx - 1, c0 + sx);
+        side(k.iy > 0, c0 - sy);
+        side(k.iy < g.ny - 1, c0 + sy);
+#pragma unroll
+        for (int e = 0; e < W; ++e) {
+            const unsigned c = c0 + e;
+            if (e > 0 || k.iz > 0) {
+                const unsigned o = c - 1;
+                if (!(g.solid && g.solid[o])) { ++dg[e]; if ((int)o != g.pin) s[e] += e > 0 ? dc[e - 1] : d1(o); }
+            }
+            if (e < W - 1 || k.iz + W < g.nz) {
+                const unsigned o = c + 1;
+                if (!(g.solid && g.solid[o])) { ++dg[e]; if ((int)o != g.pin) s[e] += e < W - 1 ? dc[e + 1] : d1(o); }
+            }
+        }
+        T qv[W], rv[W];
+        ldv<T, W>(rres + c0, rv);
+#pragma unroll
+        for (int e = 0; e < W; ++e) {
+            qv[e] = excluded(g, c0 + e) ? T(0) : T(dg[e]) * dc[e] - s[e];
+            acc[0].add(dc[e], qv[e]);
+            acc[1].add(dc[e], rv[e]);
+        }
+        stv<T, W>(dnew + c0, dc);
+        stv<T, W>(qnew + c0, qv);
+    }
+    block_dots<T, 2>(acc, part);
+    if (last_block(ticket)) {
+        const double t = block_total(part, gridDim.x, 0);
+        const double tr = block_total(part, gridDim.x, 1);
+        if (threadIdx.x == 0) {
+            scal[S_ALPHA] = t != 0.0 ? tr / t : 0.0;
+            scal[S_DQJ + newslot] = t;
             *ticket = 0;
         }
     }
@@ -347,8 +616,8 @@ __global__ void k_fcg_begin(double* scal, double threshold, double rr0) {
 
 // u -= (p_i - p_{i-1}) / h on faces between two fluid cells (calc_pressure_3d.cpp:196-232);
 // faces touching a solid cell are set to the solid's (zero) velocity.
-template <typename T>
-__global__ void k_subtract_gradient(PoissonGrid g, T invh, const T* __restrict__ p, T* __restrict__ u,
+template <typename T, typename P>
+__global__ void k_subtract_gradient(PoissonGrid g, P invh, const P* __restrict__ p, T* __restrict__ u,
                                     T* __restrict__ v, T* __restrict__ w) {
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     const unsigned nu = (unsigned)(nx + 1) * ny * nz, nv = (unsigned)nx * (ny + 1) * nz;
@@ -374,7 +643,7 @@ __global__ void k_subtract_gradient(PoissonGrid g, T invh, const T* __restrict__
         }
         if (!interior) continue;
         if (g.solid && (g.solid[c] || g.solid[cm])) f[i] = T(0);
-        else f[i] = f[i] - (p[c] - p[cm]) * invh;
+        else f[i] = (T)((P)f[i] - (p[c] - p[cm]) * invh);
     }
 }
 
@@ -405,6 +674,34 @@ __global__ void k_wall_loss(int nx, int ny, int nz, double h, const T* __restric
 // ---------------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------------
+template <typename T> struct VecW;
+template <> struct VecW<float> { static constexpr int W = 4; };
+template <> struct VecW<double> { static constexpr int W = 2; };
+
+template <typename T>
+void launch_direction(const PressureWork<T>& W, const PoissonGrid& g, const T* dold, T* dnew, bool first, const T* rres,
+                      double* part, unsigned* ticket, cudaStream_t s) {
+    constexpr int V = VecW<T>::W;
+    if (g.nz % V == 0)
+        k_cg_direction_apply<T, V><<<kRedBlocks, kRedThreads, 0, s>>>(g, W.scal, W.z, dold, dnew, W.q, first ? 1 : 0,
+                                                                       rres, part, ticket);
+    else
+        k_cg_direction_apply<T, 1><<<kRedBlocks, kRedThreads, 0, s>>>(g, W.scal, W.z, dold, dnew, W.q, first ? 1 : 0,
+                                                                       rres, part, ticket);
+}
+
+template <typename T>
+void launch_update(const PressureWork<T>& W, const PoissonGrid& g, const T* d, bool jacobi, double* part,
+                   unsigned* ticket, cudaStream_t s, const T* q = nullptr) {
+    constexpr int V = VecW<T>::W;
+    if (!q) q = W.q;
+    if (g.nz % V == 0)
+        k_cg_update<T, V><<<kRedBlocks, kRedThreads, 0, s>>>(g, W.scal, W.p, W.r, d, q, W.z, jacobi ? 1 : 0, part,
+                                                              ticket);
+    else
+        k_cg_update<T, 1><<<kRedBlocks, kRedThreads, 0, s>>>(g, W.scal, W.p, W.r, d, q, W.z, jacobi ? 1 : 0, part,
+                                                              ticket);
+}
 template <typename T>
 cudaError_t pressure_rhs(const PressureWork<T>& W, const PoissonGrid& g, double h, const T* u, const T* v,
                          const T* w, bool warm, double* bb_rr_host, cudaStream_t s) {
@@ -429,9 +726,8 @@ cudaError_t pressure_pcg(const PressureWork<T>& W, const PoissonGrid& g, double 
     while (launched < max_iter && st[0] == 0.0) {
         const int batch = std::min(kCgBatch, max_iter - launched);
         for (int b = 0; b < batch; ++b) {
-            k_cg_direction_apply<T><<<nb, nt, 0, s>>>(g, W.scal, W.z, dold, dnew, W.q, launched + b == 0 ? 1 : 0,
-                                                      W.part, W.ticket);
-            k_cg_update<T><<<nb, nt, 0, s>>>(g, W.scal, W.p, W.r, dnew, W.q, W.z, 1, W.part + 2 * nb, W.ticket + 1);
+            launch_direction<T>(W, g, dold, dnew, launched + b == 0, nullptr, W.part, W.ticket, s);
+            launch_update<T>(W, g, dnew, true, W.part + 2 * nb, W.ticket + 1, s);
             std::swap(dold, dnew);
         }
         launched += batch;
@@ -454,13 +750,23 @@ cudaError_t pressure_solve(const PressureWork<T>& W, const PoissonGrid& g, doubl
     double br[2];
     cudaError_t e = pressure_rhs<T>(W, g, h, u, v, w, false, br, s);
     if (e != cudaSuccess) return e;
-    rep->iterations = 0; rep->rel_residual = 0.0; rep->status = 0; rep->launches = 2;
+    rep->iterations = 0; rep->rel_residual = 0.0; rep->status = 0; rep->launches = 2; rep->bb = br[0];
     if (br[0] == 0.0) return cudaGetLastError();
     PressureReport r2;
     e = pressure_pcg<T>(W, g, br[0], br[1], tol, max_iter, &r2, s);
     r2.launches += 2;
+    r2.bb = br[0];
     *rep = r2;
     return e;
+}
+
+template <typename T>
+cudaError_t pressure_residual(const PressureWork<T>& W, const PoissonGrid& g, const T* rhs, double* rr_host,
+                              cudaStream_t s) {
+    k_residual<T><<<kRedBlocks, kRedThreads, 0, s>>>(g, rhs, W.p, W.r, W.part);
+    k_finish<<<1, 256, 0, s>>>(W.part, kRedBlocks, 1, W.sums);
+    cudaMemcpyAsync(rr_host, W.sums, sizeof(double), cudaMemcpyDeviceToHost, s);
+    return cudaStreamSynchronize(s);
 }
 
 template <typename T>
@@ -470,14 +776,30 @@ cudaError_t fcg_begin(const PressureWork<T>& W, double bb, double rr0, double to
 }
 
 template <typename T>
-cudaError_t fcg_iteration(const PressureWork<T>& W, const PoissonGrid& g, bool first, T* dold, T* dnew,
+cudaError_t fcg_iteration(const PressureWork<T>& W, const PoissonGrid& g, const FcgBuffers<T>& B, int it, int m,
                           cudaStream_t s) {
     const unsigned n = (unsigned)g.nx * g.ny * g.nz;
     const int nb = kRedBlocks, nt = kRedThreads;
-    k_fcg_dots<T><<<nb, nt, 0, s>>>(n, W.scal, W.z, W.q, W.r, first ? 1 : 0, W.part, W.ticket);
-    k_cg_direction_apply<T><<<nb, nt, 0, s>>>(g, W.scal, W.z, dold, dnew, W.q, first ? 1 : 0, W.part + 2 * nb,
-                                              W.ticket + 1);
-    k_cg_update<T><<<nb, nt, 0, s>>>(g, W.scal, W.p, W.r, dnew, W.q, W.z, 0, W.part, W.ticket + 2);
+    m = std::max(1, std::min(m, kFcgMaxDirs));
+    const int ring = m + 1, newslot = it % ring;
+    DirSet<T> qs, ds;
+    qs.n = ds.n = std::min(it, m);
+    for (int j = 0; j < qs.n; ++j) {
+        const int sl = (it - 1 - j) % ring;
+        qs.v[j] = B.q[sl]; qs.slot[j] = sl;
+        ds.v[j] = B.d[sl]; ds.slot[j] = sl;
+    }
+    constexpr int V = VecW<T>::W;
+    if (g.nz % V == 0) {
+        k_fcgm_dots<T, V><<<nb, nt, 0, s>>>(n, W.scal, W.z, W.r, qs, W.part, W.ticket);
+        k_fcgm_direction<T, V><<<nb, nt, 0, s>>>(g, W.scal, W.z, ds, B.d[newslot], B.q[newslot], newslot, W.r,
+                                                 W.part + (kFcgMaxDirs + 1) * nb, W.ticket + 1);
+    } else {
+        k_fcgm_dots<T, 1><<<nb, nt, 0, s>>>(n, W.scal, W.z, W.r, qs, W.part, W.ticket);
+        k_fcgm_direction<T, 1><<<nb, nt, 0, s>>>(g, W.scal, W.z, ds, B.d[newslot], B.q[newslot], newslot, W.r,
+                                                 W.part + (kFcgMaxDirs + 1) * nb, W.ticket + 1);
+    }
+    launch_update<T>(W, g, B.d[newslot], false, W.part, W.ticket + 2, s, B.q[newslot]);
     return cudaGetLastError();
 }
 
@@ -492,13 +814,79 @@ cudaError_t solver_state(const double* scal, double out[3], cudaStream_t s) {
 template <typename T>
 cudaError_t subtract_gradient(const T* p, T* u, T* v, T* w, const PoissonGrid& g, double h, double* loss_part,
                               double* loss_sums, cudaStream_t s) {
-    k_subtract_gradient<T><<<kRedBlocks, kRedThreads, 0, s>>>(g, (T)(1.0 / h), p, u, v, w);
+    k_subtract_gradient<T, T><<<kRedBlocks, kRedThreads, 0, s>>>(g, (T)(1.0 / h), p, u, v, w);
     k_wall_loss<T><<<kRedBlocks, kRedThreads, 0, s>>>(g.nx, g.ny, g.nz, h, p, loss_part);
     k_finish<<<1, 256, 0, s>>>(loss_part, kRedBlocks, 3, loss_sums);
     return cudaGetLastError();
 }
 
-size_t pressure_partials() { return (size_t)kRedBlocks * 4; }
+// ---------------------------------------------------------------------------------
+// FP64 residual refinement of the FP32 form
+// ---------------------------------------------------------------------------------
+// r = -b - B p64 in FP64 arithmetic (b = div(u) h from the FP32 velocities), stored as FP32
+// for the next correction solve; partial |r|^2
+__global__ void __launch_bounds__(kRedThreads) k_true_residual(PoissonGrid g, double h, const float* __restrict__ u,
+                                                                const float* __restrict__ v, const float* __restrict__ w,
+                                                                const double* __restrict__ p, float* __restrict__ r,
+                                                                double* part) {
+    const unsigned n = (unsigned)g.nx * g.ny * g.nz;
+    const int ny = g.ny, nz = g.nz;
+    double acc = 0.0;
+    for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        double rc = 0.0;
+        if (!excluded(g, c)) {
+            const Cell k = decode(c, ny, nz);
+            const unsigned u0 = c, u1 = c + (unsigned)ny * nz;
+            const unsigned v0 = ((unsigned)k.ix * (ny + 1) + k.iy) * nz + k.iz, v1 = v0 + nz;
+            const unsigned w0 = ((unsigned)k.ix * ny + k.iy) * (nz + 1) + k.iz, w1 = w0 + 1;
+            const double b = (((double)u[u1] - (double)u[u0]) + ((double)v[v1] - (double)v[v0]) +
+                              ((double)w[w1] - (double)w[w0])) * h;
+            double s = 0.0;
+            const int diag = for_neighbours(g, c, k, [&](unsigned o) { s += p[o]; });
+            rc = -b - ((double)diag * p[c] - s);
+        }
+        r[c] = (float)rc;
+        acc += rc * rc;
+    }
+    const double a[1] = {acc};
+    block_sums<1>(a, part);
+}
+
+__global__ void k_to_double(const float* __restrict__ a, double* __restrict__ b, unsigned n, int accumulate) {
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        b[i] = accumulate ? b[i] + (double)a[i] : (double)a[i];
+}
+__global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, unsigned n) {
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = (float)a[i];
+}
+
+cudaError_t true_residual(const PressureWork<float>& W, const PoissonGrid& g, double h, const float* u,
+                          const float* v, const float* w, const double* p64, double* rr_host, cudaStream_t s) {
+    k_true_residual<<<kRedBlocks, kRedThreads, 0, s>>>(g, h, u, v, w, p64, W.r, W.part);
+    k_finish<<<1, 256, 0, s>>>(W.part, kRedBlocks, 1, W.sums);
+    cudaMemcpyAsync(rr_host, W.sums, sizeof(double), cudaMemcpyDeviceToHost, s);
+    return cudaStreamSynchronize(s);
+}
+
+cudaError_t widen(const float* a, double* b, long long n, bool accumulate, cudaStream_t s) {
+    k_to_double<<<kRedBlocks, kRedThreads, 0, s>>>(a, b, (unsigned)n, accumulate ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t narrow(const double* a, float* b, long long n, cudaStream_t s) {
+    k_to_float<<<kRedBlocks, kRedThreads, 0, s>>>(a, b, (unsigned)n);
+    return cudaGetLastError();
+}
+
+cudaError_t subtract_gradient_p64(const double* p64, float* u, float* v, float* w, const PoissonGrid& g, double h,
+                                  double* loss_part, double* loss_sums, cudaStream_t s) {
+    k_subtract_gradient<float, double><<<kRedBlocks, kRedThreads, 0, s>>>(g, 1.0 / h, p64, u, v, w);
+    k_wall_loss<double><<<kRedBlocks, kRedThreads, 0, s>>>(g.nx, g.ny, g.nz, h, p64, loss_part);
+    k_finish<<<1, 256, 0, s>>>(loss_part, kRedBlocks, 3, loss_sums);
+    return cudaGetLastError();
+}
+
+size_t pressure_partials() { return (size_t)kRedBlocks * 8; }
 
 #define FIA_PRESSURE_INST(T)                                                                                       \
     template cudaError_t pressure_rhs<T>(const PressureWork<T>&, const PoissonGrid&, double, const T*, const T*,    \
@@ -508,7 +896,10 @@ size_t pressure_partials() { return (size_t)kRedBlocks * 4; }
     template cudaError_t pressure_solve<T>(const PressureWork<T>&, const PoissonGrid&, double, const T*, const T*,  \
                                            const T*, double, int, PressureReport*, cudaStream_t);                   \
     template cudaError_t fcg_begin<T>(const PressureWork<T>&, double, double, double, cudaStream_t);               \
-    template cudaError_t fcg_iteration<T>(const PressureWork<T>&, const PoissonGrid&, bool, T*, T*, cudaStream_t);  \
+    template cudaError_t pressure_residual<T>(const PressureWork<T>&, const PoissonGrid&, const T*, double*,         \
+                                              cudaStream_t);                                                          \
+    template cudaError_t fcg_iteration<T>(const PressureWork<T>&, const PoissonGrid&, const FcgBuffers<T>&, int, int, \
+                                          cudaStream_t);                                                              \
     template cudaError_t subtract_gradient<T>(const T*, T*, T*, T*, const PoissonGrid&, double, double*, double*,   \
                                               cudaStream_t);
 FIA_PRESSURE_INST(double)

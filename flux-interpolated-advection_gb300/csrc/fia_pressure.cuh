@@ -16,12 +16,22 @@ struct PoissonGrid {
 
 // index of r.r in PressureWork::scal (read by the learned preconditioner)
 constexpr int kScalRR = 3;
+constexpr int kScalDoubles = 32;
+// directions kept by flexible CG (FCG(m), m <= kFcgMaxDirs)
+constexpr int kFcgMaxDirs = 4;
+
+// ring of m+1 direction vectors d and their images q = B d (N^3 each)
+template <typename T>
+struct FcgBuffers {
+    T* d[kFcgMaxDirs + 1];
+    T* q[kFcgMaxDirs + 1];
+};
 
 template <typename T>
 struct PressureWork {
     T *p, *r, *z, *d, *d2, *q;  // N^3 each; p is the pressure
     double* part;               // pressure_partials() doubles
-    double* scal;               // 8 doubles: alpha beta rz rr threshold done iterations dq
+    double* scal;               // kScalDoubles doubles (layout in fia_pressure.cu)
     double* sums;               // 4 doubles
     unsigned* ticket;           // 4 last-block counters (zero between kernels)
 };
@@ -31,6 +41,7 @@ struct PressureReport {
     double rel_residual;
     int status;               // 1: iteration cap reached before the tolerance
     int launches;             // kernels launched by the solve
+    double bb = 0.0;          // |b|^2 of the right-hand side
 };
 
 size_t pressure_partials();
@@ -46,6 +57,11 @@ template <typename T>
 cudaError_t pressure_pcg(const PressureWork<T>& W, const PoissonGrid& g, double bb, double rr0, double tol,
                          int max_iter, PressureReport* rep, cudaStream_t s);
 
+// r = rhs - B p; |r|^2 into rr_host (synchronises the stream).
+template <typename T>
+cudaError_t pressure_residual(const PressureWork<T>& W, const PoissonGrid& g, const T* rhs, double* rr_host,
+                              cudaStream_t s);
+
 // Solves A p = div(u) h for the reference operator to |r| <= tol |b| (Jacobi-PCG, cold start).
 template <typename T>
 cudaError_t pressure_solve(const PressureWork<T>& W, const PoissonGrid& g, double h, const T* u, const T* v,
@@ -57,15 +73,26 @@ template <typename T>
 cudaError_t subtract_gradient(const T* p, T* u, T* v, T* w, const PoissonGrid& g, double h, double* loss_part,
                               double* loss_sums, cudaStream_t s);
 
-// Flexible CG (FCG(1)) around a preconditioner that writes z = M(r) between iterations:
-//   dots:       beta = -(z.q_old)/(d_old.q_old) (0 on the first iteration), rz = z.r
-//   direction:  d = z + beta d_old, q = B d, alpha = rz / (d.q)
+// Flexible CG (FCG(m), the last m directions kept) around a preconditioner that writes
+// z = M(r) between iterations:
+//   dots:       beta_j = -(z.q_j)/(d_j.q_j) for the kept directions j
+//   direction:  d = z + sum_j beta_j d_j, q = B d, alpha = (d.r) / (d.q)   (ring slot it % (m+1))
 //   update:     p += alpha d, r -= alpha q, rr = r.r, done flag when rr <= tol^2 bb
 template <typename T>
 cudaError_t fcg_begin(const PressureWork<T>& W, double bb, double rr0, double tol, cudaStream_t s);
 template <typename T>
-cudaError_t fcg_iteration(const PressureWork<T>& W, const PoissonGrid& g, bool first, T* dold, T* dnew,
+cudaError_t fcg_iteration(const PressureWork<T>& W, const PoissonGrid& g, const FcgBuffers<T>& B, int it, int m,
                           cudaStream_t s);
+
+// FP64 residual refinement of the FP32 form: r = -b - B p64 computed in FP64 from the FP32
+// velocities (stored as FP32 in W.r), |r|^2 into rr_host (synchronises); conversions; the
+// gradient subtraction from the FP64 pressure.
+cudaError_t true_residual(const PressureWork<float>& W, const PoissonGrid& g, double h, const float* u,
+                          const float* v, const float* w, const double* p64, double* rr_host, cudaStream_t s);
+cudaError_t widen(const float* a, double* b, long long n, bool accumulate, cudaStream_t s);
+cudaError_t narrow(const double* a, float* b, long long n, cudaStream_t s);
+cudaError_t subtract_gradient_p64(const double* p64, float* u, float* v, float* w, const PoissonGrid& g, double h,
+                                  double* loss_part, double* loss_sums, cudaStream_t s);
 
 // out = {rr, done, iterations} (synchronises the stream)
 cudaError_t solver_state(const double* scal, double out[3], cudaStream_t s);

@@ -745,7 +745,8 @@ __global__ void k_ratio(const double* sums, double* out) { out[0] = sums[0] > 0.
 // ---------------------------------------------------------------------------------
 constexpr int kRedBlocks = 304;
 
-struct Pair { float* r; float* p; double denom; };
+// a training pair with the Poisson problem it belongs to (solid mask copy, pinned cell)
+struct Pair { float* r; float* p; unsigned char* solid; int pin; double denom; };
 
 struct Net {
     int fine[3];
@@ -1006,7 +1007,7 @@ void net_destroy(Net* n) {
     if (!n) return;
     cudaStreamSynchronize(n->stream);
     for (void* p : n->allocs) cudaFree(p);
-    for (auto& pr : n->pairs) { cudaFree(pr.r); cudaFree(pr.p); }
+    for (auto& pr : n->pairs) { cudaFree(pr.r); cudaFree(pr.p); if (pr.solid) cudaFree(pr.solid); }
     delete n;
 }
 
@@ -1087,14 +1088,21 @@ cudaError_t net_apply(Net* n, const PoissonGrid& g, const float* r, float* z, co
 int net_add_pair(Net* n, const PoissonGrid& g, const float* r_dev, const float* p_dev, cudaStream_t s) {
     const long long nf = (long long)g.nx * g.ny * g.nz;
     Pair pr;
+    pr.solid = nullptr;
+    pr.pin = g.pin;
     if (cudaMalloc(&pr.r, nf * 4) != cudaSuccess) return -1;
     if (cudaMalloc(&pr.p, nf * 4) != cudaSuccess) { cudaFree(pr.r); return -1; }
+    auto fail = [&]() { cudaFree(pr.r); cudaFree(pr.p); if (pr.solid) cudaFree(pr.solid); return -1; };
     cudaMemcpyAsync(pr.r, r_dev, nf * 4, cudaMemcpyDeviceToDevice, s);
     cudaMemcpyAsync(pr.p, p_dev, nf * 4, cudaMemcpyDeviceToDevice, s);
     long long nfree = nf - 1;
     if (g.solid) {
+        if (cudaMalloc(&pr.solid, nf) != cudaSuccess) return fail();
+        cudaMemcpyAsync(pr.solid, g.solid, nf, cudaMemcpyDeviceToDevice, s);
         std::vector<unsigned char> m(nf);
-        cudaMemcpy(m.data(), g.solid, nf, cudaMemcpyDeviceToHost);
+        if (cudaMemcpyAsync(m.data(), g.solid, nf, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return fail();
         nfree = 0;
         for (long long i = 0; i < nf; ++i) nfree += (m[i] == 0 && i != g.pin);
     }
@@ -1103,7 +1111,7 @@ int net_add_pair(Net* n, const PoissonGrid& g, const float* r_dev, const float* 
     k_scale2<<<grid_for(nf), 256, 0, s>>>(pr.r, pr.p, nf, n->sums, (double)nfree);
     double h[2];
     cudaMemcpyAsync(h, n->sums, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
-    if (cudaStreamSynchronize(s) != cudaSuccess || !(h[0] > 0.0)) { cudaFree(pr.r); cudaFree(pr.p); return -1; }
+    if (cudaStreamSynchronize(s) != cudaSuccess || !(h[0] > 0.0)) return fail();
     pr.denom = h[1] / h[0] * (double)nfree;   // p^T B p = p^T r after scaling both by sqrt(nfree/rr)
     n->pairs.push_back(pr);
     return (int)n->pairs.size() - 1;
@@ -1111,9 +1119,10 @@ int net_add_pair(Net* n, const PoissonGrid& g, const float* r_dev, const float* 
 
 int net_num_pairs(const Net* n) { return (int)n->pairs.size(); }
 
-cudaError_t net_loss(Net* n, const PoissonGrid& g, int pair, bool backward_pass, double* loss, cudaStream_t s) {
+cudaError_t net_loss(Net* n, const PoissonGrid& g0, int pair, bool backward_pass, double* loss, cudaStream_t s) {
     if (pair < 0 || pair >= (int)n->pairs.size()) return cudaErrorInvalidValue;
     const Pair& pr = n->pairs[pair];
+    const PoissonGrid g{g0.nx, g0.ny, g0.nz, pr.pin, pr.solid};
     const int* d0 = n->dims[0];
     const long long nf = (long long)g.nx * g.ny * g.nz;
     const float* omega = n->w + num_parameters() - 1;
@@ -1142,9 +1151,10 @@ cudaError_t net_loss(Net* n, const PoissonGrid& g, int pair, bool backward_pass,
     return cudaGetLastError();
 }
 
-cudaError_t net_calibrate(Net* n, const PoissonGrid& g, int pair, cudaStream_t s) {
+cudaError_t net_calibrate(Net* n, const PoissonGrid& g0, int pair, cudaStream_t s) {
     if (pair < 0 || pair >= (int)n->pairs.size()) return cudaErrorInvalidValue;
     const Pair& pr = n->pairs[pair];
+    const PoissonGrid g{g0.nx, g0.ny, g0.nz, pr.pin, pr.solid};
     const int* d0 = n->dims[0];
     const long long nf = (long long)g.nx * g.ny * g.nz;
     const float* omega = n->w + num_parameters() - 1;

@@ -177,6 +177,11 @@ def _declare(lib):
     lib.fia_debug_unet_forward.argtypes = [vp, fp, fp]
     lib.fia_debug_unet_backward.argtypes = [vp, fp, fp, fp]
     lib.fia_debug_precondition.argtypes = [vp, fp, fp]
+    lib.fia_debug_learned_grad.argtypes = [vp, ip, fp, dp]
+    lib.fia_debug_solve_rhs.argtypes = [vp, fp, fp, ctypes.POINTER(SolverParams), ctypes.POINTER(SolverReport)]
+    lib.fia_debug_set_piece_capacity.argtypes = [vp, ctypes.c_longlong]
+    lib.fia_debug_piece_capacity.argtypes = [vp]
+    lib.fia_debug_piece_capacity.restype = ctypes.c_longlong
 
 
 def _check(rc, what):
@@ -421,6 +426,27 @@ class Grid3D:
         out = np.empty(num_learned_parameters(), dtype=np.float32)
         _check(self.lib.fia_debug_unet_backward(self.s, _fp(a), _fp(g), _fp(out)), "fia_debug_unet_backward")
         return out
+
+    def debug_solve_rhs(self, rhs, sp):
+        """x with B x = rhs (B = -A), FP32 sessions; returns (x, SolverReport)"""
+        a = np.ascontiguousarray(rhs, dtype=np.float32).ravel()
+        x = np.empty_like(a)
+        rep = SolverReport()
+        _check(self.lib.fia_debug_solve_rhs(self.s, _fp(a), _fp(x), ctypes.byref(sp), ctypes.byref(rep)),
+               "fia_debug_solve_rhs")
+        return x, rep
+
+    def debug_set_piece_capacity(self, pieces):
+        _check(self.lib.fia_debug_set_piece_capacity(self.s, pieces), "fia_debug_set_piece_capacity")
+
+    def debug_piece_capacity(self):
+        return int(self.lib.fia_debug_piece_capacity(self.s))
+
+    def debug_learned_grad(self, pair):
+        out = np.empty(num_learned_parameters(), dtype=np.float32)
+        loss = ctypes.c_double(0)
+        _check(self.lib.fia_debug_learned_grad(self.s, pair, _fp(out), ctypes.byref(loss)), "fia_debug_learned_grad")
+        return out, loss.value
 
     def debug_precondition(self, r):
         a = np.ascontiguousarray(r, dtype=np.float32).ravel()

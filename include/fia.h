@@ -254,6 +254,15 @@ int fia_learned_level_dims(fia_session* s, int level, int* dims3);
 int fia_debug_unet_forward(fia_session* s, const float* x0, float* y);
 int fia_debug_unet_backward(fia_session* s, const float* x0, const float* gy, float* grads);
 int fia_debug_precondition(fia_session* s, const float* r, float* z);
+/* FP32 form: solve B x = rhs (B = -A of the session's Poisson problem; host arrays) with
+ * the solver of sp, x starting from 0. */
+int fia_debug_solve_rhs(fia_session* s, const float* rhs, float* x, const fia_solver_params* sp,
+                        fia_solver_report* rep);
+/* FP32 form: capacity of the clipped-piece store (it grows when a pass needs more) */
+int fia_debug_set_piece_capacity(fia_session* s, long long pieces);
+long long fia_debug_piece_capacity(fia_session* s);
+/* gradient of the energy-norm loss of pair i with respect to all parameters (no update) */
+int fia_debug_learned_grad(fia_session* s, int pair, float* grads, double* loss);
 
 /* Test hooks: single pieces of the path on host data (FP64 buffers), mirroring the oracle. */
 /* one flux pass of a node field (comp -1 density, 0..2 velocity) with the session velocity */

@@ -106,3 +106,20 @@ def test_fp32_plume_tracks_fp64():
         assert rel(a, b) < 1e-4
     for before, after in m32:
         assert abs(after - before) <= 1e-6 * before
+
+
+def test_fp32_piece_store_grows_and_is_deterministic():
+    g, h, u, v, w, rho, dt = make(16, fia.FIA_FP32C)
+    interp, psi_mode, integ, zv, co = PASSES["weno6_integral"]
+    ref, st0 = g.debug_flux_pass(-1, rho, dt, interp, psi_mode, integ, zv, co, 3)
+    again, _ = g.debug_flux_pass(-1, rho, dt, interp, psi_mode, integ, zv, co, 3)
+    g.debug_set_piece_capacity(100)
+    grown, st1 = g.debug_flux_pass(-1, rho, dt, interp, psi_mode, integ, zv, co, 3)
+    cap = g.debug_piece_capacity()
+    g.close()
+    assert st0 == 0 and st1 == 0
+    assert cap > 100
+    # the pieces of a face are summed in the order the clipper emits them, wherever the
+    # atomics place each face's block of pieces
+    assert np.array_equal(ref, again)
+    assert np.array_equal(ref, grown)

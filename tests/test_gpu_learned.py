@@ -10,7 +10,6 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import fia  # noqa: E402
-import scenes  # noqa: E402
 import unet_oracle as U  # noqa: E402
 
 pytestmark = pytest.mark.gpu
@@ -89,16 +88,18 @@ def test_precondition_matches_oracle():
 
 
 def pair(fine, pin, m, seed):
+    """a smooth pressure (white noise filtered at 3 cells) and its right-hand side: the BF16
+    network's gradient is well conditioned for it (for white-noise pressures the layer
+    gradients move by several percent with the FP32 summation order alone)"""
+    ndimage = pytest.importorskip("scipy.ndimage")
     rng = np.random.default_rng(seed)
-    p = scenes.gaussian_blobs(fine[0], seed=seed)[: np.prod(fine)].reshape(fine) if fine[0] == fine[1] == fine[2] \
-        else rng.normal(size=fine)
-    p = p + 0.1 * rng.normal(size=fine)
+    p = ndimage.gaussian_filter(rng.normal(size=fine), 3.0)
     p[U.excluded_mask(fine, pin, m)] = 0.0
     r = U.apply_B(p, fine, pin, m)
     return r, p
 
 
-def test_loss_and_adam_step_match_oracle():
+def test_loss_gradient_and_adam_step_match_oracle():
     g, m, pin, _ = solid_session()
     w0 = g.learned_get_weights().astype(np.float64)
     r, p = pair(FINE, pin, m, 5)
@@ -107,17 +108,24 @@ def test_loss_and_adam_step_match_oracle():
     rn, pn = U.normalise_pair(r, p, FINE, pin, m)
     lo, go = U.loss_and_grad(w0, rn, pn, FINE, pin, m, rounding=True)
     assert abs(loss - lo) < 2e-3 * lo
+    gp, l2 = g.debug_learned_grad(0)
+    assert abs(l2 - lo) < 2e-3 * lo
+    o = 0
+    for i, (lev, cin, cout, *_r) in enumerate(U.LAYERS):
+        n = 27 * cin * cout
+        assert rel(gp[o:o + n], go[o:o + n]) < 3e-2, "layer %d" % i
+        o += n
+    assert abs(gp[-1] - go[-1]) < 1e-2 * abs(go[-1])     # omega
     lr = 1e-4
     losses = g.learned_train_step([0], lr)
     assert abs(losses[0] - lo) < 2e-3 * lo
     w1 = g.learned_get_weights().astype(np.float64)
     g.close()
-    # first Adam step: w1 - w0 = -lr g / (|g| + eps) = -lr sign(g) where |g| >> eps
-    big = np.abs(go) > 1e-3 * np.abs(go).max()
+    # first Adam step: w1 - w0 = -lr g / (|g| + eps), i.e. -lr sign(g) of the GPU's own gradient
+    big = np.abs(gp) > 1e-2 * np.abs(gp).max()
     step = (w1 - w0)[big]
-    agree = np.mean(np.sign(step) == -np.sign(go[big]))
-    assert agree > 0.98
-    assert np.allclose(np.abs(step), lr, rtol=0.05, atol=0)
+    assert np.all(np.sign(step) == -np.sign(gp[big]))
+    assert np.allclose(np.abs(step), lr, rtol=0.02, atol=0)
 
 
 def random_velocity(n, seed):
