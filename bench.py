@@ -229,6 +229,34 @@ def config_of(args, reference=False):
 # ------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------
+def compare_projection(g, args):
+    """One projection of the current (advected, divergent) velocity by Jacobi-PCG and by the
+    learned FCG, each from p = 0 to the bench tolerance (FP64 residual), device-timed."""
+    import torch
+    import fia
+    u0 = {k: g.get(k) for k in ("u", "v", "w")}
+    g.advect_velocity_xyz_flux_advection_3D(MAX_DT)
+    u1 = {k: g.get(k) for k in ("u", "v", "w")}
+    out = {}
+    stream = torch.cuda.ExternalStream(g.stream())
+    for name, method in (("pcg", fia.FIA_SOLVER_PCG_JACOBI), ("learned_fcg", fia.FIA_SOLVER_FCG_LEARNED)):
+        for k, a in u1.items():
+            g.set(k, a)
+        sp = fia.solver_params(tol=args.tol, max_iter=20000, method=method, fallback_iter=args.fallback_iter)
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        rep = g.calc_pressure_3D(sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[name] = {"iterations": rep.iterations, "fcg_iterations": rep.fcg_iterations, "ms": e0.elapsed_time(e1),
+                     "rel_residual": rep.rel_residual, "status": rep.status, "precond_ms": rep.precond_ms}
+    for k, a in u0.items():
+        g.set(k, a)
+    out["time_ratio_pcg_over_learned"] = out["pcg"]["ms"] / out["learned_fcg"]["ms"]
+    return out
+
+
 def fp64_plain_arm(args):
     """The plain form (FP64 throughout, Jacobi-PCG) on the same initial plume: one untimed
     step, then args.fp64_steps timed steps (device events)."""
@@ -383,6 +411,7 @@ def run_gpu(args, world, rank, local, dist):
                                                      det["pressure_s"], det["pressure_iters"], n)}
     last = reps[-1]
     fp64 = fp64_plain_arm(args) if (rank == 0 and args.fp64_steps > 0 and prec == fia.FIA_FP32C) else None
+    solvers = compare_projection(g, args) if (rank == 0 and weights_used) else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -401,6 +430,7 @@ def run_gpu(args, world, rank, local, dist):
                     "pressure_status_bits": last.status & 48,
                     "weights": weights_used,
                     "fp64_plain": fp64,
+                    "projection_pcg_vs_learned": solvers,
                     "speedup_vs_fp64_plain": (value / fp64["steps_per_s"]) if fp64 else None},
     }
     if rank == 0:

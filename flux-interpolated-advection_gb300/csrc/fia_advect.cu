@@ -80,6 +80,24 @@ NodeField psi_field(const NodeField& A) {
     return P;
 }
 
+NodeField field32(NodeField F) {
+    F.oxf = (float)F.ox; F.oyf = (float)F.oy; F.ozf = (float)F.oz;
+    return F;
+}
+
+PassDesc desc32(const PassDesc& d) {
+    PassDesc e = d;
+    e.A = field32(d.A);
+    e.P = field32(d.P);
+    for (int q = 0; q < kMaxGauss; ++q) { e.gxf[q] = (float)d.gx[q]; e.gwf[q] = (float)d.gw[q]; }
+    e.hf = (float)d.h;
+    e.invhf = (float)(1.0 / d.h);
+    e.dthf = (float)(d.dt / d.h);
+    e.color_off_f[0] = (float)d.color_off[0]; e.color_off_f[1] = (float)d.color_off[1];
+    e.minimal_area_f = (float)d.minimal_area;
+    return e;
+}
+
 // ------------------------------------------------------------------------------------
 // psi: one thread per column (i,k); psi(.,0,.) = 0, psi(.,j,.) = psi(.,j-1,.) + incr(j-1)
 // ------------------------------------------------------------------------------------

@@ -24,7 +24,16 @@ struct PassDesc {
     double gw[kMaxGauss];   // weights normalised to sum 1
     double minimal_area;    // xi-eta area above which pieces are triangulated
     double dt, h;
+    // FP32 copies for the FP32 kernels, filled on the host by desc32(): on GB300 every
+    // double-to-float conversion in a kernel runs on the (slow) FP64 pipe
+    float gxf[kMaxGauss], gwf[kMaxGauss];
+    float hf, invhf, dthf;  // h, 1/h, dt/h
+    float color_off_f[2], minimal_area_f;
 };
+
+// PassDesc / NodeField with their FP32 copies filled (host)
+NodeField field32(NodeField F);
+PassDesc desc32(const PassDesc& d);
 
 enum PsiMode : int { PSI_PLAIN = 0, PSI_WENO6 = 1, PSI_LINEAR = 2 };
 

@@ -33,10 +33,10 @@ __global__ void k_psi32(PassDesc d, const float* __restrict__ a, float2* __restr
     if (col >= (long long)Mx * Mz) return;
     const int i = (int)(col / Mz), k = (int)(col % Mz);
     const PlainLoad L{a};
-    const float hf = (float)d.h;
+    const float hf = d.hf;
     float hi = 0.f, lo = 0.f;
     psi[idx3(d.P, i, 0, k)] = make_float2(0.f, 0.f);
-    const float oy = (float)d.A.oy;
+    const float oy = d.A.oyf;
     for (int j = 1; j <= My; ++j) {
         Kahan inc;
         if (d.psi_mode == PSI_PLAIN) {
@@ -47,14 +47,14 @@ __global__ void k_psi32(PassDesc d, const float* __restrict__ a, float2* __restr
             for (int half = 0; half < 2; ++half) {
                 const float lo_y = (oy - 0.5f) + 0.5f * float(half);
                 for (int q = 0; q < d.k; ++q) {
-                    const float qq[3] = {(float)d.A.ox, lo_y + 0.25f * (1.0f + (float)d.gx[q]), (float)d.A.oz};
-                    inc.add(weno6_1dy_loc(L, d.A, anc, qq) * (0.5f * hf) * (float)d.gw[q]);
+                    const float qq[3] = {d.A.oxf, lo_y + 0.25f * (1.0f + d.gxf[q]), d.A.ozf};
+                    inc.add(weno6_1dy_loc(L, d.A, anc, qq) * (0.5f * hf) * d.gwf[q]);
                 }
             }
         } else {
             const int anc[3] = {i, j - 1, k};
-            const float q0[3] = {(float)d.A.ox, 0.25f + oy - 0.5f, (float)d.A.oz};
-            const float q1[3] = {(float)d.A.ox, 0.75f + oy - 0.5f, (float)d.A.oz};
+            const float q0[3] = {d.A.oxf, 0.25f + oy - 0.5f, d.A.ozf};
+            const float q1[3] = {d.A.oxf, 0.75f + oy - 0.5f, d.A.ozf};
             inc.add(lin3d_loc(L, d.A, anc, q0) * (0.5f * hf));
             inc.add(lin3d_loc(L, d.A, anc, q1) * (0.5f * hf));
         }
@@ -90,7 +90,7 @@ __global__ void k_backtrace32(PassDesc d, const float* __restrict__ u, const flo
     }
     if (!pinned) {
         // dt/h converts the velocity to cells per step
-        const float s = (float)(d.dt / d.h);
+        const float s = d.dthf;
         dx[0] = -interp_loc(d.interp, PlainLoad{u}, fu, anc, q) * s;
         dx[1] = -interp_loc(d.interp, PlainLoad{v}, fv, anc, q) * s;
         dx[2] = -interp_loc(d.interp, PlainLoad{w}, fw, anc, q) * s;
@@ -187,7 +187,7 @@ __device__ void piece_geom32(const LocalFace& g, const float* px, const float* p
 __device__ int piece_quad32(const PassDesc& d, const int* anc, float cx, float cy, float cz, float ny,
                             const float* __restrict__ a, const PsiLoad& pl, Kahan& F) {
     const PlainLoad al{a};
-    const float invh = (float)(1.0 / d.h);   // psi carries a length; the face terms are per cell volume
+    const float invh = d.invhf;   // psi carries a length; the face terms are per cell volume
     int evals = 0;
     if (d.use_integral) {
         const float oy = (d.comp == 1) ? -0.5f : 0.f;
@@ -202,19 +202,19 @@ __device__ int piece_quad32(const PassDesc& d, const int* anc, float cx, float c
         if (f < 0.5f) {
             const float L = cy - ylo;
             for (int q = 0; q < d.k; ++q) {
-                ys[np] = (L * 0.5f) * (float)d.gx[q] + (L * 0.5f) + ylo;
-                ws[np++] = ny * f * (float)d.gw[q];
+                ys[np] = (L * 0.5f) * d.gxf[q] + (L * 0.5f) + ylo;
+                ws[np++] = ny * f * d.gwf[q];
             }
         } else {
             float lo = ylo, L = 0.5f;
             for (int q = 0; q < d.k; ++q) {
-                ys[np] = (L * 0.5f) * (float)d.gx[q] + (L * 0.5f) + lo;
-                ws[np++] = ny * 0.5f * (float)d.gw[q];
+                ys[np] = (L * 0.5f) * d.gxf[q] + (L * 0.5f) + lo;
+                ws[np++] = ny * 0.5f * d.gwf[q];
             }
             lo = ylo + 0.5f; L = cy - lo;
             for (int q = 0; q < d.k; ++q) {
-                ys[np] = (L * 0.5f) * (float)d.gx[q] + (L * 0.5f) + lo;
-                ws[np++] = ny * (f - 0.5f) * (float)d.gw[q];
+                ys[np] = (L * 0.5f) * d.gxf[q] + (L * 0.5f) + lo;
+                ws[np++] = ny * (f - 0.5f) * d.gwf[q];
             }
         }
         bool shared = false;
@@ -244,7 +244,7 @@ __device__ void emit32(const PassDesc& d, const LocalFace& g, const float* px, c
                        unsigned& st, int& npieces, PieceSink& sink) {
     float cx, cy, area;
     centroidf(px, py, num, cx, cy, area);
-    const float minA = (float)d.minimal_area;
+    const float minA = d.minimal_area_f;
     if (!(area > minA)) {
         if (area != 0.f) { ++npieces; piece_geom32(g, px, py, num, cx, cy, sink, st); }
         return;
@@ -297,8 +297,8 @@ __device__ void clip32(const PassDesc& d, const LocalFace& g, unsigned& st, int&
     const float xi[4] = {0.f, 1.f, 1.f, 0.f}, eta[4] = {0.f, 0.f, 1.f, 1.f};
     for (int q = 0; q < 4; ++q) {
         pool[q].p0 = xi[q]; pool[q].p1 = eta[q];
-        pool[q].c0 = snap_int(g.x[q] - (float)d.color_off[0]);
-        pool[q].c1 = snap_int(g.z[q] - (float)d.color_off[1]);
+        pool[q].c0 = snap_int(g.x[q] - d.color_off_f[0]);
+        pool[q].c1 = snap_int(g.z[q] - d.color_off_f[1]);
     }
     sstart[0] = 0; snum[0] = 4; sdim[0] = 0;
     int sp = 1;
@@ -543,7 +543,7 @@ __global__ void k_gather32(PassDesc d, const float2* __restrict__ fx, const floa
     const int j = (int)((id / Mz) % My);
     const int i = (int)(id / ((long long)Mz * My));
     const float2 pc = __ldg(psi + psi_node(d.P, i, j, k));
-    const float invh = (float)(1.0 / d.h);
+    const float invh = d.invhf;
     auto base_diff = [&](int a, int b, int c) {
         const float2 p = __ldg(psi + psi_node(d.P, a, b, c));
         return ((p.x - pc.x) + (p.y - pc.y)) * invh;
@@ -572,8 +572,11 @@ inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 }  // namespace
 
 template <>
-cudaError_t run_pass<float>(const PassDesc& d, const VelocityFields& vel, const float* a, const PassWork<float>& w,
+cudaError_t run_pass<float>(const PassDesc& d64, const VelocityFields& vel64, const float* a, const PassWork<float>& w,
                             const float* in, float* out, int mode, cudaStream_t s) {
+    const PassDesc d = desc32(d64);
+    VelocityFields vel = vel64;
+    vel.fu = field32(vel64.fu); vel.fv = field32(vel64.fv); vel.fw = field32(vel64.fw);
     float2* psi = (float2*)w.psi;
     const long long cols = (long long)d.A.Mx * d.A.Mz;
     k_psi32<<<nblk(cols, 128), 128, 0, s>>>(d, a, psi);
@@ -650,17 +653,19 @@ void piece_store_free(PieceStore& p) {
 }
 
 template <>
-cudaError_t launch_psi<float>(const PassDesc& d, const float* a, float* psi, cudaStream_t s) {
+cudaError_t launch_psi<float>(const PassDesc& d64, const float* a, float* psi, cudaStream_t s) {
+    const PassDesc d = desc32(d64);
     const long long cols = (long long)d.A.Mx * d.A.Mz;
     k_psi32<<<nblk(cols, 128), 128, 0, s>>>(d, a, (float2*)psi);
     return cudaGetLastError();
 }
 
 template <>
-cudaError_t launch_backtrace<float>(const PassDesc& d, const VelocityFields& vel, float* verts, cudaStream_t s) {
+cudaError_t launch_backtrace<float>(const PassDesc& d64, const VelocityFields& vel, float* verts, cudaStream_t s) {
+    const PassDesc d = desc32(d64);
     const long long nv = (long long)(d.A.Mx + 1) * (d.A.My + 1) * (d.A.Mz + 1);
     k_backtrace32<<<nblk(nv, 128), 128, 0, s>>>(d, (const float*)vel.u, (const float*)vel.v, (const float*)vel.w,
-                                               vel.fu, vel.fv, vel.fw, verts);
+                                               field32(vel.fu), field32(vel.fv), field32(vel.fw), verts);
     return cudaGetLastError();
 }
 

@@ -1291,6 +1291,20 @@ int fia_debug_solve_rhs(fia_session* s, const float* rhs, float* x, const fia_so
     return status;
 }
 
+int fia_debug_grid_op(fia_session* s, int op, const float* in, float* out) {
+    if (!s || !s->net || !in || !out || op < 0 || op > 2) return FIA_ERR_INVALID;
+    int d[3];
+    unet::net_level_dims(s->net, 0, d);
+    const long long nc = (long long)s->N[0] * s->N[1] * s->N[2], n0 = (long long)d[0] * d[1] * d[2];
+    const long long nin = op == 1 ? n0 : nc, nout = op == 1 ? nc : n0;
+    float *din = (float*)s->pw[0], *dout = (float*)s->pw[1];
+    CK(cudaMemcpyAsync(din, in, nin * 4, cudaMemcpyHostToDevice, s->stream));
+    CK(unet::net_grid_op(s->net, poisson_grid(s), op, din, dout, s->stream));
+    CK(cudaMemcpyAsync(out, dout, nout * 4, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FIA_OK;
+}
+
 int fia_debug_precondition(fia_session* s, const float* r, float* z) {
     if (!s || !s->net || !r || !z) return FIA_ERR_INVALID;
     const long long nc = (long long)s->N[0] * s->N[1] * s->N[2];

@@ -13,6 +13,7 @@ namespace fia {
 struct NodeField {
     int Mx, My, Mz;
     double ox, oy, oz;  // node offsets in units of the cell length
+    float oxf, oyf, ozf;   // the same in FP32 for the FP32 kernels (set by the host, desc32)
 };
 
 __device__ __forceinline__ int clampi(int i, int hi) { return i < 0 ? 0 : (i > hi ? hi : i); }

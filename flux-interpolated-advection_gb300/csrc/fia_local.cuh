@@ -76,9 +76,9 @@ template <class L>
 __device__ float weno6_3d_loc(const L& load, const NodeField& F, const int* anc, const float* q) {
     int bx, by, bz;
     float sx, sy, sz;
-    locate(anc[0], q[0], (float)F.ox, bx, sx);
-    locate(anc[1], q[1], (float)F.oy, by, sy);
-    locate(anc[2], q[2], (float)F.oz, bz, sz);
+    locate(anc[0], q[0], F.oxf, bx, sx);
+    locate(anc[1], q[1], F.oyf, by, sy);
+    locate(anc[2], q[2], F.ozf, bz, sz);
     float tx[6], ty[6], tz[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
@@ -120,12 +120,12 @@ __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, 
                              const float* ys, const float* ws, int npts, Kahan& acc) {
     int bx, bz, by0, by1;
     float sx, sz, s;
-    locate(anc[0], qx, (float)F.ox, bx, sx);
-    locate(anc[2], qz, (float)F.oz, bz, sz);
+    locate(anc[0], qx, F.oxf, bx, sx);
+    locate(anc[2], qz, F.ozf, bz, sz);
     float ymin = ys[0], ymax = ys[0];
     for (int m = 1; m < npts; ++m) { ymin = fminf(ymin, ys[m]); ymax = fmaxf(ymax, ys[m]); }
-    locate(anc[1], ymin, (float)F.oy, by0, s);
-    locate(anc[1], ymax, (float)F.oy, by1, s);
+    locate(anc[1], ymin, F.oyf, by0, s);
+    locate(anc[1], ymax, F.oyf, by1, s);
     if (by1 - by0 > 1) return 0;
     const bool seven = by1 > by0;
     float tx[6], tz[6];
@@ -153,7 +153,7 @@ __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, 
     for (int m = 0; m < npts; ++m) {
         int by;
         float sy;
-        locate(anc[1], ys[m], (float)F.oy, by, sy);
+        locate(anc[1], ys[m], F.oyf, by, sy);
         const bool up = by > by0;
         float ty[6];
 #pragma unroll
@@ -176,9 +176,9 @@ template <class L>
 __device__ float weno6_1dy_loc(const L& load, const NodeField& F, const int* anc, const float* q) {
     int by;
     float sy;
-    const int ix = clampi(cell_of(anc[0], q[0], (float)F.ox - 0.5f), F.Mx - 1);
-    const int iz = clampi(cell_of(anc[2], q[2], (float)F.oz - 0.5f), F.Mz - 1);
-    locate(anc[1], q[1], (float)F.oy, by, sy);
+    const int ix = clampi(cell_of(anc[0], q[0], F.oxf - 0.5f), F.Mx - 1);
+    const int iz = clampi(cell_of(anc[2], q[2], F.ozf - 0.5f), F.Mz - 1);
+    locate(anc[1], q[1], F.oyf, by, sy);
     float t[6], f[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
@@ -192,9 +192,9 @@ template <class L>
 __device__ float lin3d_loc(const L& load, const NodeField& F, const int* anc, const float* q) {
     int bx, by, bz;
     float sx, sy, sz;
-    locate(anc[0], q[0], (float)F.ox, bx, sx);
-    locate(anc[1], q[1], (float)F.oy, by, sy);
-    locate(anc[2], q[2], (float)F.oz, bz, sz);
+    locate(anc[0], q[0], F.oxf, bx, sx);
+    locate(anc[1], q[1], F.oyf, by, sy);
+    locate(anc[2], q[2], F.ozf, bz, sz);
     const int k0 = clampi(bz, F.Mz - 1), k1 = clampi(bz + 1, F.Mz - 1);
     float yv[2];
 #pragma unroll
@@ -216,9 +216,9 @@ template <class L>
 __device__ float lin1dy_loc(const L& load, const NodeField& F, const int* anc, const float* q) {
     int by;
     float sy;
-    const int ix = clampi(cell_of(anc[0], q[0], (float)F.ox - 0.5f), F.Mx - 1);
-    const int iz = clampi(cell_of(anc[2], q[2], (float)F.oz - 0.5f), F.Mz - 1);
-    locate(anc[1], q[1], (float)F.oy, by, sy);
+    const int ix = clampi(cell_of(anc[0], q[0], F.oxf - 0.5f), F.Mx - 1);
+    const int iz = clampi(cell_of(anc[2], q[2], F.ozf - 0.5f), F.Mz - 1);
+    locate(anc[1], q[1], F.oyf, by, sy);
     const float f0 = load(idx3(F, ix, clampi(by, F.My - 1), iz));
     const float f1 = load(idx3(F, ix, clampi(by + 1, F.My - 1), iz));
     return (1.f - sy) * f0 + sy * f1;

