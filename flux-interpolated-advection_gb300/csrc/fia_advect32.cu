@@ -196,37 +196,31 @@ __device__ int piece_quad32(const PassDesc& d, const int* anc, float cx, float c
         const float f = r - fl;
         const float ylo = fl + oy;   // local y of the y-face below the centroid
         // the density quadrature points (polygon_3D.cpp:286-453): k on [ylo, cy] when the
-        // centroid is in the lower half of the cell, else k on each of [ylo, ylo+1/2], [ylo+1/2, cy]
-        float ys[2 * kMaxGauss], ws[2 * kMaxGauss];
-        int np = 0;
-        if (f < 0.5f) {
-            const float L = cy - ylo;
-            for (int q = 0; q < d.k; ++q) {
-                ys[np] = (L * 0.5f) * d.gxf[q] + (L * 0.5f) + ylo;
-                ws[np++] = ny * f * d.gwf[q];
-            }
-        } else {
-            float lo = ylo, L = 0.5f;
-            for (int q = 0; q < d.k; ++q) {
-                ys[np] = (L * 0.5f) * d.gxf[q] + (L * 0.5f) + lo;
-                ws[np++] = ny * 0.5f * d.gwf[q];
-            }
-            lo = ylo + 0.5f; L = cy - lo;
-            for (int q = 0; q < d.k; ++q) {
-                ys[np] = (L * 0.5f) * d.gxf[q] + (L * 0.5f) + lo;
-                ws[np++] = ny * (f - 0.5f) * d.gwf[q];
-            }
-        }
+        // centroid is in the lower half of the cell, else k on each of [ylo, ylo+1/2], [ylo+1/2, cy];
+        // point m is generated on demand (no per-thread arrays)
+        const bool two = !(f < 0.5f);
+        const float lo0 = ylo, hl0 = two ? 0.25f : (cy - ylo) * 0.5f, wf0 = two ? ny * 0.5f : ny * f;
+        const float lo1 = ylo + 0.5f, hl1 = (cy - lo1) * 0.5f, wf1 = ny * (f - 0.5f);
+        const int k = d.k, np = two ? 2 * k : k;
+        auto point = [&](int m, float& y, float& w) {
+            const bool second = m >= k;
+            const int q = second ? m - k : m;
+            const float hl = second ? hl1 : hl0;
+            y = hl * d.gxf[q] + hl + (second ? lo1 : lo0);
+            w = (second ? wf1 : wf0) * d.gwf[q];
+        };
         bool shared = false;
         if (d.interp == INTERP_WENO6) {
-            const int n1d = weno6_ycolumn(al, d.A, anc, cx, cz, ys, ws, np, F);
+            const int n1d = weno6_ycolumn(al, d.A, anc, cx, cz, ylo, cy, np, point, F);
             shared = n1d > 0;
             evals += n1d;          // 1D WENO6 evaluations executed
         }
         if (!shared) {
             for (int m = 0; m < np; ++m) {
-                const float qq[3] = {cx, ys[m], cz};
-                F.add(interp_loc(d.interp, al, d.A, anc, qq) * ws[m]);
+                float y, w;
+                point(m, y, w);
+                const float qq[3] = {cx, y, cz};
+                F.add(interp_loc(d.interp, al, d.A, anc, qq) * w);
             }
             if (d.interp == INTERP_WENO6) evals += 43 * np;
         }

@@ -79,7 +79,7 @@ __device__ __forceinline__ WenoCoef<T> weno_coef(const T* t) {
 // (no term in the samples themselves survives: the indicators are shift invariant).  In
 // FP32 the sample-product form cancels to an absolute error of ~1e-3 f^2, far above the
 // 1e-6 regularisation; the difference form keeps full relative accuracy and costs less.
-template <typename T>
+template <typename T, bool FASTDIV = false>
 __device__ __forceinline__ T weno6_eval(const T* f, const WenoCoef<T>& w) {
     const T D0 = f[1] - f[0], D1 = f[2] - f[1], D2 = f[3] - f[2], D3 = f[4] - f[3], D4 = f[5] - f[4];
     const T S0 = D1 - D0, S1 = D2 - D1, S2 = D3 - D2;      // second differences
@@ -101,10 +101,16 @@ __device__ __forceinline__ T weno6_eval(const T* f, const WenoCoef<T>& w) {
     // e0^2 e1^2 e2^2 / max(e^2)^2 leaves the weights unchanged and needs two divisions
     // instead of six; the scaling by the largest e^2 keeps the products in range.
     const T q0 = e0 * e0, q1 = e1 * e1, q2 = e2 * e2;
-    const T rq = T(1) / fmax(q0, fmax(q1, q2));
+    const T qm = fmax(q0, fmax(q1, q2));
+    // FP32 form: the two divisions by __fdividef (2 ulp; both denominators are in
+    // [1e-12, 1e4] for sample values of order 1, far inside its range)
+    T rq;
+    if constexpr (FASTDIV) rq = __fdividef(T(1), qm);
+    else rq = T(1) / qm;
     const T t0 = q0 * rq, t1 = q1 * rq, t2 = q2 * rq;
     const T a0 = w.C[0] * (t1 * t2), a1 = w.C[1] * (t0 * t2), a2 = w.C[2] * (t0 * t1);
-    return (a0 * P[0] + a1 * P[1] + a2 * P[2]) / (a0 + a1 + a2);
+    if constexpr (FASTDIV) return __fdividef(a0 * P[0] + a1 * P[1] + a2 * P[2], a0 + a1 + a2);
+    else return (a0 * P[0] + a1 * P[1] + a2 * P[2]) / (a0 + a1 + a2);
 }
 
 // Tensor-product WENO6 of a node field at p (z, then y, then x), stencil indices clamped

@@ -21,7 +21,7 @@ namespace fia {
 // holds; ncu showed most warps waiting on instruction fetch.  Arguments travel in registers.
 __device__ __noinline__ float weno6_f(float f0, float f1, float f2, float f3, float f4, float f5, WenoCoef<float> w) {
     const float f[6] = {f0, f1, f2, f3, f4, f5};
-    return weno6_eval(f, w);
+    return weno6_eval<float, true>(f, w);
 }
 __device__ __forceinline__ float weno6_call(const float* f, const WenoCoef<float>& w) {
     return weno6_f(f[0], f[1], f[2], f[3], f[4], f[5], w);
@@ -112,20 +112,18 @@ __device__ float weno6_3d_loc(const L& load, const NodeField& F, const int* anc,
 // WENO6 at npts points that share x and z and lie within one cell in y (the density
 // quadrature points of one piece, polygon_3D.cpp:286-453): the z-pass over the 6 x 7
 // (x, y) stencil rows is done once and shared; each point then needs 6 y- and 1 x-
-// evaluation instead of 43.  Bit-identical to evaluating the points one by one.  Returns
-// the number of 1D evaluations made, or 0 (nothing accumulated) if the points span more
-// than one cell.
-template <class L>
-__device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, float qx, float qz,
-                             const float* ys, const float* ws, int npts, Kahan& acc) {
+// evaluation instead of 43.  Bit-identical to evaluating the points one by one.  The points
+// come from point(m, y, w) and lie in [ya, yb]; returns the number of 1D evaluations made, or
+// 0 (nothing accumulated) if [ya, yb] spans more than one cell of the field.
+template <class L, class P>
+__device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, float qx, float qz, float ya,
+                             float yb, int npts, const P& point, Kahan& acc) {
     int bx, bz, by0, by1;
     float sx, sz, s;
     locate(anc[0], qx, F.oxf, bx, sx);
     locate(anc[2], qz, F.ozf, bz, sz);
-    float ymin = ys[0], ymax = ys[0];
-    for (int m = 1; m < npts; ++m) { ymin = fminf(ymin, ys[m]); ymax = fmaxf(ymax, ys[m]); }
-    locate(anc[1], ymin, F.oyf, by0, s);
-    locate(anc[1], ymax, F.oyf, by1, s);
+    locate(anc[1], ya, F.oyf, by0, s);
+    locate(anc[1], yb, F.oyf, by1, s);
     if (by1 - by0 > 1) return 0;
     const bool seven = by1 > by0;
     float tx[6], tz[6];
@@ -151,9 +149,11 @@ __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, 
         }
     }
     for (int m = 0; m < npts; ++m) {
+        float y, w;
+        point(m, y, w);
         int by;
         float sy;
-        locate(anc[1], ys[m], F.oyf, by, sy);
+        locate(anc[1], y, F.oyf, by, sy);
         const bool up = by > by0;
         float ty[6];
 #pragma unroll
@@ -167,7 +167,7 @@ __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, 
             for (int i = 0; i < 6; ++i) f[i] = up ? zr[ix][i + 1] : zr[ix][i];
             yv[ix] = weno6_call(f, cy);
         }
-        acc.add(weno6_call(yv, cx) * ws[m]);
+        acc.add(weno6_call(yv, cx) * w);
     }
     return (seven ? 42 : 36) + 7 * npts;
 }

@@ -91,7 +91,6 @@ struct ConvArgs {
     int relu;
     int nt;               // n-tiles (8 output channels) of the weight fragments
     int nsplit;           // CTAs sharing one brick, each with nt / nsplit n-tiles
-    int wsm;              // 1: the CTA's weight slice is staged in shared memory after the halo
 };
 
 __device__ __forceinline__ int swz(int u) { return (u & ~7) | ((u ^ (u >> 3)) & 7); }
@@ -272,20 +271,7 @@ __global__ void __launch_bounds__(kConvThreads) k_conv2(ConvArgs a) {
     const int n0 = part * NTL;
     const int bz = zb * 16, by = blockIdx.y * 4, bx = blockIdx.z * MT;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    constexpr int HV = (MT + 2) * HY * HZ;
-    const int halo_units = TAP ? (HV * 2 + 15) / 16 : HV * odd_units(a.cin);
-    uint2* wsh = reinterpret_cast<uint2*>(smem + halo_units);
     const int NT = a.nt;
-    if (a.wsm) {
-        // the weight fragments of this CTA's n-tiles, 256 bytes per (k chunk, n-tile)
-        const int nk = TAP ? 2 : 27 * (a.cin >> 4);
-        const uint32_t wbase = (uint32_t)__cvta_generic_to_shared(wsh);
-        for (int ch = threadIdx.x; ch < nk * NTL * 16; ch += blockDim.x) {
-            const int piece = ch & 15, n = (ch >> 4) % NTL, kk = (ch >> 4) / NTL;
-            const char* src = reinterpret_cast<const char*>(a.wfrag + ((size_t)kk * NT + n0 + n) * 32) + piece * 16;
-            cp_async16(wbase + (uint32_t)((kk * NTL + n) * 256 + piece * 16), src, 16);
-        }
-    }
     if (TAP) stage2_scalar<MT>(a, reinterpret_cast<__nv_bfloat16*>(smem), bx, by, bz);
     else stage2<MT>(a, smem, bx, by, bz);
     cp_async_wait_all();
@@ -320,7 +306,7 @@ __global__ void __launch_bounds__(kConvThreads) k_conv2(ConvArgs a) {
                 for (int mt = 0; mt < MT; ++mt) ldsm_x4(A[mt], addr[mt] + c16 * 32);
 #pragma unroll
                 for (int n = 0; n < NTL; ++n) {
-                    const uint2 b = a.wsm ? wsh[((tap * nc16 + c16) * NTL + n) * 32 + lane] : __ldg(wt + (c16 * NT + n) * 32);
+                    const uint2 b = __ldg(wt + (c16 * NT + n) * 32);
 #pragma unroll
                     for (int mt = 0; mt < MT; ++mt) mma_bf16(acc[mt][n], A[mt], b.x, b.y);
                 }
@@ -353,7 +339,7 @@ __global__ void __launch_bounds__(kConvThreads) k_conv2(ConvArgs a) {
             }
 #pragma unroll
             for (int n = 0; n < NTL; ++n) {
-                const uint2 b = a.wsm ? wsh[(kc * NTL + n) * 32 + lane] : __ldg(a.wfrag + (kc * NT + n0 + n) * 32 + lane);
+                const uint2 b = __ldg(a.wfrag + (kc * NT + n0 + n) * 32 + lane);
 #pragma unroll
                 for (int mt = 0; mt < MT; ++mt) mma_bf16(acc[mt][n], A[mt], b.x, b.y);
             }
@@ -887,23 +873,15 @@ size_t conv2_smem(int cin, int mt) {
     return (size_t)hv * odd_units(cin) * 16;
 }
 
-// bytes of the weight fragments of one CTA (ntl n-tiles)
-size_t conv2_wbytes(int cin, int ntl) { return (size_t)(cin == 1 ? 2 : 27 * (cin / 16)) * ntl * 256; }
-
-constexpr size_t kConvSmemMax = 200 * 1024;
-
 template <int NTL, int MT, bool TAP>
 cudaError_t launch_conv2_t(ConvArgs a, int nsplit, cudaStream_t s) {
+    const size_t sm = conv2_smem(a.cin, MT);
     static bool attr = false;
     if (!attr) {
-        UCK(cudaFuncSetAttribute(k_conv2<NTL, MT, TAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kConvSmemMax));
+        UCK(cudaFuncSetAttribute(k_conv2<NTL, MT, TAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024));
         attr = true;
     }
-    // weights in shared memory when the CTA still fits twice on an SM (227 KB)
-    const size_t halo = conv2_smem(a.cin, MT), wb = conv2_wbytes(a.cin, NTL);
-    a.wsm = halo + wb <= 110 * 1024 ? 1 : 0;
-    const size_t sm = halo + (a.wsm ? wb : 0);
-    if (sm > kConvSmemMax) return cudaErrorInvalidValue;
+    if (sm > 120 * 1024) return cudaErrorInvalidValue;
     a.nsplit = nsplit;
     const dim3 grid(((a.dims[2] + 15) / 16) * nsplit, (a.dims[1] + 3) / 4, (a.dims[0] + MT - 1) / MT);
     k_conv2<NTL, MT, TAP><<<grid, kConvThreads, sm, s>>>(a);
@@ -911,9 +889,10 @@ cudaError_t launch_conv2_t(ConvArgs a, int nsplit, cudaStream_t s) {
 }
 
 // Chooses the brick (MT) and the n-tile split for a convolution with cout_padded output
-// channels: 4 x 4 x 16 bricks where the grid gives at least two CTAs per SM and the halo
-// and weights of the CTA fit three times on an SM, 2 x 4 x 16 bricks otherwise; on coarse
-// levels the output channels are split 16 per CTA.
+// channels: whole bricks of 4 x 4 x 16 voxels (up to 32 output channels) or 2 x 4 x 16 where
+// the grid gives at least two CTAs per SM, else 2 x 4 x 16 bricks with the output channels
+// split 16 per CTA.  (Staging the weights in shared memory as well was measured slower: it
+// costs CTAs per SM, and the weights stay in L1.)
 cudaError_t launch_conv(ConvArgs a, int cout_padded, cudaStream_t s) {
     const int nt = cout_padded / 8;
     a.nt = nt;
@@ -925,11 +904,10 @@ cudaError_t launch_conv(ConvArgs a, int cout_padded, cudaStream_t s) {
     }
     if (a.cin % 16 != 0) return cudaErrorInvalidValue;
     if (big) {
-        const bool fits4 = conv2_smem(a.cin, 4) + conv2_wbytes(a.cin, nt) <= 75 * 1024;
         switch (nt) {
-            case 1: return fits4 ? launch_conv2_t<1, 4, false>(a, 1, s) : launch_conv2_t<1, 2, false>(a, 1, s);
-            case 2: return fits4 ? launch_conv2_t<2, 4, false>(a, 1, s) : launch_conv2_t<2, 2, false>(a, 1, s);
-            case 4: return fits4 ? launch_conv2_t<4, 4, false>(a, 1, s) : launch_conv2_t<4, 2, false>(a, 1, s);
+            case 1: return launch_conv2_t<1, 4, false>(a, 1, s);
+            case 2: return launch_conv2_t<2, 4, false>(a, 1, s);
+            case 4: return launch_conv2_t<4, 4, false>(a, 1, s);
             case 6: return launch_conv2_t<6, 2, false>(a, 1, s);
             case 8: return launch_conv2_t<8, 2, false>(a, 1, s);
             case 10: return launch_conv2_t<10, 2, false>(a, 1, s);

@@ -19,8 +19,9 @@ The network (fia_unet.cu) is trained with Adam on the energy-norm loss
 out for validation.  Finally flexible CG with the trained network is compared with Jacobi-PCG
 on a fresh plume state.
 
-    python train_preconditioner.py [--grid 128] [--runs 6] [--steps 30] [--iters 1500] \
-        [--batch 4] [--lr 2e-3] [--seed 1] [--out weights/unet_precond.f32]
+    python train_preconditioner.py [--grid 128] [--runs 6] [--steps 30] [--iters 6000] \
+        [--batch 4] [--lr 1e-3] [--onpolicy 120] [--onpolicy-share 0.25] [--seed 1] \
+        [--eval-grids 128,256] [--out weights/unet_precond.f32]
 
 Writes the FP32 parameter vector (fia_learned_num_parameters() floats, little endian) to
 --out and the training record (losses, iteration counts) next to it as JSON.
@@ -201,8 +202,11 @@ def main():
     ap.add_argument("--iters", type=int, default=6000)
     ap.add_argument("--synthetic", type=int, default=25, help="multi-scale pairs per run")
     ap.add_argument("--onpolicy", type=int, default=120, help="flexible-CG residual pairs after phase 1")
+    ap.add_argument("--onpolicy-share", type=float, default=0.25,
+                    help="fraction of each batch drawn from the on-policy pairs once they exist")
+    ap.add_argument("--eval-grids", default="128", help="grids of the final solver comparison")
     ap.add_argument("--batch", type=int, default=4)
-    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--out", default=DEFAULT_OUT)
     ap.add_argument("--init", default=None, help="start from these weights instead of a random init")
@@ -228,16 +232,20 @@ def main():
     curve = []
     t0 = time.time()
     phase1 = args.iters // 3
+    onpol = []
     for it in range(args.iters):
         if it == phase1 and args.onpolicy > 0:
             first = g.learned_num_pairs()
             t1 = time.time()
             add_onpolicy_pairs(g, n, rng, args.onpolicy)
-            train += list(range(first, g.learned_num_pairs()))
+            onpol = list(range(first, g.learned_num_pairs()))
             record["onpolicy_seconds"] = time.time() - t1
-            print("added %d on-policy pairs (%.1f s)" % (g.learned_num_pairs() - first, time.time() - t1), flush=True)
+            print("added %d on-policy pairs (%.1f s)" % (len(onpol), time.time() - t1), flush=True)
         lr = args.lr * 0.5 * (1.0 + math.cos(math.pi * it / args.iters))
-        batch = rng.choice(train, size=args.batch, replace=False)
+        k_on = int(round(args.batch * args.onpolicy_share)) if onpol else 0
+        batch = list(rng.choice(train, size=args.batch - k_on, replace=False))
+        if k_on:
+            batch += list(rng.choice(onpol, size=k_on, replace=False))
         losses = g.learned_train_step(batch, lr)
         curve.append(float(np.mean(losses)))
         if (it + 1) % 250 == 0 or it == 0:
@@ -252,6 +260,12 @@ def main():
     w.astype("<f4").tofile(args.out)
     record["solvers"] = compare_solvers(g, n, args.seed + 1000)
     print(json.dumps(record["solvers"]), flush=True)
+    for m in [int(x) for x in args.eval_grids.split(",") if x and int(x) != n]:
+        ge = fia.Grid3D(m, m, m, 1.0 / m, precision=fia.FIA_FP32C)
+        ge.learned_set_weights(w)
+        record["solvers_%d" % m] = compare_solvers(ge, m, args.seed + 1000, steps=6)
+        print(m, json.dumps(record["solvers_%d" % m]), flush=True)
+        ge.close()
     with open(os.path.splitext(args.out)[0] + ".json", "w") as f:
         json.dump(record, f, indent=1)
     g.close()
