@@ -51,7 +51,7 @@ def read_peaks():
 def traffic_from_profile():
     """dram bytes per k_quad32 launch at 256^3 from the committed ncu summary (measured on a
     smaller plume and scaled by the pieces processed), if present."""
-    path = os.path.join(ROOT, "profiles", "k_quad32_plume.md")
+    path = os.path.join(ROOT, "profiles", "k_quad32_plume128.md")
     try:
         for line in open(path):
             if line.strip().startswith("traffic_bytes_per_launch_256:"):
