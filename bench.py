@@ -34,7 +34,7 @@ UNIT = "steps/s"
 # FP32 operation count of one 1D WENO6 evaluation as implemented in fia_device.cuh
 # (weno6_eval: differences 12, three cubic candidates 18, three smoothness indicators 57,
 # nonlinear weights and the weighted sum 26; an FMA counted as two).  The face kernel counts
-# the 1D evaluations it executes.  Frozen; see the design doc.
+# the 1D evaluations it executes.  Frozen.
 WENO1D_FLOP = 113
 FP32_LANES_PER_SM = 128
 SMS = 152
