@@ -488,7 +488,7 @@ __global__ void __launch_bounds__(128) k_clip32(PassDesc d, int fam, const float
     }
 }
 
-__global__ void __launch_bounds__(128, 5) k_quad32(PassDesc d, const float* __restrict__ a, const float2* __restrict__ psi,
+__global__ void __launch_bounds__(128) k_quad32(PassDesc d, const float* __restrict__ a, const float2* __restrict__ psi,
                                                 PieceStore ps, long long npc, unsigned long long* counters) {
     unsigned long long ec = 0;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < npc; t += (long long)gridDim.x * blockDim.x) {
