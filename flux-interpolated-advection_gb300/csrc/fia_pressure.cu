@@ -151,6 +151,30 @@ __device__ __forceinline__ int for_neighbours(const PoissonGrid& g, unsigned c, 
     return diag;
 }
 
+// Net outflow of free cell c, summed over its six faces in the accumulation type A.  A face
+// shared with a solid cell carries the solid's zero velocity whatever the array holds there
+// (advection and buoyancy write every face), so the right-hand side matches the operator,
+// whose rows drop solid neighbours, and the projected field is divergence-free next to solids.
+template <typename A, typename T>
+__device__ __forceinline__ A net_outflow(const PoissonGrid& g, unsigned c, Cell k, const T* __restrict__ u,
+                                         const T* __restrict__ v, const T* __restrict__ w) {
+    const int ny = g.ny, nz = g.nz;
+    const unsigned sx = (unsigned)ny * nz;
+    const unsigned u0 = c, u1 = c + sx;
+    const unsigned v0 = ((unsigned)k.ix * (ny + 1) + k.iy) * nz + k.iz, v1 = v0 + nz;
+    const unsigned w0 = ((unsigned)k.ix * ny + k.iy) * (nz + 1) + k.iz, w1 = w0 + 1;
+    A fu0 = (A)u[u0], fu1 = (A)u[u1], fv0 = (A)v[v0], fv1 = (A)v[v1], fw0 = (A)w[w0], fw1 = (A)w[w1];
+    if (g.solid) {
+        if (k.ix > 0 && g.solid[c - sx]) fu0 = A(0);
+        if (k.ix < g.nx - 1 && g.solid[c + sx]) fu1 = A(0);
+        if (k.iy > 0 && g.solid[c - nz]) fv0 = A(0);
+        if (k.iy < ny - 1 && g.solid[c + nz]) fv1 = A(0);
+        if (k.iz > 0 && g.solid[c - 1]) fw0 = A(0);
+        if (k.iz < nz - 1 && g.solid[c + 1]) fw1 = A(0);
+    }
+    return (fu1 - fu0) + (fv1 - fv0) + (fw1 - fw0);
+}
+
 template <typename T>
 __device__ __forceinline__ T inv_count(int d) {
     return d > 0 ? T(1) / T(d) : T(0);
@@ -172,10 +196,7 @@ __global__ void __launch_bounds__(kRedThreads) k_rhs(PoissonGrid g, T h, const T
         const Cell k = decode(c, ny, nz);
         T b = T(0), rc = T(0);
         if (!excluded(g, c)) {
-            const unsigned u0 = c, u1 = c + (unsigned)ny * nz;
-            const unsigned v0 = ((unsigned)k.ix * (ny + 1) + k.iy) * nz + k.iz, v1 = v0 + nz;
-            const unsigned w0 = ((unsigned)k.ix * ny + k.iy) * (nz + 1) + k.iz, w1 = w0 + 1;
-            b = ((u[u1] - u[u0]) + (v[v1] - v[v0]) + (w[w1] - w[w0])) * h;
+            b = net_outflow<T>(g, c, k, u, v, w) * h;
             rc = -b;
             if (warm) {
                 T s = T(0);
@@ -836,11 +857,7 @@ __global__ void __launch_bounds__(kRedThreads) k_true_residual(PoissonGrid g, do
         double rc = 0.0;
         if (!excluded(g, c)) {
             const Cell k = decode(c, ny, nz);
-            const unsigned u0 = c, u1 = c + (unsigned)ny * nz;
-            const unsigned v0 = ((unsigned)k.ix * (ny + 1) + k.iy) * nz + k.iz, v1 = v0 + nz;
-            const unsigned w0 = ((unsigned)k.ix * ny + k.iy) * (nz + 1) + k.iz, w1 = w0 + 1;
-            const double b = (((double)u[u1] - (double)u[u0]) + ((double)v[v1] - (double)v[v0]) +
-                              ((double)w[w1] - (double)w[w0])) * h;
+            const double b = net_outflow<double>(g, c, k, u, v, w) * h;
             double s = 0.0;
             const int diag = for_neighbours(g, c, k, [&](unsigned o) { s += p[o]; });
             rc = -b - ((double)diag * p[c] - s);
