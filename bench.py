@@ -32,10 +32,10 @@ import numpy as np  # noqa: E402
 METRIC = "steps/s at 256^3 smoke step (flux advection of density and velocity + pressure to 1e-6)"
 UNIT = "steps/s"
 # FP32 operation count of one 1D WENO6 evaluation as implemented in fia_device.cuh
-# (weno6_eval: differences 12, three cubic candidates 18, three smoothness indicators 57,
-# nonlinear weights and the weighted sum 26; an FMA counted as two).  The face kernel counts
-# the 1D evaluations it executes.  Frozen.
-WENO1D_FLOP = 113
+# (weno6_eval, FP32 form: differences 12, three cubic candidates 18, three smoothness
+# indicators in Horner form 42, nonlinear weights and the weighted sum 26; an FMA counted as
+# two).  The face kernel counts the 1D evaluations it executes.
+WENO1D_FLOP = 98
 FP32_LANES_PER_SM = 128
 SMS = 152
 

@@ -88,22 +88,37 @@ __device__ __forceinline__ T weno6_eval(const T* f, const WenoCoef<T>& w) {
     T P[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) P[i] = f[i] + D[i] * w.a[i] + S[i] * w.b[i] + Tt[i] * w.c[i];
-    const T r180 = T(1) / T(180);
-    const T b0 = (T(244) * D0 * D0 - T(1171) * D0 * D1 + T(683) * D0 * D2 + T(1561) * D1 * D1
-                  - T(1951) * D1 * D2 + T(814) * D2 * D2) * r180;
-    const T b1 = (T(244) * D1 * D1 - T(781) * D1 * D2 + T(293) * D1 * D3 + T(961) * D2 * D2
-                  - T(781) * D2 * D3 + T(244) * D3 * D3) * r180;
-    const T b2 = (T(814) * D2 * D2 - T(1951) * D2 * D3 + T(683) * D2 * D4 + T(1561) * D3 * D3
-                  - T(1171) * D3 * D4 + T(244) * D4 * D4) * r180;
-    const T eps = T(0.000001);
-    const T e0 = eps + b0, e1 = eps + b1, e2 = eps + b2;
+    T e0, e1, e2;
+    if constexpr (FASTDIV) {
+        // FP32 form: the indicators in Horner form, and all three (and eps) scaled by 180,
+        // which cancels in the normalised weights: 180 eps + 180 beta_i with no division
+        const T s0 = D0 * (T(244) * D0 - T(1171) * D1 + T(683) * D2) + D1 * (T(1561) * D1 - T(1951) * D2)
+                     + T(814) * D2 * D2;
+        const T s1 = D1 * (T(244) * D1 - T(781) * D2 + T(293) * D3) + D2 * (T(961) * D2 - T(781) * D3)
+                     + T(244) * D3 * D3;
+        const T s2 = D2 * (T(814) * D2 - T(1951) * D3 + T(683) * D4) + D3 * (T(1561) * D3 - T(1171) * D4)
+                     + T(244) * D4 * D4;
+        const T eps180 = T(0.00018);
+        e0 = eps180 + s0; e1 = eps180 + s1; e2 = eps180 + s2;
+    } else {
+        const T r180 = T(1) / T(180);
+        const T b0 = (T(244) * D0 * D0 - T(1171) * D0 * D1 + T(683) * D0 * D2 + T(1561) * D1 * D1
+                      - T(1951) * D1 * D2 + T(814) * D2 * D2) * r180;
+        const T b1 = (T(244) * D1 * D1 - T(781) * D1 * D2 + T(293) * D1 * D3 + T(961) * D2 * D2
+                      - T(781) * D2 * D3 + T(244) * D3 * D3) * r180;
+        const T b2 = (T(814) * D2 * D2 - T(1951) * D2 * D3 + T(683) * D2 * D4 + T(1561) * D3 * D3
+                      - T(1171) * D3 * D4 + T(244) * D4 * D4) * r180;
+        const T eps = T(0.000001);
+        e0 = eps + b0; e1 = eps + b1; e2 = eps + b2;
+    }
     // alpha_i = C_i / e_i^2 and w_i = alpha_i / sum(alpha).  Multiplying every alpha by
     // e0^2 e1^2 e2^2 / max(e^2)^2 leaves the weights unchanged and needs two divisions
     // instead of six; the scaling by the largest e^2 keeps the products in range.
     const T q0 = e0 * e0, q1 = e1 * e1, q2 = e2 * e2;
     const T qm = fmax(q0, fmax(q1, q2));
-    // FP32 form: the two divisions by __fdividef (2 ulp; both denominators are in
-    // [1e-12, 1e4] for sample values of order 1, far inside its range)
+    // FP32 form: the two divisions by __fdividef (2 ulp; qm is at least (180 eps)^2 and, for
+    // sample values of order 1, below 1e9, and the weight sum lies in [min C, 3]: both far
+    // inside its range, which ends at 2^126)
     T rq;
     if constexpr (FASTDIV) rq = __fdividef(T(1), qm);
     else rq = T(1) / qm;
