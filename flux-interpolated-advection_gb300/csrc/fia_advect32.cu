@@ -184,8 +184,10 @@ __device__ void piece_geom32(const LocalFace& g, const float* px, const float* p
 
 // The quadrature of one piece (polygon_3D.cpp:257-487): density points on the y-interval
 // below the centroid and one psi point; returns the number of 1D WENO6 evaluations.
+constexpr int kQuadThreads = 128;
+
 __device__ int piece_quad32(const PassDesc& d, const int* anc, float cx, float cy, float cz, float ny,
-                            const float* __restrict__ a, const PsiLoad& pl, Kahan& F) {
+                            const float* __restrict__ a, const PsiLoad& pl, Kahan& F, float* zs) {
     const PlainLoad al{a};
     const float invh = d.invhf;   // psi carries a length; the face terms are per cell volume
     int evals = 0;
@@ -211,7 +213,7 @@ __device__ int piece_quad32(const PassDesc& d, const int* anc, float cx, float c
         };
         bool shared = false;
         if (d.interp == INTERP_WENO6) {
-            const int n1d = weno6_ycolumn(al, d.A, anc, cx, cz, ylo, cy, np, point, F);
+            const int n1d = weno6_ycolumn<kQuadThreads>(al, d.A, anc, cx, cz, ylo, cy, np, point, F, zs);
             shared = n1d > 0;
             evals += n1d;          // 1D WENO6 evaluations executed
         }
@@ -488,8 +490,10 @@ __global__ void __launch_bounds__(128) k_clip32(PassDesc d, int fam, const float
     }
 }
 
-__global__ void __launch_bounds__(128) k_quad32(PassDesc d, const float* __restrict__ a, const float2* __restrict__ psi,
-                                                PieceStore ps, long long npc, unsigned long long* counters) {
+__global__ void __launch_bounds__(kQuadThreads) k_quad32(PassDesc d, const float* __restrict__ a,
+                                                         const float2* __restrict__ psi, PieceStore ps, long long npc,
+                                                         unsigned long long* counters) {
+    __shared__ float zcol[42 * kQuadThreads];   // each thread's z-pass column (weno6_ycolumn)
     unsigned long long ec = 0;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < npc; t += (long long)gridDim.x * blockDim.x) {
         const float4 p = ps.rec[t];
@@ -500,7 +504,7 @@ __global__ void __launch_bounds__(128) k_quad32(PassDesc d, const float* __restr
         const float2 b = __ldg(psi + psi_node(d.P, anc[0], anc[1], anc[2]));
         const PsiLoad pl{psi, b.x, b.y};
         Kahan F;
-        ec += (unsigned long long)piece_quad32(d, anc, p.x, p.y, p.z, p.w, a, pl, F);
+        ec += (unsigned long long)piece_quad32(d, anc, p.x, p.y, p.z, p.w, a, pl, F, zcol + threadIdx.x);
         ps.flux[t] = F.value();
     }
     for (int o = 16; o > 0; o >>= 1) ec += __shfl_down_sync(0xffffffffu, ec, o);
@@ -602,7 +606,7 @@ cudaError_t run_pass<float>(const PassDesc& d64, const VelocityFields& vel64, co
     if ((long long)npc > ps.cap) return cudaErrorMemoryAllocation;
     if (npc > 0) {
         prof_mark(w, 0, s);
-        k_quad32<<<152 * 8, 128, 0, s>>>(d, a, psi, ps, (long long)npc, w.counters);
+        k_quad32<<<152 * 8, kQuadThreads, 0, s>>>(d, a, psi, ps, (long long)npc, w.counters);
         prof_mark(w, 1, s);
     }
     for (int fam = 0; fam < 3; ++fam)

@@ -26,6 +26,17 @@ __device__ __noinline__ float weno6_f(float f0, float f1, float f2, float f3, fl
 __device__ __forceinline__ float weno6_call(const float* f, const WenoCoef<float>& w) {
     return weno6_f(f[0], f[1], f[2], f[3], f[4], f[5], w);
 }
+// Two evaluations with the same coefficients in one call: the two dependency chains (the
+// weights end in a serial max / reciprocal / normalise tail) interleave, which a call per
+// evaluation prevents, at half the calls.  Each result equals weno6_f's.
+__device__ __noinline__ float2 weno6_f2(float a0, float a1, float a2, float a3, float a4, float a5, float b0, float b1,
+                                        float b2, float b3, float b4, float b5, WenoCoef<float> w) {
+    const float fa[6] = {a0, a1, a2, a3, a4, a5}, fb[6] = {b0, b1, b2, b3, b4, b5};
+    return make_float2(weno6_eval<float, true>(fa, w), weno6_eval<float, true>(fb, w));
+}
+__device__ __forceinline__ float2 weno6_call2(const float* a, const float* b, const WenoCoef<float>& w) {
+    return weno6_f2(a[0], a[1], a[2], a[3], a[4], a[5], b[0], b[1], b[2], b[3], b[4], b[5], w);
+}
 
 // error-free sum of two floats (Knuth TwoSum)
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
@@ -96,13 +107,14 @@ __device__ float weno6_3d_loc(const L& load, const NodeField& F, const int* anc,
         const int ii = clampi(bx - 2 + ix, F.Mx - 1);
         float zv[6];
 #pragma unroll
-        for (int iy = 0; iy < 6; ++iy) {
-            const int jj = clampi(by - 2 + iy, F.My - 1);
-            const long long row = (long long)F.Mz * ((long long)F.My * ii + jj);
-            float f[6];
+        for (int iy = 0; iy < 6; iy += 2) {
+            const long long j0 = clampi(by - 2 + iy, F.My - 1), j1 = clampi(by - 1 + iy, F.My - 1);
+            const long long row0 = F.Mz * (F.My * (long long)ii + j0), row1 = F.Mz * (F.My * (long long)ii + j1);
+            float f0[6], f1[6];
 #pragma unroll
-            for (int iz = 0; iz < 6; ++iz) f[iz] = load(row + kk[iz]);
-            zv[iy] = weno6_call(f, cz);
+            for (int iz = 0; iz < 6; ++iz) { f0[iz] = load(row0 + kk[iz]); f1[iz] = load(row1 + kk[iz]); }
+            const float2 v = weno6_call2(f0, f1, cz);
+            zv[iy] = v.x; zv[iy + 1] = v.y;
         }
         yv[ix] = weno6_call(zv, cy);
     }
@@ -115,9 +127,12 @@ __device__ float weno6_3d_loc(const L& load, const NodeField& F, const int* anc,
 // evaluation instead of 43.  Bit-identical to evaluating the points one by one.  The points
 // come from point(m, y, w) and lie in [ya, yb]; returns the number of 1D evaluations made, or
 // 0 (nothing accumulated) if [ya, yb] spans more than one cell of the field.
-template <class L, class P>
+// The 6 x 7 z-pass results live in shared memory, zs[(7 ix + r) * stride] (the calling
+// thread's column of a block-wide array, stride = threads per block): in registers they held
+// 42 of the face kernel's 128.
+template <int STRIDE, class L, class P>
 __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, float qx, float qz, float ya,
-                             float yb, int npts, const P& point, Kahan& acc) {
+                             float yb, int npts, const P& point, Kahan& acc, float* zs) {
     int bx, bz, by0, by1;
     float sx, sz, s;
     locate(anc[0], qx, F.oxf, bx, sx);
@@ -133,19 +148,21 @@ __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, 
     int kk[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) kk[i] = clampi(bz - 2 + i, F.Mz - 1);
-    float zr[6][7];
-#pragma unroll
-    for (int ix = 0; ix < 6; ++ix) {
-        const int ii = clampi(bx - 2 + ix, F.Mx - 1);
+#pragma unroll 1
+    for (int ix = 0; ix < 6; ix += 2) {
+        const long long i0 = clampi(bx - 2 + ix, F.Mx - 1), i1 = clampi(bx - 1 + ix, F.Mx - 1);
+        float* z0 = zs + 7 * ix * STRIDE;
+        float* z1 = z0 + 7 * STRIDE;
 #pragma unroll
         for (int r = 0; r < 7; ++r) {
-            if (r == 6 && !seven) { zr[ix][6] = 0.f; continue; }
-            const int jj = clampi(by0 - 2 + r, F.My - 1);
-            const long long row = (long long)F.Mz * ((long long)F.My * ii + jj);
-            float f[6];
+            if (r == 6 && !seven) break;
+            const long long jj = clampi(by0 - 2 + r, F.My - 1);
+            const long long row0 = F.Mz * (F.My * i0 + jj), row1 = F.Mz * (F.My * i1 + jj);
+            float f0[6], f1[6];
 #pragma unroll
-            for (int iz = 0; iz < 6; ++iz) f[iz] = load(row + kk[iz]);
-            zr[ix][r] = weno6_call(f, cz);
+            for (int iz = 0; iz < 6; ++iz) { f0[iz] = load(row0 + kk[iz]); f1[iz] = load(row1 + kk[iz]); }
+            const float2 v = weno6_call2(f0, f1, cz);
+            z0[r * STRIDE] = v.x; z1[r * STRIDE] = v.y;
         }
     }
     for (int m = 0; m < npts; ++m) {
@@ -160,12 +177,17 @@ __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, 
         for (int i = 0; i < 6; ++i) ty[i] = sy + float(2 - i);
         const WenoCoef<float> cy = weno_coef(ty);
         float yv[6];
+        const float* zb = zs + (up ? STRIDE : 0);
 #pragma unroll
-        for (int ix = 0; ix < 6; ++ix) {
-            float f[6];
+        for (int ix = 0; ix < 6; ix += 2) {
+            float f0[6], f1[6];
 #pragma unroll
-            for (int i = 0; i < 6; ++i) f[i] = up ? zr[ix][i + 1] : zr[ix][i];
-            yv[ix] = weno6_call(f, cy);
+            for (int i = 0; i < 6; ++i) {
+                f0[i] = zb[(7 * ix + i) * STRIDE];
+                f1[i] = zb[(7 * ix + 7 + i) * STRIDE];
+            }
+            const float2 v = weno6_call2(f0, f1, cy);
+            yv[ix] = v.x; yv[ix + 1] = v.y;
         }
         acc.add(weno6_call(yv, cx) * w);
     }
