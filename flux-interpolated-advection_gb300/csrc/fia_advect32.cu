@@ -226,13 +226,21 @@ __device__ int piece_quad32(const PassDesc& d, const int* anc, float cx, float c
             }
             if (d.interp == INTERP_WENO6) evals += 43 * np;
         }
+        // the psi point lies on the psi node row of the y-face below the centroid
         const float qp[3] = {cx, ylo, cz};
-        F.add(interp_loc(d.interp, pl, d.P, anc, qp) * (ny * invh));
+        float v;
+        const int n1d = d.interp == INTERP_WENO6 ? weno6_3d_noderow(pl, d.P, anc, qp, v) : 0;
+        if (n1d == 0) {
+            v = interp_loc(d.interp, pl, d.P, anc, qp);
+            if (d.interp == INTERP_WENO6) evals += 43;
+        }
+        evals += n1d;
+        F.add(v * (ny * invh));
     } else {
         const float qp[3] = {cx, cy, cz};
         F.add(interp_loc(d.interp, pl, d.P, anc, qp) * (ny * invh));
+        if (d.interp == INTERP_WENO6) evals += 43;
     }
-    if (d.interp == INTERP_WENO6) evals += 43;
     return evals;
 }
 

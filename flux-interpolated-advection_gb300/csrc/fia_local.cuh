@@ -246,6 +246,43 @@ __device__ float lin1dy_loc(const L& load, const NodeField& F, const int* anc, c
     return (1.f - sy) * f0 + sy * f1;
 }
 
+// WENO6 at a point whose y lies on a node row of F (fractional offset exactly 0, as for the
+// psi point of a piece, which sits on the y-face below the centroid).  Every candidate
+// polynomial of the y-pass interpolates that node and the weights sum to one, so the y-pass
+// returns the row's value: the interpolant is the (x, z) WENO6 of the row, 7 evaluations
+// instead of 43, equal to the full form in exact arithmetic.  Returns the number of 1D
+// evaluations, or 0 (out untouched) if y is not on a node row.
+template <class L>
+__device__ int weno6_3d_noderow(const L& load, const NodeField& F, const int* anc, const float* q, float& out) {
+    int bx, by, bz;
+    float sx, sy, sz;
+    locate(anc[1], q[1], F.oyf, by, sy);
+    if (sy != 0.f) return 0;
+    locate(anc[0], q[0], F.oxf, bx, sx);
+    locate(anc[2], q[2], F.ozf, bz, sz);
+    float tx[6], tz[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) { tx[i] = sx + float(2 - i); tz[i] = sz + float(2 - i); }
+    const WenoCoef<float> cx = weno_coef(tx), cz = weno_coef(tz);
+    int kk[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) kk[i] = clampi(bz - 2 + i, F.Mz - 1);
+    const long long jj = clampi(by, F.My - 1);
+    float xv[6];
+#pragma unroll
+    for (int ix = 0; ix < 6; ix += 2) {
+        const long long i0 = clampi(bx - 2 + ix, F.Mx - 1), i1 = clampi(bx - 1 + ix, F.Mx - 1);
+        const long long row0 = F.Mz * (F.My * i0 + jj), row1 = F.Mz * (F.My * i1 + jj);
+        float f0[6], f1[6];
+#pragma unroll
+        for (int iz = 0; iz < 6; ++iz) { f0[iz] = load(row0 + kk[iz]); f1[iz] = load(row1 + kk[iz]); }
+        const float2 v = weno6_call2(f0, f1, cz);
+        xv[ix] = v.x; xv[ix + 1] = v.y;
+    }
+    out = weno6_call(xv, cx);
+    return 7;
+}
+
 template <class L>
 __device__ __forceinline__ float interp_loc(int method, const L& load, const NodeField& F, const int* anc,
                                             const float* q) {
