@@ -1305,6 +1305,15 @@ int fia_debug_grid_op(fia_session* s, int op, const float* in, float* out) {
     return FIA_OK;
 }
 
+int fia_debug_learned_tc(fia_session* s, int enable, unsigned* status) {
+    if (!s || enable < -1 || enable > 1) return FIA_ERR_INVALID;
+    int r = ensure_net(s);
+    if (r != FIA_OK) return r;
+    if (enable >= 0) unet::net_set_tc(s->net, enable == 1);
+    if (status) CK(unet::net_tc_status(s->net, status, s->stream));
+    return FIA_OK;
+}
+
 int fia_debug_precondition(fia_session* s, const float* r, float* z) {
     if (!s || !s->net || !r || !z) return FIA_ERR_INVALID;
     const long long nc = (long long)s->N[0] * s->N[1] * s->N[2];

@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <random>
 
@@ -85,6 +86,7 @@ struct ConvArgs {
     int cin;              // staged channels (1: scalar input packed over taps)
     int dims[3];          // grid of the convolution (output = input grid)
     const uint2* wfrag;   // weights in fragment order
+    const uint4* wtc;     // forward weights for k_conv_tc, (tap, unit, n) x 8 channels; null: not eligible
     int out_kind;
     void* out;
     int out_cstride, out_coff, cout_real;
@@ -376,6 +378,223 @@ __global__ void __launch_bounds__(kConvThreads) k_conv2(ConvArgs a) {
 }
 
 // ---------------------------------------------------------------------------------
+// forward convolution on the 5th-generation tensor cores: tcgen05.mma (BF16 operands in
+// shared memory, FP32 accumulators in tensor memory).
+//
+// A CTA computes TXC tiles of M = 128 output voxels, each an x-plane of 16 y-lines x 8 z-voxels,
+// for all N output channels (N = 16..64).  The halo brick (TXC+2) x 18 x 10 is staged
+// unit-major: 16-byte unit u (8 channels) of halo voxel hv at (u * HVP + hv) * 16, HVP odd so
+// that the staging writes of consecutive units spread over the banks.  In this layout the A
+// operand of every tap is the canonical K-major, no-swizzle layout at a shifted start
+// address: rows m = 8 ly + lz, the 8 rows of a core matrix are one z-line (16 bytes apart),
+// the 8-row groups are the y-lines (SBO = 10 voxels = 160 bytes), the K chunks are the units
+// (LBO = HVP * 16).  The weights (B = N x K per tap, K-major) are laid out (tap, unit, n) x 16
+// bytes (SBO = 128, LBO = N * 16) and streamed in chunks of TPC taps through two shared
+// buffers by one-dimensional bulk copies (cp.async.bulk, completion counted in bytes on the
+// buffer's "full" mbarrier).  Thread 0 issues the MMAs of a chunk once its buffer is full and
+// commits them to the buffer's "empty" mbarrier, which thread 32 waits on before refilling
+// the buffer.  The epilogue reads the accumulators with tcgen05.ld (warp w: TMEM lanes
+// 32w..32w+31 = rows), applies ReLU and stores BF16 channels-last.
+//
+// Every wait is bounded; on a timeout the kernel sets bit 0 of *status, skips the epilogue
+// and still frees its tensor memory.
+// ---------------------------------------------------------------------------------
+constexpr int TCY = 16, TCZ = 8, HCY = TCY + 2, HCZ = TCZ + 2;
+constexpr int kTcThreads = 128;
+constexpr int kTcWaitLimit = 1 << 22;
+constexpr size_t kTcSmemBudget = 110 * 1024;   // two CTAs per SM
+constexpr int kTcSmemMax = 112 * 1024;
+
+__host__ __device__ __forceinline__ int tc_hvp(int txc) { return ((txc + 2) * HCY * HCZ) | 1; }
+
+__device__ __forceinline__ uint64_t umma_sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+           (1ull << 46);   // descriptor version of tcgen05; base offset 0, no swizzle
+}
+// kind::f16 instruction descriptor: FP32 accumulate, BF16 A and B, both K-major, M = 128
+__host__ __device__ __forceinline__ uint32_t umma_idesc(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+}
+__device__ __forceinline__ bool mbar_wait(uint32_t mb, uint32_t parity) {
+    for (int it = 0; it < kTcWaitLimit; ++it) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred q;\n\tmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, q;\n\t}"
+                     : "=r"(done) : "r"(mb), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+template <int TXC>
+__global__ void __launch_bounds__(kTcThreads) k_conv_tc(ConvArgs a, int n_out, int tpc, unsigned* status) {
+    extern __shared__ __align__(1024) unsigned char tsm[];
+    __shared__ __align__(8) uint64_t bar_full[2], bar_empty[2];
+    __shared__ uint32_t tmem_slot;
+    __shared__ int failed;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nu = a.cin >> 3, hvp = tc_hvp(TXC);
+    const int bz = blockIdx.x * TCZ, by = blockIdx.y * TCY, bx = blockIdx.z * TXC;
+    const uint32_t halo = (uint32_t)__cvta_generic_to_shared(tsm);
+    const uint32_t halo_bytes = ((uint32_t)(hvp * nu * 16) + 127u) & ~127u;
+    const uint32_t chunk_bytes = (uint32_t)(tpc * nu * n_out * 16);
+    const uint32_t wbuf0 = halo + halo_bytes;
+    const int nchunks = (27 + tpc - 1) / tpc;
+    uint32_t ncols = 32;
+    while (ncols < (uint32_t)(TXC * n_out)) ncols <<= 1;
+
+    if (warp == 0) {
+        const uint32_t slot = (uint32_t)__cvta_generic_to_shared(&tmem_slot);
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(ncols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        failed = 0;
+        for (int b = 0; b < 2; ++b) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&bar_full[b])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&bar_empty[b])));
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tbase = tmem_slot;
+    // weight chunk c into buffer c & 1 (one thread), completion counted on the buffer's full barrier
+    const unsigned char* wg = reinterpret_cast<const unsigned char*>(a.wtc);
+    auto issue_chunk = [&](int c) {
+        const int b = c & 1;
+        const uint32_t full = (uint32_t)__cvta_generic_to_shared(&bar_full[b]);
+        const int t0 = c * tpc, nt = min(tpc, 27 - t0);
+        const uint32_t bytes = (uint32_t)(nt * nu * n_out * 16);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full), "r"(bytes) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(wbuf0 + (uint32_t)b * chunk_bytes), "l"(wg + (size_t)t0 * nu * n_out * 16), "r"(bytes),
+                     "r"(full)
+                     : "memory");
+    };
+    // the first two chunks load while the halo is staged
+    if (tid == 32) for (int c = 0; c < min(2, nchunks); ++c) issue_chunk(c);
+    // halo: plain and upsampled BF16 by cp.async (zero fill outside the grid), the rest computed
+    const int total = ((TXC + 2) * HCY * HCZ) * nu;
+    for (int i = tid; i < total; i += kTcThreads) {
+        const int hv = i / nu, u = i - hv * nu;
+        const int hz = hv % HCZ, hy = (hv / HCZ) % HCY, hx = hv / (HCZ * HCY);
+        const int x = bx + hx - 1, y = by + hy - 1, z = bz + hz - 1;
+        const bool in = x >= 0 && y >= 0 && z >= 0 && x < a.dims[0] && y < a.dims[1] && z < a.dims[2];
+        const int c = u << 3;
+        const uint32_t off = (uint32_t)(u * hvp + hv) * 16u;
+        uint4* dptr = reinterpret_cast<uint4*>(tsm + off);
+        if (c < a.s0.C) stage_one(a.s0, x, y, z, c, in, halo + off, dptr);
+        else stage_one(a.s1, x, y, z, c - a.s0.C, in, halo + off, dptr);
+    }
+    cp_async_wait_all();
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+
+    if (tid == 32) {
+        // producer: the remaining chunks, each once the MMAs of the chunk two before are done
+        for (int c = 2; c < nchunks; ++c) {
+            if (!mbar_wait((uint32_t)__cvta_generic_to_shared(&bar_empty[c & 1]), (uint32_t)((c >> 1) - 1) & 1u)) {
+                failed = 1;
+                break;
+            }
+            issue_chunk(c);
+        }
+    } else if (tid == 0) {
+        // MMA issue
+        const uint32_t idesc = umma_idesc(n_out);
+        const uint32_t lbo_a = (uint32_t)hvp * 16u, lbo_b = (uint32_t)n_out * 16u;
+        for (int c = 0; c < nchunks; ++c) {
+            const int b = c & 1;
+            if (!mbar_wait((uint32_t)__cvta_generic_to_shared(&bar_full[b]), (uint32_t)(c >> 1) & 1u)) {
+                failed = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int t0 = c * tpc, nt = min(tpc, 27 - t0);
+            const uint32_t wb = wbuf0 + (uint32_t)b * chunk_bytes;
+            for (int tl = 0; tl < nt; ++tl) {
+                int dx, dy, dz;
+                tap_offsets(t0 + tl, dx, dy, dz);
+                for (int ks = 0; ks < (nu >> 1); ++ks) {
+                    const uint64_t bd = umma_sdesc(wb + (uint32_t)((tl * nu + 2 * ks) * n_out) * 16u, lbo_b, 128u);
+#pragma unroll
+                    for (int tx = 0; tx < TXC; ++tx) {
+                        const uint32_t hv0 = (uint32_t)(((tx + dx) * HCY + dy) * HCZ + dz);
+                        const uint64_t ad =
+                            umma_sdesc(halo + ((uint32_t)(2 * ks) * (uint32_t)hvp + hv0) * 16u, lbo_a, HCZ * 16u);
+                        const uint32_t acc = (t0 + tl > 0 || ks > 0) ? 1u : 0u;
+                        asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                                     ::"r"(tbase + (uint32_t)(tx * n_out)), "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                                     : "memory");
+                    }
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                         ::"r"((uint32_t)__cvta_generic_to_shared(&bar_empty[b]))
+                         : "memory");
+        }
+    }
+    __syncthreads();
+    // all MMAs complete: the last chunk's commit tracks every earlier MMA of thread 0; the
+    // decision is made block-wide (tcgen05.ld is warp-collective)
+    bool ok = !failed;
+    if (ok) {
+        const int cl = nchunks - 1;
+        ok = mbar_wait((uint32_t)__cvta_generic_to_shared(&bar_empty[cl & 1]), (uint32_t)(cl >> 1) & 1u);
+    }
+    ok = __syncthreads_and(ok ? 1 : 0) != 0;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!ok) {
+        if (lane == 0) atomicOr(status, 1u);
+    } else {
+        const int m = warp * 32 + lane, ly = m >> 3, lz = m & 7;
+        const int y = by + ly, z = bz + lz;
+        for (int tx = 0; tx < TXC; ++tx) {
+            const int x = bx + tx;
+            const bool st = x < a.dims[0] && y < a.dims[1] && z < a.dims[2];
+            const long long ov = st ? vox(a.dims, x, y, z) * a.out_cstride + a.out_coff : 0;
+            for (int c0 = 0; c0 < n_out; c0 += 16) {
+                uint32_t r[16];
+                const uint32_t ta = tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)(tx * n_out + c0);
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                               "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                               "=r"(r[14]), "=r"(r[15])
+                             : "r"(ta));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (st && a.out_kind == OUT_BF16) {
+                    uint32_t pk[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        float v0 = __uint_as_float(r[2 * j]), v1 = __uint_as_float(r[2 * j + 1]);
+                        if (a.relu) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
+                        pk[j] = pack_bf16(v0, v1);
+                    }
+                    uint4* dst = reinterpret_cast<uint4*>((__nv_bfloat16*)a.out + ov + c0);
+                    dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                    dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+                } else if (st) {   // FP32 output of the first cout_real channels (the last layer)
+                    float* dst = (float*)a.out + ov;
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        if (c0 + j >= a.cout_real) break;
+                        float v = __uint_as_float(r[j]);
+                        if (a.relu) v = fmaxf(v, 0.f);
+                        dst[c0 + j] = v;
+                    }
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(ncols));
+}
+
+// ---------------------------------------------------------------------------------
 // backward weights: dW[tap][ci][co] += sum_v x[v + off(tap)][ci] g[v][co]
 // ---------------------------------------------------------------------------------
 template <int COUT>
@@ -512,6 +731,21 @@ __global__ void k_pack(const float* __restrict__ W, int cin, int cout, int trans
         r.x = pack_bf16(wv(2 * q), wv(2 * q + 1));
         r.y = pack_bf16(wv(2 * q + 8), wv(2 * q + 9));
         frag[e] = r;
+    }
+}
+
+// forward weights for k_conv_tc: unit (tap, u, n) = W[tap][8u .. 8u+7][n] as BF16, n < nout
+// (columns n >= cout are zero)
+__global__ void k_pack_tc(const float* __restrict__ W, int cin, int cout, int nout, uint4* __restrict__ out) {
+    const int nu = cin / 8;
+    const int total = 27 * nu * nout;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        const int n = e % nout, u = (e / nout) % nu, tap = e / (nout * nu);
+        if (n >= cout) { out[e] = make_uint4(0, 0, 0, 0); continue; }
+        const float* w = W + ((size_t)tap * cin + 8 * u) * cout + n;
+        out[e] = make_uint4(pack_bf16(w[0], w[(size_t)cout]), pack_bf16(w[2 * (size_t)cout], w[3 * (size_t)cout]),
+                            pack_bf16(w[4 * (size_t)cout], w[5 * (size_t)cout]),
+                            pack_bf16(w[6 * (size_t)cout], w[7 * (size_t)cout]));
     }
 }
 
@@ -825,6 +1059,10 @@ struct Net {
     float *w, *gw, *m, *v;
     uint2* wf[kLayers];
     uint2* wb[kLayers];
+    uint4* wt[kLayers];   // k_conv_tc weights (layers with cin, cout multiples of 16)
+    unsigned* tc_status;  // bit 0: a k_conv_tc wait ran out
+    bool use_tc;
+    size_t tc_budget;     // shared memory per k_conv_tc CTA
     void* act[kTensors];
     float* grad[kTensors];
     float* temp;       // backward data output of concat / pool inputs
@@ -886,6 +1124,52 @@ cudaError_t launch_conv2_t(ConvArgs a, int nsplit, cudaStream_t s) {
     const dim3 grid(((a.dims[2] + 15) / 16) * nsplit, (a.dims[1] + 3) / 4, (a.dims[0] + MT - 1) / MT);
     k_conv2<NTL, MT, TAP><<<grid, kConvThreads, sm, s>>>(a);
     return cudaGetLastError();
+}
+
+template <int TXC>
+cudaError_t launch_conv_tc_t(const ConvArgs& a, int n_out, int tpc, size_t smem, unsigned* status, cudaStream_t s) {
+    static bool attr = false;
+    if (!attr) {
+        UCK(cudaFuncSetAttribute(k_conv_tc<TXC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemMax));
+        attr = true;
+    }
+    const dim3 grid((a.dims[2] + TCZ - 1) / TCZ, (a.dims[1] + TCY - 1) / TCY, (a.dims[0] + TXC - 1) / TXC);
+    k_conv_tc<TXC><<<grid, kTcThreads, smem, s>>>(a, n_out, tpc, status);
+    return cudaGetLastError();
+}
+
+size_t conv_tc_smem(int txc, int cin, int n_out, int tpc) {
+    const size_t halo = ((size_t)tc_hvp(txc) * (cin / 8) * 16 + 127) & ~(size_t)127;
+    const int nbuf = (27 + tpc - 1) / tpc > 1 ? 2 : 1;
+    return halo + (size_t)nbuf * tpc * (cin / 8) * n_out * 16;
+}
+
+// The tensor-core path when the layer qualifies (cin a multiple of 16; BF16 output with cout a
+// multiple of 16 up to 64, or the single FP32 output channel of the last layer, computed as 16
+// with zero weights) and its tiles make at least one wave.  Configurations, best first: all
+// 27 taps in one or two weight chunks (no refill wait, both loads overlap the halo staging),
+// two x-planes per CTA before one; then 9-, 3- and 1-tap chunks; each within 110 KB of shared
+// memory (two CTAs per SM).  Returns false (nothing launched) otherwise.
+int tc_nout(int cout) { return cout == 1 ? 16 : cout; }
+
+bool try_conv_tc(const ConvArgs& a, int cout, size_t budget, unsigned* status, cudaStream_t s, cudaError_t* err) {
+    if (!a.wtc || a.cin % 16 || cout != a.cout_real) return false;
+    const bool f32_single = a.out_kind == OUT_F32 && cout == 1;
+    if (!f32_single && (a.out_kind != OUT_BF16 || cout % 16 || cout > 64)) return false;
+    const int n_out = tc_nout(cout);
+    const long long tiles1 = (long long)((a.dims[2] + TCZ - 1) / TCZ) * ((a.dims[1] + TCY - 1) / TCY) * a.dims[0];
+    if (tiles1 < 152) return false;
+    static const int order[][2] = {{2, 27}, {2, 14}, {1, 27}, {1, 14}, {2, 9}, {1, 9}, {2, 3}, {1, 3}, {2, 1}, {1, 1}};
+    for (const auto& o : order) {
+        const int txc = o[0], tpc = o[1];
+        if (txc == 2 && tiles1 / 2 < 2 * 152) continue;
+        const size_t sm = conv_tc_smem(txc, a.cin, n_out, tpc);
+        if (sm > budget) continue;
+        *err = txc == 2 ? launch_conv_tc_t<2>(a, n_out, tpc, sm, status, s)
+                        : launch_conv_tc_t<1>(a, n_out, tpc, sm, status, s);
+        return true;
+    }
+    return false;
 }
 
 // Chooses the brick (MT) and the n-tile split for a convolution with cout_padded output
@@ -980,7 +1264,10 @@ cudaError_t forward(Net* n, cudaStream_t s) {
         a.cout_real = d.shape.cout;
         if (d.out == T_Y) { a.out_kind = OUT_F32; a.out = n->act[T_Y]; a.out_cstride = 1; a.out_coff = 0; }
         else { a.out_kind = OUT_BF16; a.out = n->act[d.out]; a.out_cstride = d.shape.cout; a.out_coff = 0; }
-        UCK(launch_conv(a, std::max(8, d.shape.cout), s));
+        a.wtc = n->use_tc ? n->wt[l] : nullptr;
+        cudaError_t e = cudaSuccess;
+        if (try_conv_tc(a, d.shape.cout, n->tc_budget, n->tc_status, s, &e)) UCK(e);
+        else UCK(launch_conv(a, std::max(8, d.shape.cout), s));
         ++n->launches;
     }
     return cudaSuccess;
@@ -1004,6 +1291,7 @@ cudaError_t backward(Net* n, cudaStream_t s) {
         }
         ConvArgs a;
         layer_sources(n, l, a);
+        a.wtc = nullptr;
         UCK(launch_wgrad(a, gs, d.shape.cout, n->gw + layer_offset(l), s));
         if (l == 0) break;
         // backward data: conv of gs with the flipped/transposed weights
@@ -1049,6 +1337,9 @@ cudaError_t pack_all(Net* n, cudaStream_t s) {
         k_pack<<<grid_for((long long)frag_count(sh.cin, sh.cout, false)), 256, 0, s>>>(W, sh.cin, sh.cout, 0, n->wf[l]);
         if (l > 0)
             k_pack<<<grid_for((long long)frag_count(sh.cin, sh.cout, true)), 256, 0, s>>>(W, sh.cin, sh.cout, 1, n->wb[l]);
+        if (n->wt[l])
+            k_pack_tc<<<grid_for(27LL * (sh.cin / 8) * tc_nout(sh.cout)), 256, 0, s>>>(W, sh.cin, sh.cout,
+                                                                                    tc_nout(sh.cout), n->wt[l]);
     }
     return cudaGetLastError();
 }
@@ -1073,6 +1364,16 @@ Net* net_create(int nx, int ny, int nz, cudaStream_t s) {
         const LayerShape& sh = kDefs[l].shape;
         n->wf[l] = (uint2*)A(frag_count(sh.cin, sh.cout, false) * sizeof(uint2));
         n->wb[l] = l > 0 ? (uint2*)A(frag_count(sh.cin, sh.cout, true) * sizeof(uint2)) : nullptr;
+        const bool tc = sh.cin % 16 == 0 && ((sh.cout % 16 == 0 && sh.cout <= 64) || sh.cout == 1);
+        n->wt[l] = tc ? (uint4*)A(27LL * (sh.cin / 8) * tc_nout(sh.cout) * sizeof(uint4)) : nullptr;
+    }
+    n->tc_status = (unsigned*)A(sizeof(unsigned));
+    n->use_tc = true;
+    // FIA_TC_SMEM_KB overrides the shared memory per tensor-core convolution CTA (tuning)
+    n->tc_budget = kTcSmemBudget;
+    if (const char* e = std::getenv("FIA_TC_SMEM_KB")) {
+        const long kb = std::strtol(e, nullptr, 10);
+        if (kb >= 16 && kb * 1024 <= kTcSmemMax) n->tc_budget = (size_t)kb * 1024;
     }
     size_t tmax = 0;
     for (int t = 0; t < kTensors; ++t) {
@@ -1223,6 +1524,13 @@ int net_add_pair(Net* n, const PoissonGrid& g, const float* r_dev, const float* 
 }
 
 int net_num_pairs(const Net* n) { return (int)n->pairs.size(); }
+
+void net_set_tc(Net* n, bool on) { n->use_tc = on; }
+
+cudaError_t net_tc_status(Net* n, unsigned* out, cudaStream_t s) {
+    UCK(cudaMemcpyAsync(out, n->tc_status, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    return cudaStreamSynchronize(s);
+}
 
 cudaError_t net_loss(Net* n, const PoissonGrid& g0, int pair, bool backward_pass, double* loss, cudaStream_t s) {
     if (pair < 0 || pair >= (int)n->pairs.size()) return cudaErrorInvalidValue;

@@ -75,6 +75,9 @@ cudaError_t net_forward_level0(Net* n, const float* x0, float* y, cudaStream_t s
 cudaError_t net_backward_level0(Net* n, const float* gy, cudaStream_t s);
 void net_level_dims(const Net* n, int level, int dims[3]);
 int net_launches(const Net* n);   // kernels launched by the last net_apply
+// the tcgen05 convolution path (on by default) and its error bits (bit 0: a wait ran out)
+void net_set_tc(Net* n, bool on);
+cudaError_t net_tc_status(Net* n, unsigned* out, cudaStream_t s);
 
 }  // namespace unet
 }  // namespace fia

@@ -177,6 +177,7 @@ def _declare(lib):
     lib.fia_debug_unet_forward.argtypes = [vp, fp, fp]
     lib.fia_debug_unet_backward.argtypes = [vp, fp, fp, fp]
     lib.fia_debug_precondition.argtypes = [vp, fp, fp]
+    lib.fia_debug_learned_tc.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_uint)]
     lib.fia_debug_learned_grad.argtypes = [vp, ip, fp, dp]
     lib.fia_debug_grid_op.argtypes = [vp, ip, fp, fp]
     lib.fia_debug_solve_rhs.argtypes = [vp, fp, fp, ctypes.POINTER(SolverParams), ctypes.POINTER(SolverReport)]
@@ -456,6 +457,13 @@ class Grid3D:
         loss = ctypes.c_double(0)
         _check(self.lib.fia_debug_learned_grad(self.s, pair, _fp(out), ctypes.byref(loss)), "fia_debug_learned_grad")
         return out, loss.value
+
+    def debug_learned_tc(self, enable=-1):
+        """switch the network's tcgen05 convolution path (1 on, 0 off, -1 leave); returns its
+        error bits"""
+        st = ctypes.c_uint(0)
+        _check(self.lib.fia_debug_learned_tc(self.s, enable, ctypes.byref(st)), "fia_debug_learned_tc")
+        return st.value
 
     def debug_precondition(self, r):
         a = np.ascontiguousarray(r, dtype=np.float32).ravel()

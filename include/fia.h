@@ -266,6 +266,10 @@ int fia_debug_set_piece_capacity(fia_session* s, long long pieces);
 long long fia_debug_piece_capacity(fia_session* s);
 /* gradient of the energy-norm loss of pair i with respect to all parameters (no update) */
 int fia_debug_learned_grad(fia_session* s, int pair, float* grads, double* loss);
+/* the network's tensor-core (tcgen05) convolution path: enable 1 / 0 switches it on / off
+ * (on by default; off runs every layer on the mma.sync kernel), -1 leaves it; *status (if
+ * not null) receives the path's error bits (bit 0: a bounded wait ran out) */
+int fia_debug_learned_tc(fia_session* s, int enable, unsigned* status);
 
 /* Test hooks: single pieces of the path on host data (FP64 buffers), mirroring the oracle. */
 /* one flux pass of a node field (comp -1 density, 0..2 velocity) with the session velocity */

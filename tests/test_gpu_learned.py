@@ -47,6 +47,26 @@ def test_unet_forward_matches_oracle():
     assert rel(y, yo) < 5e-3
 
 
+@pytest.mark.parametrize("fine", [(160, 144, 136), (320, 256, 128)])
+def test_tensor_core_convolutions_match_mma_path(fine):
+    """The tcgen05 convolutions against the mma.sync kernel (checked against the oracle above)
+    on the same weights and input.  The two sizes cover one and two x-planes per CTA, weight
+    chunks of 27, 14, 9, 3 and 1 taps, plain, pooled and upsampled-concatenated inputs, 16 to 48
+    output channels and the single FP32 output channel, and ragged tiles in y and z."""
+    g = fia.Grid3D(*fine, 1.0 / fine[0], precision=fia.FIA_FP32C)
+    g.learned_init(5)
+    dims = tuple(g.learned_level_dims(0))
+    x0 = np.random.default_rng(4).normal(size=dims).astype(np.float32)
+    assert g.debug_learned_tc(1) == 0
+    y_tc = g.debug_unet_forward(x0)
+    st = g.debug_learned_tc(0)
+    y_ref = g.debug_unet_forward(x0)
+    g.close()
+    assert st == 0
+    assert np.all(np.isfinite(y_tc))
+    assert rel(y_tc, y_ref) < 1e-2
+
+
 def test_unet_gradients_match_oracle():
     g = session(seed=11)
     w = g.learned_get_weights().astype(np.float64)
