@@ -405,7 +405,7 @@ constexpr int kTcWaitLimit = 1 << 22;
 constexpr size_t kTcSmemBudget = 110 * 1024;   // two CTAs per SM
 constexpr int kTcSmemMax = 112 * 1024;
 
-__host__ __device__ __forceinline__ int tc_hvp(int txc) { return ((txc + 2) * HCY * HCZ) | 1; }
+__host__ __device__ constexpr int tc_hvp(int txc) { return ((txc + 2) * HCY * HCZ) | 1; }
 
 __device__ __forceinline__ uint64_t umma_sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
     return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
@@ -426,14 +426,14 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mb, uint32_t parity) {
     return false;
 }
 
-template <int TXC>
+template <int TXC, int NU>
 __global__ void __launch_bounds__(kTcThreads) k_conv_tc(ConvArgs a, int n_out, int tpc, unsigned* status) {
     extern __shared__ __align__(1024) unsigned char tsm[];
     __shared__ __align__(8) uint64_t bar_full[2], bar_empty[2];
     __shared__ uint32_t tmem_slot;
     __shared__ int failed;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int nu = a.cin >> 3, hvp = tc_hvp(TXC);
+    constexpr int nu = NU, hvp = tc_hvp(TXC);   // NU = cin / 8
     const int bz = blockIdx.x * TCZ, by = blockIdx.y * TCY, bx = blockIdx.z * TXC;
     const uint32_t halo = (uint32_t)__cvta_generic_to_shared(tsm);
     const uint32_t halo_bytes = ((uint32_t)(hvp * nu * 16) + 127u) & ~127u;
@@ -502,9 +502,11 @@ __global__ void __launch_bounds__(kTcThreads) k_conv_tc(ConvArgs a, int n_out, i
             issue_chunk(c);
         }
     } else if (tid == 0) {
-        // MMA issue
+        // MMA issue.  The descriptors of the halo and of each weight buffer are built once; an
+        // operand at a later address adds its offset in 16-byte units to the start-address
+        // field (shared addresses stay below 256 KB, so the 14-bit field does not overflow).
         const uint32_t idesc = umma_idesc(n_out);
-        const uint32_t lbo_a = (uint32_t)hvp * 16u, lbo_b = (uint32_t)n_out * 16u;
+        const uint64_t adesc0 = umma_sdesc(halo, (uint32_t)hvp * 16u, HCZ * 16u);
         for (int c = 0; c < nchunks; ++c) {
             const int b = c & 1;
             if (!mbar_wait((uint32_t)__cvta_generic_to_shared(&bar_full[b]), (uint32_t)(c >> 1) & 1u)) {
@@ -513,18 +515,18 @@ __global__ void __launch_bounds__(kTcThreads) k_conv_tc(ConvArgs a, int n_out, i
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const int t0 = c * tpc, nt = min(tpc, 27 - t0);
-            const uint32_t wb = wbuf0 + (uint32_t)b * chunk_bytes;
+            const uint64_t bdesc0 = umma_sdesc(wbuf0 + (uint32_t)b * chunk_bytes, (uint32_t)n_out * 16u, 128u);
             for (int tl = 0; tl < nt; ++tl) {
-                int dx, dy, dz;
-                tap_offsets(t0 + tl, dx, dy, dz);
-                for (int ks = 0; ks < (nu >> 1); ++ks) {
-                    const uint64_t bd = umma_sdesc(wb + (uint32_t)((tl * nu + 2 * ks) * n_out) * 16u, lbo_b, 128u);
+                const int tap = t0 + tl;
+                const int dx = tap / 9, dy = (tap / 3) % 3, dz = tap % 3;
+                const uint32_t hvt = (uint32_t)((dx * HCY + dy) * HCZ + dz);
+#pragma unroll
+                for (int ks = 0; ks < NU / 2; ++ks) {
+                    const uint64_t bd = bdesc0 + (uint64_t)((tl * NU + 2 * ks) * n_out);
+                    const uint32_t acc = (tap > 0 || ks > 0) ? 1u : 0u;
 #pragma unroll
                     for (int tx = 0; tx < TXC; ++tx) {
-                        const uint32_t hv0 = (uint32_t)(((tx + dx) * HCY + dy) * HCZ + dz);
-                        const uint64_t ad =
-                            umma_sdesc(halo + ((uint32_t)(2 * ks) * (uint32_t)hvp + hv0) * 16u, lbo_a, HCZ * 16u);
-                        const uint32_t acc = (t0 + tl > 0 || ks > 0) ? 1u : 0u;
+                        const uint64_t ad = adesc0 + (uint64_t)(2 * ks * hvp + hvt + tx * HCY * HCZ);
                         asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
                                      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
                                      ::"r"(tbase + (uint32_t)(tx * n_out)), "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
@@ -1126,16 +1128,29 @@ cudaError_t launch_conv2_t(ConvArgs a, int nsplit, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-template <int TXC>
+template <int TXC, int NU>
 cudaError_t launch_conv_tc_t(const ConvArgs& a, int n_out, int tpc, size_t smem, unsigned* status, cudaStream_t s) {
     static bool attr = false;
     if (!attr) {
-        UCK(cudaFuncSetAttribute(k_conv_tc<TXC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemMax));
+        UCK(cudaFuncSetAttribute(k_conv_tc<TXC, NU>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemMax));
         attr = true;
     }
     const dim3 grid((a.dims[2] + TCZ - 1) / TCZ, (a.dims[1] + TCY - 1) / TCY, (a.dims[0] + TXC - 1) / TXC);
-    k_conv_tc<TXC><<<grid, kTcThreads, smem, s>>>(a, n_out, tpc, status);
+    k_conv_tc<TXC, NU><<<grid, kTcThreads, smem, s>>>(a, n_out, tpc, status);
     return cudaGetLastError();
+}
+
+template <int TXC>
+cudaError_t launch_conv_tc_nu(const ConvArgs& a, int n_out, int tpc, size_t smem, unsigned* status, cudaStream_t s) {
+    switch (a.cin / 8) {
+        case 2: return launch_conv_tc_t<TXC, 2>(a, n_out, tpc, smem, status, s);
+        case 4: return launch_conv_tc_t<TXC, 4>(a, n_out, tpc, smem, status, s);
+        case 6: return launch_conv_tc_t<TXC, 6>(a, n_out, tpc, smem, status, s);
+        case 8: return launch_conv_tc_t<TXC, 8>(a, n_out, tpc, smem, status, s);
+        case 10: return launch_conv_tc_t<TXC, 10>(a, n_out, tpc, smem, status, s);
+        case 14: return launch_conv_tc_t<TXC, 14>(a, n_out, tpc, smem, status, s);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 size_t conv_tc_smem(int txc, int cin, int n_out, int tpc) {
@@ -1165,8 +1180,8 @@ bool try_conv_tc(const ConvArgs& a, int cout, size_t budget, unsigned* status, c
         if (txc == 2 && tiles1 / 2 < 2 * 152) continue;
         const size_t sm = conv_tc_smem(txc, a.cin, n_out, tpc);
         if (sm > budget) continue;
-        *err = txc == 2 ? launch_conv_tc_t<2>(a, n_out, tpc, sm, status, s)
-                        : launch_conv_tc_t<1>(a, n_out, tpc, sm, status, s);
+        *err = txc == 2 ? launch_conv_tc_nu<2>(a, n_out, tpc, sm, status, s)
+                        : launch_conv_tc_nu<1>(a, n_out, tpc, sm, status, s);
         return true;
     }
     return false;
