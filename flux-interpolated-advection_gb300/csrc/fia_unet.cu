@@ -393,14 +393,15 @@ __global__ void __launch_bounds__(kConvThreads) k_conv2(ConvArgs a) {
 // buffers by one-dimensional bulk copies (cp.async.bulk, completion counted in bytes on the
 // buffer's "full" mbarrier).  Thread 0 issues the MMAs of a chunk once its buffer is full and
 // commits them to the buffer's "empty" mbarrier, which thread 32 waits on before refilling
-// the buffer.  The epilogue reads the accumulators with tcgen05.ld (warp w: TMEM lanes
-// 32w..32w+31 = rows), applies ReLU and stores BF16 channels-last.
+// the buffer.  The CTA has 256 or 512 threads (8 or 16 warps, for the halo staging); the
+// epilogue reads the accumulators with tcgen05.ld (warps w, w + 4, ...: TMEM lanes 32 (w mod 4)
+// .. + 31 = rows, splitting the 16-column blocks), applies ReLU and stores BF16 channels-last.
 //
 // Every wait is bounded; on a timeout the kernel sets bit 0 of *status, skips the epilogue
 // and still frees its tensor memory.
 // ---------------------------------------------------------------------------------
 constexpr int TCY = 16, TCZ = 8, HCY = TCY + 2, HCZ = TCZ + 2;
-constexpr int kTcThreads = 128;
+constexpr int kTcThreadsMax = 512;
 constexpr int kTcWaitLimit = 1 << 22;
 constexpr size_t kTcSmemBudget = 110 * 1024;   // two CTAs per SM
 constexpr int kTcSmemMax = 112 * 1024;
@@ -426,8 +427,8 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mb, uint32_t parity) {
     return false;
 }
 
-template <int TXC, int NU>
-__global__ void __launch_bounds__(kTcThreads) k_conv_tc(ConvArgs a, int n_out, int tpc, unsigned* status) {
+template <int TXC, int NU, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_conv_tc(ConvArgs a, int n_out, int tpc, unsigned* status) {
     extern __shared__ __align__(1024) unsigned char tsm[];
     __shared__ __align__(8) uint64_t bar_full[2], bar_empty[2];
     __shared__ uint32_t tmem_slot;
@@ -477,7 +478,7 @@ __global__ void __launch_bounds__(kTcThreads) k_conv_tc(ConvArgs a, int n_out, i
     if (tid == 32) for (int c = 0; c < min(2, nchunks); ++c) issue_chunk(c);
     // halo: plain and upsampled BF16 by cp.async (zero fill outside the grid), the rest computed
     const int total = ((TXC + 2) * HCY * HCZ) * nu;
-    for (int i = tid; i < total; i += kTcThreads) {
+    for (int i = tid; i < total; i += THREADS) {
         const int hv = i / nu, u = i - hv * nu;
         const int hz = hv % HCZ, hy = (hv / HCZ) % HCY, hx = hv / (HCZ * HCY);
         const int x = bx + hx - 1, y = by + hy - 1, z = bz + hz - 1;
@@ -552,15 +553,19 @@ __global__ void __launch_bounds__(kTcThreads) k_conv_tc(ConvArgs a, int n_out, i
     if (!ok) {
         if (lane == 0) atomicOr(status, 1u);
     } else {
-        const int m = warp * 32 + lane, ly = m >> 3, lz = m & 7;
+        // warp w reads TMEM lanes 32 (w mod 4) ..; the warp groups split the 16-column blocks
+        const int q4 = warp & 3, grp = warp >> 2;
+        const int m = q4 * 32 + lane, ly = m >> 3, lz = m & 7;
         const int y = by + ly, z = bz + lz;
-        for (int tx = 0; tx < TXC; ++tx) {
+        const int nblk = n_out >> 4;
+        for (int item = grp; item < TXC * nblk; item += THREADS / 128) {
+            const int tx = item / nblk, c0 = (item - tx * nblk) * 16;
             const int x = bx + tx;
             const bool st = x < a.dims[0] && y < a.dims[1] && z < a.dims[2];
             const long long ov = st ? vox(a.dims, x, y, z) * a.out_cstride + a.out_coff : 0;
-            for (int c0 = 0; c0 < n_out; c0 += 16) {
+            {
                 uint32_t r[16];
-                const uint32_t ta = tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)(tx * n_out + c0);
+                const uint32_t ta = tbase + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(tx * n_out + c0);
                 asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
                              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
                                "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
@@ -1128,16 +1133,25 @@ cudaError_t launch_conv2_t(ConvArgs a, int nsplit, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-template <int TXC, int NU>
-cudaError_t launch_conv_tc_t(const ConvArgs& a, int n_out, int tpc, size_t smem, unsigned* status, cudaStream_t s) {
+template <int TXC, int NU, int THREADS>
+cudaError_t launch_conv_tc_k(const ConvArgs& a, int n_out, int tpc, size_t smem, unsigned* status, cudaStream_t s) {
     static bool attr = false;
     if (!attr) {
-        UCK(cudaFuncSetAttribute(k_conv_tc<TXC, NU>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemMax));
+        UCK(cudaFuncSetAttribute(k_conv_tc<TXC, NU, THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemMax));
         attr = true;
     }
     const dim3 grid((a.dims[2] + TCZ - 1) / TCZ, (a.dims[1] + TCY - 1) / TCY, (a.dims[0] + TXC - 1) / TXC);
-    k_conv_tc<TXC, NU><<<grid, kTcThreads, smem, s>>>(a, n_out, tpc, status);
+    k_conv_tc<TXC, NU, THREADS><<<grid, THREADS, smem, s>>>(a, n_out, tpc, status);
     return cudaGetLastError();
+}
+
+// 256 threads where the CTA is small enough for many CTAs per SM, else 512 (measured at
+// 256^3: the 16 -> 16 layers 92 us with 256 threads, 130 with 512; the 48 -> 16 layer 379 us
+// with 256, 352 with 512)
+template <int TXC, int NU>
+cudaError_t launch_conv_tc_t(const ConvArgs& a, int n_out, int tpc, size_t smem, unsigned* status, cudaStream_t s) {
+    if (smem <= 40 * 1024) return launch_conv_tc_k<TXC, NU, 256>(a, n_out, tpc, smem, status, s);
+    return launch_conv_tc_k<TXC, NU, kTcThreadsMax>(a, n_out, tpc, smem, status, s);
 }
 
 template <int TXC>
