@@ -332,7 +332,7 @@ int pressure_fcg(fia_session* s, const fia_solver_params* sp, PressureReport& r,
         CK(unet::net_apply(s->net, g, W.r, W.z, W.scal + kScalRR, (double)s->n_free, s->stream));
         CK(cudaEventRecord(s->pev[1], s->stream));
         CK(fcg_iteration<T>(W, g, s->fcg, it, kFcgMaxDirs, s->stream));
-        s->launches += (unsigned long long)unet::net_launches(s->net) + 3;
+        s->launches += (unsigned long long)unet::net_launches(s->net) + 4;
         CK(solver_state(W.scal, st, s->stream));
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, s->pev[0], s->pev[1]));

@@ -542,6 +542,35 @@ __global__ void __launch_bounds__(kRedThreads) k_fcgm_dots(unsigned n, double* _
     }
 }
 
+// d_new = z + sum_j beta_j d_j (streamed once; the stencil kernel below then reads d_new
+// instead of recomputing it for each neighbour)
+template <typename T, int W>
+__global__ void __launch_bounds__(kRedThreads) k_fcgm_combine(unsigned n, const double* __restrict__ scal,
+                                                               const T* __restrict__ z, DirSet<T> ds,
+                                                               T* __restrict__ dnew) {
+    if (scal[S_DONE] != 0.0) return;
+    const unsigned ngr = n / W;
+    T beta[kFcgMaxDirs];
+#pragma unroll
+    for (int j = 0; j < kFcgMaxDirs; ++j) beta[j] = j < ds.n ? (T)scal[S_BETAJ + ds.slot[j]] : T(0);
+    for (unsigned gi = blockIdx.x * blockDim.x + threadIdx.x; gi < ngr; gi += gridDim.x * blockDim.x) {
+        const unsigned c0 = gi * W;
+        T o[W];
+        ldv<T, W>(z + c0, o);
+#pragma unroll
+        for (int j = 0; j < kFcgMaxDirs; ++j) {
+            if (j >= ds.n) break;
+            T b[W];
+            ldv<T, W>(ds.v[j] + c0, b);
+#pragma unroll
+            for (int e = 0; e < W; ++e) o[e] += beta[j] * b[e];
+        }
+        stv<T, W>(dnew + c0, o);
+    }
+}
+
+// q = B d for d = z + sum_j beta_j d_j (with ds.n = 0 and dnew null: d = z, already combined);
+// d.q and d.r; the last block sets alpha = d.r / d.q
 template <typename T, int W>
 __global__ void __launch_bounds__(kRedThreads) k_fcgm_direction(PoissonGrid g, double* __restrict__ scal,
                                                                  const T* __restrict__ z, DirSet<T> ds,
@@ -615,7 +644,7 @@ __global__ void __launch_bounds__(kRedThreads) k_fcgm_direction(PoissonGrid g, d
             acc[0].add(dc[e], qv[e]);
             acc[1].add(dc[e], rv[e]);
         }
-        stv<T, W>(dnew + c0, dc);
+        if (dnew) stv<T, W>(dnew + c0, dc);
         stv<T, W>(qnew + c0, qv);
     }
     block_dots<T, 2>(acc, part);
@@ -811,14 +840,18 @@ cudaError_t fcg_iteration(const PressureWork<T>& W, const PoissonGrid& g, const 
         ds.v[j] = B.d[sl]; ds.slot[j] = sl;
     }
     constexpr int V = VecW<T>::W;
+    DirSet<T> none = ds;
+    none.n = 0;
     if (g.nz % V == 0) {
         k_fcgm_dots<T, V><<<nb, nt, 0, s>>>(n, W.scal, W.z, W.r, qs, W.part, W.ticket);
-        k_fcgm_direction<T, V><<<nb, nt, 0, s>>>(g, W.scal, W.z, ds, B.d[newslot], B.q[newslot], newslot, W.r,
-                                                 W.part + (kFcgMaxDirs + 1) * nb, W.ticket + 1);
+        k_fcgm_combine<T, V><<<nb, nt, 0, s>>>(n, W.scal, W.z, ds, B.d[newslot]);
+        k_fcgm_direction<T, V><<<nb, nt, 0, s>>>(g, W.scal, B.d[newslot], none, (T*)nullptr, B.q[newslot], newslot,
+                                                 W.r, W.part + (kFcgMaxDirs + 1) * nb, W.ticket + 1);
     } else {
         k_fcgm_dots<T, 1><<<nb, nt, 0, s>>>(n, W.scal, W.z, W.r, qs, W.part, W.ticket);
-        k_fcgm_direction<T, 1><<<nb, nt, 0, s>>>(g, W.scal, W.z, ds, B.d[newslot], B.q[newslot], newslot, W.r,
-                                                 W.part + (kFcgMaxDirs + 1) * nb, W.ticket + 1);
+        k_fcgm_combine<T, 1><<<nb, nt, 0, s>>>(n, W.scal, W.z, ds, B.d[newslot]);
+        k_fcgm_direction<T, 1><<<nb, nt, 0, s>>>(g, W.scal, B.d[newslot], none, (T*)nullptr, B.q[newslot], newslot,
+                                                 W.r, W.part + (kFcgMaxDirs + 1) * nb, W.ticket + 1);
     }
     launch_update<T>(W, g, B.d[newslot], false, W.part, W.ticket + 2, s, B.q[newslot]);
     return cudaGetLastError();
