@@ -483,6 +483,7 @@ struct PassParams {
     int k;               // Gauss points per half cell
     real minimal_area;
     real dt;
+    int maccormack = 0;  // flux MacCormack: faces at rest (0.5), backtraced (1), traced back (-0.5)
 };
 
 struct Velocity { Field u, v, w; };
@@ -517,6 +518,36 @@ static void backtrace_vertex(const Grid& G, const Velocity& vel, const PassParam
     }
 }
 
+// Second trace of the flux MacCormack scheme (calc_backtraced_face_3D.cpp:9-128 with
+// time_direction "backward"): from the backtraced position x1, x2 = x1 + dt u(x1) with the
+// velocity interpolated at x1, the same pin rule (by the vertex's lattice index), then clamped
+// (clamp_vertex_position_by_grid_3D, :131-160).
+static void forward_trace_vertex(const Grid& G, const Velocity& vel, const PassParams& P, const int* vidx,
+                                 const real* x1, real* pos) {
+    const real h = G.h;
+    for (int d = 0; d < 3; ++d) pos[d] = x1[d];
+    if (P.zero_velocity) return;
+    bool pinned = false;
+    if (P.comp >= 0) {
+        int c = P.comp;
+        if (vidx[c] <= 1 || vidx[c] >= G.N[c]) pinned = true;
+    }
+    real u[3];
+    u[0] = interp(P.interp, vel.u, x1, h);
+    u[1] = interp(P.interp, vel.v, x1, h);
+    u[2] = interp(P.interp, vel.w, x1, h);
+    if (!pinned) {
+        for (int d = 0; d < 3; ++d) pos[d] += u[d] * P.dt;
+    }
+    for (int d = 0; d < 3; ++d) {
+        int e = (d == P.comp);
+        real lo = 0.0 - e * 0.5 * h;
+        real hi = 0.0 + h * G.N[d] + e * 0.5 * h;
+        if (pos[d] < lo) pos[d] = lo;
+        if (pos[d] > hi) pos[d] = hi;
+    }
+}
+
 struct PassCounters { long faces = 0; long polys = 0; int status = 0; };
 
 // One flux pass over the cells [c0, c1) of the advected field A (node field of the
@@ -536,11 +567,22 @@ static void pass_range(const Grid& G, const Velocity& vel, const Field& A, const
         int ix = (int)(cell / ((long)M[2] * M[1]));
         real acc = 0.0;
         for (int f = 0; f < 6; ++f) {
-            real v[4][3];
+            real vb[4][3], v0[4][3], v2[4][3];
             for (int q = 0; q < 4; ++q) {
                 int vi[3] = {ix + kFaceVerts[f][q][0], iy + kFaceVerts[f][q][1], iz + kFaceVerts[f][q][2]};
-                backtrace_vertex(G, vel, P, vi, v[q]);
+                backtrace_vertex(G, vel, P, vi, vb[q]);
+                if (P.maccormack) {
+                    // the face before the backtrace (backtrace_..._for_integrate_density.cpp:139-144)
+                    for (int d = 0; d < 3; ++d) v0[q][d] = vi[d] * h - ((d == P.comp) ? 1 * 0.5 * h : 0.0);
+                    forward_trace_vertex(G, vel, P, vi, vb[q], v2[q]);
+                }
             }
+            // the flux MacCormack branch adds the quadrature of three faces with weights 0.5, 1
+            // and -0.5 (backtrace_..._for_integrate_density.cpp:146-234); otherwise one face
+            const int nstage = P.maccormack ? 3 : 1;
+            for (int stage = 0; stage < nstage; ++stage) {
+            const real (*v)[3] = !P.maccormack ? vb : (stage == 0 ? v0 : (stage == 1 ? vb : v2));
+            const real wgt = !P.maccormack ? 1.0 : (stage == 0 ? 0.5 : (stage == 1 ? 1.0 : -0.5));
             polys.clear();
             cnt.status |= split_face(v, h, P.color_off, P.minimal_area, polys);
             cnt.faces++;
@@ -556,29 +598,30 @@ static void pass_range(const Grid& G, const Velocity& vel, const Field& A, const
                         real a = iy0 * h + origin[1], b = sp.pos[1];
                         for (int t = 0; t < g.k; ++t) {
                             q[1] = gauss_pos(g, t, a, b);
-                            real wy = sp.n[1] * f01 * h * g.w[t];
+                            real wy = sp.n[1] * f01 * h * g.w[t] * wgt;
                             acc += interp(P.interp, A, q, h) * wy / V;
                         }
                     } else {
                         real a = iy0 * h + origin[1], b = (iy0 + 0.5) * h + origin[1];
                         for (int t = 0; t < g.k; ++t) {
                             q[1] = gauss_pos(g, t, a, b);
-                            real wy = sp.n[1] * 0.5 * h * g.w[t];
+                            real wy = sp.n[1] * 0.5 * h * g.w[t] * wgt;
                             acc += interp(P.interp, A, q, h) * wy / V;
                         }
                         a = (iy0 + 0.5) * h + origin[1]; b = (iy0 + f01) * h + origin[1];
                         for (int t = 0; t < g.k; ++t) {
                             q[1] = gauss_pos(g, t, a, b);
-                            real wy = sp.n[1] * (f01 - 0.5) * h * g.w[t];
+                            real wy = sp.n[1] * (f01 - 0.5) * h * g.w[t] * wgt;
                             acc += interp(P.interp, A, q, h) * wy / V;
                         }
                     }
                     real qp[3] = {sp.pos[0], iy0 * h + origin[1], sp.pos[2]};
-                    acc += interp(P.interp, Psi, qp, h) * sp.n[1] / V;
+                    acc += interp(P.interp, Psi, qp, h) * (sp.n[1] * wgt) / V;
                 } else {
                     // calc_density_in_cell_from_quadrature_point_list.cpp:101-131
-                    acc += interp(P.interp, Psi, sp.pos, h) * sp.n[1] / V;
+                    acc += interp(P.interp, Psi, sp.pos, h) * (sp.n[1] * wgt) / V;
                 }
+            }
             }
         }
         out[cell] = acc;
@@ -648,14 +691,14 @@ static void split_offsets(int comp, int error_pass, const real* density_main, re
 static int advect_field(const Grid& G, const Velocity& vel, int comp, const real* in, real* out,
                         real dt, int interp_method, int k, int correction, int use_integral,
                         const real* density_split, real minimal_area, int nthreads,
-                        long* faces, long* polys) {
+                        long* faces, long* polys, int maccormack) {
     Field A = make_field(in, G, comp);
     if (comp < 0) { for (int d = 0; d < 3; ++d) { A.M[d] = G.N[d]; A.off[d] = 0.5; } }
     long n = (long)A.M[0] * A.M[1] * A.M[2];
     PassParams P;
     P.comp = comp; P.interp = interp_method; P.k = k; P.minimal_area = minimal_area; P.dt = dt;
     P.psi_mode = use_integral ? (interp_method == I_WENO6 ? PSI_WENO6 : PSI_LINEAR) : PSI_PLAIN;
-    P.use_integral = use_integral; P.zero_velocity = 0;
+    P.use_integral = use_integral; P.zero_velocity = 0; P.maccormack = maccormack;
     split_offsets(comp, 0, density_split, P.color_off);
     int status = run_pass(G, vel, A, P, out, nthreads, 0, n, faces, polys);
     if (!correction) return status;
@@ -679,7 +722,7 @@ static int advect_field(const Grid& G, const Velocity& vel, int comp, const real
 // =================================== C ABI =========================================
 extern "C" {
 
-int fo_version(void) { return 3; }
+int fo_version(void) { return 4; }
 
 // Gauss rule (for tests): writes k nodes on [-1,1] and normalised weights.
 int fo_gauss(int k, double* x, double* w) {
@@ -750,14 +793,14 @@ int fo_flux_pass(int nx, int ny, int nz, double h, const double* u, const double
                  int comp, const double* field, double dt, int interp_method, int psi_mode,
                  int use_integral, int zero_velocity, const double* color_off, int k,
                  double minimal_area, int nthreads, long c0, long c1, double* out,
-                 long* faces, long* polys) {
+                 long* faces, long* polys, int maccormack) {
     Grid G; G.N[0] = nx; G.N[1] = ny; G.N[2] = nz; G.h = h;
     Velocity vel = make_velocity(G, u, v, w);
     Field A = make_field(field, G, comp);
     PassParams P;
     P.comp = comp; P.interp = interp_method; P.psi_mode = psi_mode; P.use_integral = use_integral;
     P.zero_velocity = zero_velocity; P.color_off[0] = color_off[0]; P.color_off[1] = color_off[1];
-    P.k = k; P.minimal_area = minimal_area; P.dt = dt;
+    P.k = k; P.minimal_area = minimal_area; P.dt = dt; P.maccormack = maccormack;
     return run_pass(G, vel, A, P, out, nthreads, c0, c1, faces, polys);
 }
 
@@ -765,20 +808,20 @@ int fo_flux_pass(int nx, int ny, int nz, double h, const double* u, const double
 int fo_move_substances_3D(int nx, int ny, int nz, double h, const double* u, const double* v,
                           const double* w, double* rho, double dt, int interp_method, int k,
                           int correction, int use_integral, const double* split_off,
-                          double minimal_area, int nthreads) {
+                          double minimal_area, int nthreads, int maccormack) {
     Grid G; G.N[0] = nx; G.N[1] = ny; G.N[2] = nz; G.h = h;
     Velocity vel = make_velocity(G, u, v, w);
     long n = (long)nx * ny * nz;
     std::vector<double> in(rho, rho + n);
     return advect_field(G, vel, -1, in.data(), rho, dt, interp_method, k, correction, use_integral,
-                        split_off, minimal_area, nthreads, nullptr, nullptr);
+                        split_off, minimal_area, nthreads, nullptr, nullptr, maccormack);
 }
 
 // advect_velocity_xyz_flux_advection_3D: all three components advected by the old
 // velocity (advect_velocity_flux_advection_3d.cpp:1138-1272), in place.
 int fo_advect_velocity_3D(int nx, int ny, int nz, double h, double* u, double* v, double* w,
                           double dt, int interp_method, int k, int correction, int use_integral,
-                          double minimal_area, int nthreads) {
+                          double minimal_area, int nthreads, int maccormack) {
     Grid G; G.N[0] = nx; G.N[1] = ny; G.N[2] = nz; G.h = h;
     long nu = (long)(nx + 1) * ny * nz, nv = (long)nx * (ny + 1) * nz, nw = (long)nx * ny * (nz + 1);
     std::vector<double> u0(u, u + nu), v0(v, v + nv), w0(w, w + nw);
@@ -789,7 +832,7 @@ int fo_advect_velocity_3D(int nx, int ny, int nz, double h, double* u, double* v
     const real dummy[2] = {0.5, 0.5};
     for (int c = 0; c < 3; ++c)
         status |= advect_field(G, vel, c, ins[c], outs[c], dt, interp_method, k, correction, use_integral,
-                               dummy, minimal_area, nthreads, nullptr, nullptr);
+                               dummy, minimal_area, nthreads, nullptr, nullptr, maccormack);
     return status;
 }
 

@@ -92,7 +92,7 @@ class Oracle:
         return out.reshape(L[0], L[1], L[2], 3)
 
     def flux_pass(self, N, h, u, v, w, comp, field, dt, interp, psi_mode, use_integral, zero_velocity,
-                  color_off, k, minimal_area=1.0, nthreads=1, c0=0, c1=-1):
+                  color_off, k, minimal_area=1.0, nthreads=1, c0=0, c1=-1, maccormack=0):
         u, v, w, field = _f64(u), _f64(v), _f64(w), _f64(field)
         out = np.zeros(field.size)
         co = (ctypes.c_double * 2)(*color_off)
@@ -101,26 +101,26 @@ class Oracle:
                                    _ptr(field), ctypes.c_double(dt), interp, psi_mode, use_integral,
                                    zero_velocity, co, k, ctypes.c_double(minimal_area), nthreads,
                                    ctypes.c_long(c0), ctypes.c_long(c1), _ptr(out), ctypes.byref(nf),
-                                   ctypes.byref(npoly))
+                                   ctypes.byref(npoly), int(maccormack))
         return out, st, nf.value, npoly.value
 
     # ---- reference entry points ----
     def move_substances_3D(self, N, h, u, v, w, rho, dt, interp=0, k=3, correction=1, use_integral=1,
-                           split_off=(0.5, 0.5), minimal_area=1.0, nthreads=1):
+                           split_off=(0.5, 0.5), minimal_area=1.0, nthreads=1, maccormack=0):
         u, v, w = _f64(u), _f64(v), _f64(w)
         r = _f64(rho).copy()
         so = (ctypes.c_double * 2)(*split_off)
         st = self.lib.fo_move_substances_3D(N[0], N[1], N[2], ctypes.c_double(h), _ptr(u), _ptr(v), _ptr(w),
                                             _ptr(r), ctypes.c_double(dt), interp, k, correction, use_integral,
-                                            so, ctypes.c_double(minimal_area), nthreads)
+                                            so, ctypes.c_double(minimal_area), nthreads, int(maccormack))
         return r, st
 
     def advect_velocity_3D(self, N, h, u, v, w, dt, interp=0, k=3, correction=1, use_integral=1,
-                           minimal_area=1.0, nthreads=1):
+                           minimal_area=1.0, nthreads=1, maccormack=0):
         u, v, w = _f64(u).copy(), _f64(v).copy(), _f64(w).copy()
         st = self.lib.fo_advect_velocity_3D(N[0], N[1], N[2], ctypes.c_double(h), _ptr(u), _ptr(v), _ptr(w),
                                             ctypes.c_double(dt), interp, k, correction, use_integral,
-                                            ctypes.c_double(minimal_area), nthreads)
+                                            ctypes.c_double(minimal_area), nthreads, int(maccormack))
         return u, v, w, st
 
     def pressure_rhs(self, N, h, u, v, w):
@@ -174,19 +174,20 @@ class Reference:
         self.lib.fr_split_face(_ptr(v), ctypes.c_double(h), split, ctypes.c_double(minimal_area), max_out, _ptr(out), ctypes.byref(n))
         return out[:6 * min(n.value, max_out)].reshape(-1, 6)
 
-    def density_pass(self, N, h, u, v, w, rho, dt, interp, psi, use_integral, zero_vel, split, k, minimal_area=1.0):
+    def density_pass(self, N, h, u, v, w, rho, dt, interp, psi, use_integral, zero_vel, split, k, minimal_area=1.0,
+                     maccormack=0):
         out = np.zeros(N[0] * N[1] * N[2])
         self.lib.fr_density_pass(N[0], N[1], N[2], ctypes.c_double(h), _ptr(_f64(u)), _ptr(_f64(v)), _ptr(_f64(w)),
                                  _ptr(_f64(rho)), ctypes.c_double(dt), interp, psi, use_integral, zero_vel, split, k,
-                                 ctypes.c_double(minimal_area), _ptr(out))
+                                 ctypes.c_double(minimal_area), _ptr(out), int(maccormack))
         return out
 
     def move_substances_3D(self, N, h, u, v, w, rho, dt, interp=0, split=0, k=3, correction=1, use_integral=1,
-                           minimal_area=1.0):
+                           minimal_area=1.0, maccormack=0):
         r = _f64(rho).copy()
         self.lib.fr_move_substances_3D(N[0], N[1], N[2], ctypes.c_double(h), _ptr(_f64(u)), _ptr(_f64(v)), _ptr(_f64(w)),
                                        _ptr(r), ctypes.c_double(dt), interp, split, k, correction, use_integral,
-                                       ctypes.c_double(minimal_area))
+                                       ctypes.c_double(minimal_area), int(maccormack))
         return r
 
     def velocity_pass_linear(self, N, h, u, v, w, dim, dt, k, minimal_area=1.0):

@@ -62,7 +62,7 @@ void fill_velocity(Grid_3D& g, const double* u, const double* v, const double* w
 // single-threaded: i_thread = 0 over the whole face range.
 void density_pass(Grid_3D& g, std::vector<MY_FLOAT_TYPE>& values, MY_FLOAT_TYPE dt,
                   const std::string& split, const std::string& interp, const std::string& interp_psi,
-                  bool zero_vel, bool use_integral, int k, MY_FLOAT_TYPE minimal_area) {
+                  bool zero_vel, bool use_integral, int k, MY_FLOAT_TYPE minimal_area, bool maccormack = false) {
     const size_t nface = (size_t)g.Grid_num_x * g.Grid_num_y * g.Grid_num_z * 6;
     calc_psi_on_cell_face_from_density_on_cell_center_3D(
         g, g.psi_substance_density_cell_face_x, g.psi_substance_density_cell_face_y,
@@ -72,12 +72,12 @@ void density_pass(Grid_3D& g, std::vector<MY_FLOAT_TYPE>& values, MY_FLOAT_TYPE 
     if (use_integral) {
         quadrature_point_vector qd, qp, qv;
         backtrace_and_calc_all_quadrature_point_list_for_integrate_density(
-            -1, qd, qp, qv, 0, nface, false, g, dt, split, "gauss", 1, 0, interp, zero_vel, k, false,
+            -1, qd, qp, qv, 0, nface, maccormack, g, dt, split, "gauss", 1, 0, interp, zero_vel, k, false,
             "density", minimal_area);
         calc_density_in_cell_from_quadrature_point_list_for_integrate_density(qd, qp, g, after, 0, interp, values);
     } else {
         quadrature_point_vector q;
-        backtrace_and_calc_all_quadrature_point_list(-1, q, 0, nface, false, g, dt, split, "gauss", 1, 0,
+        backtrace_and_calc_all_quadrature_point_list(-1, q, 0, nface, maccormack, g, dt, split, "gauss", 1, 0,
                                                      interp, zero_vel, minimal_area);
         calc_density_in_cell_from_quadrature_point_list(q, g, after, 0, interp);
     }
@@ -180,13 +180,13 @@ int fr_split_face(const double* verts12, double h, int split, double minimal_are
 // One density pass.  interp: 0 WENO6 1 linear 2 1Dy_linear; psi: 0 WENO6 1 linear 3 const.
 int fr_density_pass(int nx, int ny, int nz, double h, const double* u, const double* v, const double* w,
                     const double* rho, double dt, int interp, int psi, int use_integral, int zero_vel,
-                    int split, int k, double minimal_area, double* out) {
+                    int split, int k, double minimal_area, double* out, int maccormack) {
     Grid_3D g(nx, ny, nz, (MY_FLOAT_TYPE)h);
     fill_velocity(g, u, v, w);
     std::vector<MY_FLOAT_TYPE> R; to_vec(R, rho, (long)nx * ny * nz);
     std::string ps = psi == 3 ? "const" : interp_name(psi);
     density_pass(g, R, (MY_FLOAT_TYPE)dt, split_name(split), interp_name(interp), ps, zero_vel != 0, use_integral != 0, k,
-                 (MY_FLOAT_TYPE)minimal_area);
+                 (MY_FLOAT_TYPE)minimal_area, maccormack != 0);
     for (size_t i = 0; i < R.size(); ++i) out[i] = R[i];
     return 0;
 }
@@ -195,19 +195,20 @@ int fr_density_pass(int nx, int ny, int nz, double h, const double* u, const dou
 // move_substances_3d.cpp:58-226 (interp 0 WENO6 or 1 linear).
 int fr_move_substances_3D(int nx, int ny, int nz, double h, const double* u, const double* v, const double* w,
                           double* rho, double dt, int interp, int split, int k, int correction, int use_integral,
-                          double minimal_area) {
+                          double minimal_area, int maccormack) {
     Grid_3D g(nx, ny, nz, (MY_FLOAT_TYPE)h);
     fill_velocity(g, u, v, w);
     long n = (long)nx * ny * nz;
     std::vector<MY_FLOAT_TYPE> before; to_vec(before, rho, n);
     std::vector<MY_FLOAT_TYPE> R = before;
     std::string im = interp_name(interp), ipsi = interp == 0 ? "WENO6" : "linear";
-    density_pass(g, R, (MY_FLOAT_TYPE)dt, split_name(split), im, ipsi, false, use_integral != 0, k, (MY_FLOAT_TYPE)minimal_area);
+    const bool mc = maccormack != 0;
+    density_pass(g, R, (MY_FLOAT_TYPE)dt, split_name(split), im, ipsi, false, use_integral != 0, k, (MY_FLOAT_TYPE)minimal_area, mc);
     if (correction) {
         std::vector<MY_FLOAT_TYPE> c = before;
-        density_pass(g, c, (MY_FLOAT_TYPE)dt, split_name(split), im, ipsi, true, false, k, (MY_FLOAT_TYPE)minimal_area);
+        density_pass(g, c, (MY_FLOAT_TYPE)dt, split_name(split), im, ipsi, true, false, k, (MY_FLOAT_TYPE)minimal_area, mc);
         for (long i = 0; i < n; ++i) { c[i] *= -1.0; c[i] += before[i]; }
-        density_pass(g, c, (MY_FLOAT_TYPE)dt, "xz-AxisAligned", "1Dy_linear", "const", false, false, k, (MY_FLOAT_TYPE)minimal_area);
+        density_pass(g, c, (MY_FLOAT_TYPE)dt, "xz-AxisAligned", "1Dy_linear", "const", false, false, k, (MY_FLOAT_TYPE)minimal_area, mc);
         for (long i = 0; i < n; ++i) R[i] += c[i];
     }
     for (long i = 0; i < n; ++i) rho[i] = R[i];

@@ -6,6 +6,7 @@ small seeded inputs and stores inputs and outputs.  The oracle is pinned against
 files by tests/test_oracle_golden.py; the GPU library is then checked against the oracle.
 
     python tests/golden/make_golden.py          (needs the reference checkout)
+    python tests/golden/make_golden.py maccormack   (the MacCormack fixtures only)
 """
 import os
 import sys
@@ -102,8 +103,38 @@ def main():
         for p, R in refs.items():
             out["vel_%d_%s" % (dim, p)] = R.velocity_pass_linear(N, h, u, v, w, dim, dt, 3)
     np.savez_compressed(os.path.join(HERE, "velocity.npz"), **out)
+    maccormack(refs)
     print("golden fixtures written to", HERE)
 
 
+def maccormack(refs):
+    """the flux MacCormack branch (backtrace_..._for_integrate_density.cpp:146-234): the density
+    passes and move_substances_3D of the 16^3 scene with use_MacCormack_scheme on"""
+    n = 16; N = (n, n, n); h = 1.0 / n
+    u, v, w = scenes.fourier_velocity(n, seed=1)
+    rho = scenes.gaussian_blobs(n, seed=2)
+    dt = 2.0 * h
+    out = {"N": np.array(N), "h": h, "u": u, "v": v, "w": w, "rho": rho, "dt": dt}
+    passes = {  # name: (interp, psi, use_integral, zero_velocity, split)
+        "weno6_integral": (0, 0, 1, 0, 0),
+        "weno6_zero_velocity": (0, 0, 0, 1, 0),
+        "error_1dy_linear": (2, 3, 0, 0, 1),
+        "linear_integral": (1, 1, 1, 0, 0),
+    }
+    for name, (interp, psi, integ, zv, split) in passes.items():
+        for p, R in refs.items():
+            out["pass_%s_%s" % (name, p)] = R.density_pass(N, h, u, v, w, rho, dt, interp, psi, integ, zv, split, 3,
+                                                           maccormack=1)
+    for p, R in refs.items():
+        out["move_substances_%s" % p] = R.move_substances_3D(N, h, u, v, w, rho, dt, interp=0, split=0, k=3,
+                                                             correction=1, use_integral=1, maccormack=1)
+    np.savez_compressed(os.path.join(HERE, "maccormack.npz"), **out)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["maccormack"]:
+        if not os.path.exists(os.path.join(orc.REF_DIR, "libfia_ref_double.so")):
+            orc.build_reference()
+        maccormack({p: orc.Reference(p) for p in ("double", "float")})
+    else:
+        main()
