@@ -183,6 +183,44 @@ __global__ void k_backtrace(PassDesc d, const T* __restrict__ u, const T* __rest
     verts[3 * id + 0] = p[0]; verts[3 * id + 1] = p[1]; verts[3 * id + 2] = p[2];
 }
 
+// Second trace of the flux MacCormack scheme (calc_backtraced_face_3D.cpp:9-128, time
+// direction "backward"): x2 = x1 + dt u(x1), the velocity interpolated at the backtraced
+// position x1, the pin rule of the first trace, then the clamp (:131-160).
+template <typename T>
+__global__ void k_forward_trace(PassDesc d, const T* __restrict__ u, const T* __restrict__ v,
+                                const T* __restrict__ w, NodeField fu, NodeField fv, NodeField fw,
+                                const T* __restrict__ verts, T* __restrict__ verts2) {
+    const int Lx = d.A.Mx + 1, Ly = d.A.My + 1, Lz = d.A.Mz + 1;
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= (long long)Lx * Ly * Lz) return;
+    const int k = (int)(id % Lz);
+    const int j = (int)((id / Lz) % Ly);
+    const int i = (int)(id / ((long long)Lz * Ly));
+    const T h = T(d.h);
+    T p[3] = {verts[3 * id], verts[3 * id + 1], verts[3 * id + 2]};
+    bool pinned = false;
+    if (d.comp >= 0) {
+        const int vi = d.comp == 0 ? i : (d.comp == 1 ? j : k);
+        pinned = (vi <= 1 || vi >= d.N[d.comp]);
+    }
+    if (!pinned) {
+        const T vx = interp(d.interp, u, fu, h, p[0], p[1], p[2]);
+        const T vy = interp(d.interp, v, fv, h, p[0], p[1], p[2]);
+        const T vz = interp(d.interp, w, fw, h, p[0], p[1], p[2]);
+        const T dt = T(d.dt);
+        p[0] += vx * dt; p[1] += vy * dt; p[2] += vz * dt;
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const int e = (c == d.comp);
+        const T lo = T(0) - T(e) * T(0.5) * h;
+        const T hi = T(0) + h * T(d.N[c]) + T(e) * T(0.5) * h;
+        if (p[c] < lo) p[c] = lo;
+        if (p[c] > hi) p[c] = hi;
+    }
+    verts2[3 * id + 0] = p[0]; verts2[3 * id + 1] = p[1]; verts2[3 * id + 2] = p[2];
+}
+
 // ------------------------------------------------------------------------------------
 // clipping in (xi, eta) space with an explicit stack
 // ------------------------------------------------------------------------------------
@@ -475,11 +513,13 @@ __device__ __forceinline__ void face_corners(int fam, int i, int j, int k, int* 
     }
 }
 
+// flux = wgt * F (acc = 0) or flux + wgt * F (acc = 1): the weighted faces of the flux
+// MacCormack scheme accumulate into one flux per face (wgt = 1, acc = 0 otherwise)
 template <typename T>
 __global__ void __launch_bounds__(128) k_faces(PassDesc d, int fam, const T* __restrict__ a,
                                                const T* __restrict__ psi, const T* __restrict__ verts,
                                                T* __restrict__ flux, T* __restrict__ flux_rev,
-                                               unsigned* status, unsigned long long* counters) {
+                                               unsigned* status, unsigned long long* counters, T wgt, int acc) {
     const int Fx = d.A.Mx + (fam == 0), Fy = d.A.My + (fam == 1), Fz = d.A.Mz + (fam == 2);
     const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long nface = (long long)Fx * Fy * Fz;
@@ -517,8 +557,8 @@ __global__ void __launch_bounds__(128) k_faces(PassDesc d, int fam, const T* __r
             ++nmulti;
         }
         if (!isfinite(F) || !isfinite(Fr)) st |= ST_NONFINITE;
-        flux[id] = F;
-        flux_rev[id] = Fr;
+        flux[id] = acc ? flux[id] + wgt * F : wgt * F;
+        flux_rev[id] = acc ? flux_rev[id] + wgt * Fr : wgt * Fr;
     }
     // warp-aggregated counters and status
     unsigned long long pc = (unsigned long long)npieces;
@@ -584,15 +624,21 @@ cudaError_t launch_backtrace(const PassDesc& d, const VelocityFields& vel, T* ve
 }
 
 template <typename T>
-cudaError_t launch_faces(const PassDesc& d, const T* a, const PassWork<T>& w, cudaStream_t s) {
+static cudaError_t launch_faces_from(const PassDesc& d, const T* a, const PassWork<T>& w, const T* verts, T wgt,
+                                     int acc, cudaStream_t s) {
     for (int fam = 0; fam < 3; ++fam) {
         const long long n = (long long)(d.A.Mx + (fam == 0)) * (d.A.My + (fam == 1)) * (d.A.Mz + (fam == 2));
         prof_mark(w, 0, s);
-        k_faces<T><<<blocks_for(n, 128), 128, 0, s>>>(d, fam, a, w.psi, w.verts, w.flux[fam], w.flux_rev[fam],
-                                                      w.status, w.counters);
+        k_faces<T><<<blocks_for(n, 128), 128, 0, s>>>(d, fam, a, w.psi, verts, w.flux[fam], w.flux_rev[fam],
+                                                      w.status, w.counters, wgt, acc);
         prof_mark(w, 1, s);
     }
     return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_faces(const PassDesc& d, const T* a, const PassWork<T>& w, cudaStream_t s) {
+    return launch_faces_from<T>(d, a, w, w.verts, T(1), 0, s);
 }
 
 template <typename T>
@@ -612,7 +658,21 @@ cudaError_t run_pass(const PassDesc& d, const VelocityFields& vel, const T* a, c
         e = launch_backtrace<T>(d, vel, w.verts, s);
         if (e != cudaSuccess) return e;
     }
-    e = launch_faces<T>(d, a, w, s);
+    if (!d.maccormack || d.zero_velocity) {
+        // one face per face slot; with zero velocity the MacCormack faces coincide and their
+        // weights sum to one
+        e = launch_faces<T>(d, a, w, s);
+    } else {
+        if (!w.verts2) return cudaErrorInvalidValue;
+        const long long nv = (long long)(d.A.Mx + 1) * (d.A.My + 1) * (d.A.Mz + 1);
+        k_forward_trace<T><<<blocks_for(nv, 128), 128, 0, s>>>(d, (const T*)vel.u, (const T*)vel.v, (const T*)vel.w,
+                                                              vel.fu, vel.fv, vel.fw, w.verts, w.verts2);
+        PassDesc rest = d;
+        rest.zero_velocity = 1;
+        e = launch_faces_from<T>(rest, a, w, w.verts, T(0.5), 0, s);            // the face at rest
+        if (e == cudaSuccess) e = launch_faces_from<T>(d, a, w, w.verts, T(1), 1, s);   // backtraced
+        if (e == cudaSuccess) e = launch_faces_from<T>(d, a, w, w.verts2, T(-0.5), 1, s);   // traced back
+    }
     if (e != cudaSuccess) return e;
     return launch_gather<T>(d, w, in, out, mode, s);
 }

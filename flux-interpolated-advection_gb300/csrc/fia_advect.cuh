@@ -18,6 +18,7 @@ struct PassDesc {
     int psi_mode;           // PSI_PLAIN / PSI_WENO6 / PSI_LINEAR
     int use_integral;       // 1: y-integral quadrature per piece (polygon_3D.cpp:257-487)
     int zero_velocity;      // 1: faces are not moved (zero-velocity pass)
+    int maccormack;         // flux MacCormack: faces at rest (0.5), backtraced (1), traced back (-0.5)
     double color_off[2];    // split method: colour = x/h - off0, z/h - off1
     int k;                  // Gauss points per half cell
     double gx[kMaxGauss];   // Gauss nodes on [-1,1] (centre first, then -/+ pairs)
@@ -52,6 +53,7 @@ struct PieceStore {
     int* face = nullptr;         // family << 29 | face index
     float* flux = nullptr;       // flux of each piece
     int2* range[3] = {nullptr, nullptr, nullptr};   // per face: start, nfwd | nrev << 15 | multi << 30
+    float2* normal[3] = {nullptr, nullptr, nullptr};  // per face: y-normal sums of both clips (lower, upper cell)
     unsigned* count = nullptr;   // device counter of pieces
     long long cap = 0;           // pieces the buffers hold
 };
@@ -64,6 +66,7 @@ template <typename T>
 struct PassWork {
     T* psi;            // P.Mx*P.My*P.Mz
     T* verts;          // 3 * (A.Mx+1)(A.My+1)(A.Mz+1)  backtraced vertex positions
+    T* verts2 = nullptr;   // the same, traced back from verts (flux MacCormack only)
     T* flux[3];        // per face family: (Mx+1)MyMz, Mx(My+1)Mz, MxMy(Mz+1); lower cell's view
     T* flux_rev[3];    // the same faces seen from the upper cell (its own clip when needed)
     unsigned* status;  // one word

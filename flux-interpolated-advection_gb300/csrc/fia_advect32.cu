@@ -106,6 +106,46 @@ __global__ void k_backtrace32(PassDesc d, const float* __restrict__ u, const flo
     disp[3 * id + 0] = dx[0]; disp[3 * id + 1] = dx[1]; disp[3 * id + 2] = dx[2];
 }
 
+// Second trace of the flux MacCormack scheme: from the backtraced position (rest + disp),
+// disp2 = disp + dt/h u(rest + disp), the pin rule and clamp of k_backtrace32
+// (calc_backtraced_face_3D.cpp:9-160, time direction "backward").
+__global__ void k_forward32(PassDesc d, const float* __restrict__ u, const float* __restrict__ v,
+                            const float* __restrict__ w, NodeField fu, NodeField fv, NodeField fw,
+                            const float* __restrict__ disp, float* __restrict__ disp2) {
+    const int Lx = d.A.Mx + 1, Ly = d.A.My + 1, Lz = d.A.Mz + 1;
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= (long long)Lx * Ly * Lz) return;
+    const int k = (int)(id % Lz);
+    const int j = (int)((id / Lz) % Ly);
+    const int i = (int)(id / ((long long)Lz * Ly));
+    const int anc[3] = {i, j, k};
+    float q0[3] = {0.f, 0.f, 0.f};
+    if (d.comp >= 0) q0[d.comp] = -0.5f;
+    float dx[3] = {disp[3 * id], disp[3 * id + 1], disp[3 * id + 2]};
+    bool pinned = false;
+    if (d.comp >= 0) {
+        const int vi = anc[d.comp];
+        pinned = (vi <= 1 || vi >= d.N[d.comp]);
+    }
+    if (!pinned) {
+        const float q[3] = {q0[0] + dx[0], q0[1] + dx[1], q0[2] + dx[2]};
+        const float s = d.dthf;
+        const float v0 = interp_loc(d.interp, PlainLoad{u}, fu, anc, q);
+        const float v1 = interp_loc(d.interp, PlainLoad{v}, fv, anc, q);
+        const float v2 = interp_loc(d.interp, PlainLoad{w}, fw, anc, q);
+        dx[0] += v0 * s; dx[1] += v1 * s; dx[2] += v2 * s;
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float e = (c == d.comp) ? 0.5f : 0.f;
+        const float rest = float(anc[c]) + q0[c];
+        const float lo = -e, hi = float(d.N[c]) + e;
+        if (rest + dx[c] < lo) dx[c] = lo - rest;
+        if (rest + dx[c] > hi) dx[c] = hi - rest;
+    }
+    disp2[3 * id + 0] = dx[0]; disp2[3 * id + 1] = dx[1]; disp2[3 * id + 2] = dx[2];
+}
+
 // ---------------------------------------------------------------------------------
 // faces
 // ---------------------------------------------------------------------------------
@@ -413,9 +453,8 @@ __device__ __forceinline__ void face_of(int fam, const NodeField& A, long long i
     i = (int)(id / ((long long)Fz * Fy));
 }
 
-__global__ void __launch_bounds__(128) k_clip32(PassDesc d, int fam, const float* __restrict__ disp,
-                                                float2* __restrict__ flux, float2* __restrict__ flux_rev,
-                                                PieceStore ps, unsigned* status, unsigned long long* counters) {
+__global__ void __launch_bounds__(128) k_clip32(PassDesc d, int fam, const float* __restrict__ disp, PieceStore ps,
+                                                unsigned* status, unsigned long long* counters) {
     const int Fx = d.A.Mx + (fam == 0), Fy = d.A.My + (fam == 1), Fz = d.A.Mz + (fam == 2);
     const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long nface = (long long)Fx * Fy * Fz;
@@ -459,8 +498,7 @@ __global__ void __launch_bounds__(128) k_clip32(PassDesc d, int fam, const float
             Nr = sink.ny.value();
             ++nmulti;
         }
-        flux[id].y = N;
-        flux_rev[id].y = Nr;
+        ps.normal[fam][id] = make_float2(N, Nr);
     }
     // contiguous slots for this thread's pieces: warp prefix sum, one atomic per warp
     const int cnt = sink.n;
@@ -519,8 +557,10 @@ __global__ void __launch_bounds__(kQuadThreads) k_quad32(PassDesc d, const float
     if ((threadIdx.x & 31) == 0 && ec) atomicAdd(&counters[3], ec);
 }
 
+// flux = wgt (F, N) (acc = 0) or flux + wgt (F, N) (acc = 1): the weighted faces of the flux
+// MacCormack scheme accumulate into one (flux, y-normal sum) pair per face
 __global__ void k_facesum32(PassDesc d, int fam, PieceStore ps, float2* __restrict__ flux, float2* __restrict__ flux_rev,
-                            unsigned* status) {
+                            unsigned* status, float wgt, int acc) {
     const long long nface = (long long)(d.A.Mx + (fam == 0)) * (d.A.My + (fam == 1)) * (d.A.Mz + (fam == 2));
     const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= nface) return;
@@ -531,8 +571,14 @@ __global__ void k_facesum32(PassDesc d, int fam, PieceStore ps, float2* __restri
     for (int q = 0; q < nf; ++q) F.add(ps.flux[(long long)r.x + q]);
     for (int q = 0; q < nr; ++q) Fr.add(ps.flux[(long long)r.x + nf + q]);
     const float f = F.value(), fr = multi ? Fr.value() : -f;
-    flux[id].x = f;
-    flux_rev[id].x = fr;
+    const float2 nrm = ps.normal[fam][id];
+    float2 a = make_float2(wgt * f, wgt * nrm.x), b = make_float2(wgt * fr, wgt * nrm.y);
+    if (acc) {
+        const float2 a0 = flux[id], b0 = flux_rev[id];
+        a.x += a0.x; a.y += a0.y; b.x += b0.x; b.y += b0.y;
+    }
+    flux[id] = a;
+    flux_rev[id] = b;
     if (!isfinite(f) || !isfinite(fr)) atomicOr(status, (unsigned)ST_NONFINITE);
 }
 
@@ -577,20 +623,10 @@ inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 
 }  // namespace
 
-template <>
-cudaError_t run_pass<float>(const PassDesc& d64, const VelocityFields& vel64, const float* a, const PassWork<float>& w,
-                            const float* in, float* out, int mode, cudaStream_t s) {
-    const PassDesc d = desc32(d64);
-    VelocityFields vel = vel64;
-    vel.fu = field32(vel64.fu); vel.fv = field32(vel64.fv); vel.fw = field32(vel64.fw);
-    float2* psi = (float2*)w.psi;
-    const long long cols = (long long)d.A.Mx * d.A.Mz;
-    k_psi32<<<nblk(cols, 128), 128, 0, s>>>(d, a, psi);
-    if (!d.zero_velocity) {
-        const long long nv = (long long)(d.A.Mx + 1) * (d.A.My + 1) * (d.A.Mz + 1);
-        k_backtrace32<<<nblk(nv, 128), 128, 0, s>>>(d, (const float*)vel.u, (const float*)vel.v, (const float*)vel.w,
-                                                   vel.fu, vel.fv, vel.fw, w.verts);
-    }
+// One face stage of the FP32 pipeline: clip (growing the piece store and clipping again when
+// it is too small), per-piece quadrature, per-face sums weighted into the face fluxes.
+static cudaError_t face_stage32(const PassDesc& d, const float* a, const float2* psi, const float* disp,
+                                const PassWork<float>& w, float wgt, int acc, cudaStream_t s) {
     PieceStore& ps = *w.pieces;
     long long nface[3];
     for (int fam = 0; fam < 3; ++fam)
@@ -600,8 +636,7 @@ cudaError_t run_pass<float>(const PassDesc& d64, const VelocityFields& vel64, co
     for (int attempt = 0; attempt < 2; ++attempt) {
         cudaMemsetAsync(ps.count, 0, sizeof(unsigned), s);
         for (int fam = 0; fam < 3; ++fam)
-            k_clip32<<<nblk(nface[fam], 128), 128, 0, s>>>(d, fam, w.verts, (float2*)w.flux[fam],
-                                                           (float2*)w.flux_rev[fam], ps, w.status, w.counters);
+            k_clip32<<<nblk(nface[fam], 128), 128, 0, s>>>(d, fam, disp, ps, w.status, w.counters);
         cudaError_t e = cudaMemcpyAsync(&npc, ps.count, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return e;
@@ -619,7 +654,39 @@ cudaError_t run_pass<float>(const PassDesc& d64, const VelocityFields& vel64, co
     }
     for (int fam = 0; fam < 3; ++fam)
         k_facesum32<<<nblk(nface[fam], 256), 256, 0, s>>>(d, fam, ps, (float2*)w.flux[fam], (float2*)w.flux_rev[fam],
-                                                          w.status);
+                                                          w.status, wgt, acc);
+    return cudaGetLastError();
+}
+
+template <>
+cudaError_t run_pass<float>(const PassDesc& d64, const VelocityFields& vel64, const float* a, const PassWork<float>& w,
+                            const float* in, float* out, int mode, cudaStream_t s) {
+    const PassDesc d = desc32(d64);
+    VelocityFields vel = vel64;
+    vel.fu = field32(vel64.fu); vel.fv = field32(vel64.fv); vel.fw = field32(vel64.fw);
+    float2* psi = (float2*)w.psi;
+    const long long cols = (long long)d.A.Mx * d.A.Mz;
+    k_psi32<<<nblk(cols, 128), 128, 0, s>>>(d, a, psi);
+    const long long nv = (long long)(d.A.Mx + 1) * (d.A.My + 1) * (d.A.Mz + 1);
+    if (!d.zero_velocity)
+        k_backtrace32<<<nblk(nv, 128), 128, 0, s>>>(d, (const float*)vel.u, (const float*)vel.v, (const float*)vel.w,
+                                                   vel.fu, vel.fv, vel.fw, w.verts);
+    cudaError_t e;
+    if (!d.maccormack || d.zero_velocity) {
+        // one face per face slot; with zero velocity the MacCormack faces coincide and their
+        // weights sum to one
+        e = face_stage32(d, a, psi, w.verts, w, 1.f, 0, s);
+    } else {
+        if (!w.verts2) return cudaErrorInvalidValue;
+        k_forward32<<<nblk(nv, 128), 128, 0, s>>>(d, (const float*)vel.u, (const float*)vel.v, (const float*)vel.w,
+                                                 vel.fu, vel.fv, vel.fw, w.verts, w.verts2);
+        PassDesc rest = d;
+        rest.zero_velocity = 1;
+        e = face_stage32(rest, a, psi, w.verts, w, 0.5f, 0, s);                       // the face at rest
+        if (e == cudaSuccess) e = face_stage32(d, a, psi, w.verts, w, 1.f, 1, s);     // backtraced
+        if (e == cudaSuccess) e = face_stage32(d, a, psi, w.verts2, w, -0.5f, 1, s);  // traced back
+    }
+    if (e != cudaSuccess) return e;
     const long long nc = (long long)d.A.Mx * d.A.My * d.A.Mz;
     k_gather32<<<nblk(nc, 256), 256, 0, s>>>(d, (const float2*)w.flux[0], (const float2*)w.flux[1],
                                              (const float2*)w.flux[2], (const float2*)w.flux_rev[0],
@@ -646,6 +713,7 @@ cudaError_t piece_store_reserve(PieceStore& p, long long pieces, long long faces
     if (!p.range[0]) {
         for (int f = 0; f < 3; ++f) {
             cudaError_t e = cudaMalloc(&p.range[f], faces_per_family * sizeof(int2));
+            if (e == cudaSuccess) e = cudaMalloc(&p.normal[f], faces_per_family * sizeof(float2));
             if (e != cudaSuccess) return e;
         }
     }
@@ -654,7 +722,7 @@ cudaError_t piece_store_reserve(PieceStore& p, long long pieces, long long faces
 
 void piece_store_free(PieceStore& p) {
     cudaFree(p.rec); cudaFree(p.face); cudaFree(p.flux); cudaFree(p.count);
-    for (int f = 0; f < 3; ++f) cudaFree(p.range[f]);
+    for (int f = 0; f < 3; ++f) { cudaFree(p.range[f]); cudaFree(p.normal[f]); }
     p = PieceStore();
 }
 

@@ -33,6 +33,8 @@ struct fia_session {
     void* vel[3]; void* vel_next[3];
     void* cbuf;                  // correction field (pass 2 result)
     void* psi; void* verts; void* flux[3]; void* flux_rev[3];
+    void* verts2 = nullptr;      // flux MacCormack: the vertices traced back (allocated on first use)
+    size_t verts_bytes = 0;      // one coordinate of every vertex of the largest field
     void* pw[5];                 // pressure work vectors r z d q (+ spare)
     double* part; double* scal; double* sums;
     unsigned* status; unsigned long long* counters;
@@ -147,8 +149,15 @@ cudaError_t reduce(fia_session* s, const void* a, long long n, int kind, bool ac
     return cudaGetLastError();
 }
 
-// kernels launched by one run_pass: psi, backtrace (moving passes), three face families, gather
-inline unsigned pass_launches(const PassDesc& d) { return d.zero_velocity ? 5u : 6u; }
+// kernels launched by one run_pass: psi, backtrace (moving passes), the face stages (one, or
+// three for the flux MacCormack scheme, plus its second trace), gather.  A face stage is three
+// face-family launches (FP64), or three clips, the per-piece quadrature and three per-face
+// sums (FP32 form).
+inline unsigned pass_launches(const PassDesc& d, int precision) {
+    const bool mc = d.maccormack && !d.zero_velocity;
+    const unsigned stage = precision == FIA_FP64 ? 3u : 7u;
+    return 2u + (d.zero_velocity ? 0u : 1u) + (mc ? 3u * stage + 1u : stage);
+}
 
 // Split offsets (colour = pos/h - off) per field for the main and the error-advection pass
 // (move_substances_3d.cpp:189; advect_velocity_flux_advection_3d.cpp:622-628, :721,
@@ -168,7 +177,7 @@ void split_offsets(int comp, int error_pass, int density_split, double* off) {
 
 int check_params(const fia_advect_params* p) {
     if (!p) return FIA_ERR_INVALID;
-    if (p->use_MacCormack_scheme || p->enable_cell_volume_correction) return FIA_ERR_UNSUPPORTED;
+    if (p->enable_cell_volume_correction) return FIA_ERR_UNSUPPORTED;
     if (p->interpolation_method != FIA_INTERP_WENO6 && p->interpolation_method != FIA_INTERP_LINEAR) return FIA_ERR_INVALID;
     if (p->split_method < 0 || p->split_method > 3) return FIA_ERR_INVALID;
     const int k = p->num_gauss_quadrature_point_for_integrate_density;
@@ -192,7 +201,7 @@ PassDesc base_desc(const fia_session* s, int comp, double dt) {
 template <typename T>
 PassWork<T> work(fia_session* s) {
     PassWork<T> w;
-    w.psi = (T*)s->psi; w.verts = (T*)s->verts;
+    w.psi = (T*)s->psi; w.verts = (T*)s->verts; w.verts2 = (T*)s->verts2;
     for (int f = 0; f < 3; ++f) { w.flux[f] = (T*)s->flux[f]; w.flux_rev[f] = (T*)s->flux_rev[f]; }
     w.status = s->status; w.counters = s->counters;
     w.prof_ev = s->prof_ev.empty() ? nullptr : s->prof_ev.data();
@@ -218,6 +227,12 @@ cudaError_t advect_field(fia_session* s, int comp, const T* in, T* out, double d
     d.k = p->num_gauss_quadrature_point_for_integrate_density;
     make_gauss(d.k, d.gx, d.gw);
     d.minimal_area = p->minimal_area;
+    d.maccormack = p->use_MacCormack_scheme ? 1 : 0;
+    if (d.maccormack && !s->verts2) {
+        const size_t bytes = 3 * s->verts_bytes;
+        if (cudaMalloc(&s->verts2, bytes) != cudaSuccess) return cudaErrorMemoryAllocation;
+        s->allocations.push_back(s->verts2);
+    }
     const VelocityFields vel = velocity(s, vel_fields);
     const PassWork<T> w = work<T>(s);
     // pass 1
@@ -227,18 +242,18 @@ cudaError_t advect_field(fia_session* s, int comp, const T* in, T* out, double d
     d.zero_velocity = 0;
     split_offsets(comp, 0, p->split_method, d.color_off);
     cudaError_t e = run_pass<T>(d, vel, in, w, in, out, 0, s->stream);
-    s->launches += pass_launches(d);
+    s->launches += pass_launches(d, s->precision);
     if (e != cudaSuccess || !p->enable_eliminate_zero_velocity_false_diffusion) return e;
     // pass 2: zero velocity, psi at the piece centroid, plain psi; c = in - A2(in)
     T* c = (T*)s->cbuf;
     d.zero_velocity = 1; d.use_integral = 0; d.psi_mode = PSI_PLAIN;
     e = run_pass<T>(d, vel, in, w, in, c, 1, s->stream);
-    s->launches += pass_launches(d);
+    s->launches += pass_launches(d, s->precision);
     if (e != cudaSuccess) return e;
     // pass 3: advect the error with 1Dy-linear interpolation and the error split
     d.zero_velocity = 0; d.interp = INTERP_1DY_LINEAR;
     split_offsets(comp, 1, p->split_method, d.color_off);
-    s->launches += pass_launches(d);
+    s->launches += pass_launches(d, s->precision);
     return run_pass<T>(d, vel, c, w, nullptr, out, 2, s->stream);
 }
 
@@ -809,6 +824,7 @@ fia_session* fia_create(int nx, int ny, int nz, double cell_length, int precisio
     A(s->rho, fb); A(s->rho_next, fb); A(s->pres, fb); A(s->cbuf, (size_t)big * 8); A(s->psi, pb);
     for (int c = 0; c < 3; ++c) { A(s->vel[c], fb); A(s->vel_next[c], fb); A(s->flux[c], pb); A(s->flux_rev[c], pb); }
     A(s->verts, 3 * fb);
+    s->verts_bytes = fb;
     for (int q = 0; q < 5; ++q) A(s->pw[q], fb);
     { void* t2; A(t2, 4 * sizeof(unsigned)); s->ticket = (unsigned*)t2; }
     void* t;

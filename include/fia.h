@@ -80,8 +80,11 @@ typedef struct fia_advect_params {
     int num_gauss_quadrature_point_for_integrate_density;   /* odd, 1..13 */
     int use_integral;                                       /* y-integral quadrature (main.cpp:64) */
     int enable_eliminate_zero_velocity_false_diffusion;     /* passes 2 and 3 (main.cpp:70) */
-    int use_MacCormack_scheme;                              /* must be 0 */
-    int enable_cell_volume_correction;                      /* must be 0 */
+    int use_MacCormack_scheme;                              /* flux MacCormack: each face at rest, backtraced
+                                                               and traced back, weights 0.5, 1, -0.5
+                                                               (backtrace_..._for_integrate_density.cpp:146-234);
+                                                               not in fia_move_substances_3D_noalloc */
+    int enable_cell_volume_correction;                      /* must be 0 (FIA_ERR_UNSUPPORTED) */
     double minimal_area;                                    /* xi-eta triangulation threshold (main.cpp:82) */
 } fia_advect_params;
 

@@ -94,6 +94,16 @@ def test_fp32_move_substances():
     assert rel(got, ref) < 2e-6
 
 
+def test_fp32_move_substances_maccormack():
+    """the chosen form with the flux MacCormack scheme against the FP64 oracle"""
+    g, h, u, v, w, rho, dt = make(32, fia.FIA_FP32C, seed=3)
+    g.move_substances_3D(dt, fia.advect_params(use_MacCormack_scheme=True))
+    got = g.get("density")
+    g.close()
+    ref, _ = O.move_substances_3D((32, 32, 32), h, u, v, w, rho, dt, nthreads=8, maccormack=1)
+    assert rel(got, ref) < 2e-6
+
+
 def run_plume(n, precision, steps):
     import scenes as sc
     g = fia.Grid3D(n, n, n, 1.0 / n, precision=precision)

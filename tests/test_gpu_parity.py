@@ -198,10 +198,41 @@ def test_cfl_reduction_and_mass():
     g.close()
 
 
+@pytest.mark.parametrize("interp,corr,shape", [("WENO6", True, (16, 16, 16)), ("WENO6", False, (16, 16, 16)),
+                                               ("linear", True, (16, 16, 16)), ("WENO6", True, (7, 9, 6))])
+def test_move_substances_maccormack(interp, corr, shape):
+    """The flux MacCormack scheme (faces at rest, backtraced and traced back, weights 0.5, 1,
+    -0.5) against the oracle, which follows the reference's branch and is pinned against the
+    reference's own code (tests/test_oracle_golden.py)."""
+    g, h, u, v, w, rho, dt = make(*shape, seed=5)
+    p = fia.advect_params(interpolation_method=interp, enable_eliminate_zero_velocity_false_diffusion=corr,
+                          use_MacCormack_scheme=True)
+    st = g.move_substances_3D(dt, p)
+    got = g.get("density")
+    g.close()
+    ref, ost = O.move_substances_3D(shape, h, u, v, w, rho, dt, interp=fia.INTERP[interp], k=3,
+                                    correction=int(corr), maccormack=1)
+    plain, _ = O.move_substances_3D(shape, h, u, v, w, rho, dt, interp=fia.INTERP[interp], k=3,
+                                    correction=int(corr))
+    assert st == 0 and ost == 0
+    assert rel(got, ref) < 1e-10
+    assert rel(got, plain) > 1e-3      # the scheme is in effect
+
+
+def test_advect_velocity_maccormack():
+    g, h, u, v, w, rho, dt = make(12, 12, 12, seed=11, cfl=1.5)
+    g.advect_velocity_xyz_flux_advection_3D(dt, fia.advect_params(use_MacCormack_scheme=True))
+    got = [g.get(c) for c in "uvw"]
+    g.close()
+    ou, ov, ow, _ = O.advect_velocity_3D((12, 12, 12), h, u, v, w, dt, maccormack=1)
+    for a, b in zip(got, (ou, ov, ow)):
+        assert rel(a, b) < 1e-10
+
+
 def test_invalid_arguments_fail_loudly():
     g = fia.Grid3D(8, 8, 8, 1.0 / 8)
     with pytest.raises(fia.FiaError):
-        g.move_substances_3D(0.01, fia.advect_params(use_MacCormack_scheme=True))
+        g.move_substances_3D(0.01, fia.advect_params(enable_cell_volume_correction=True))
     with pytest.raises(fia.FiaError):
         g.move_substances_3D(0.01, fia.advect_params(num_gauss_quadrature_point_for_integrate_density=2))
     with pytest.raises(fia.FiaError):
