@@ -554,7 +554,7 @@ struct PassCounters { long faces = 0; long polys = 0; int status = 0; };
 // advected quantity), writing out[cell] for those cells.
 static void pass_range(const Grid& G, const Velocity& vel, const Field& A, const Field& Psi,
                        const PassParams& P, const Gauss1D& g, real* out, long c0, long c1,
-                       PassCounters& cnt) {
+                       PassCounters& cnt, real* vol) {
     const real h = G.h;
     const real V = h * h * h;
     const int* M = A.M;
@@ -565,7 +565,7 @@ static void pass_range(const Grid& G, const Velocity& vel, const Field& A, const
         int iz = (int)(cell % M[2]);
         int iy = (int)((cell / M[2]) % M[1]);
         int ix = (int)(cell / ((long)M[2] * M[1]));
-        real acc = 0.0;
+        real acc = 0.0, vacc = 0.0;
         for (int f = 0; f < 6; ++f) {
             real vb[4][3], v0[4][3], v2[4][3];
             for (int q = 0; q < 4; ++q) {
@@ -588,6 +588,9 @@ static void pass_range(const Grid& G, const Velocity& vel, const Field& A, const
             cnt.faces++;
             cnt.polys += (long)polys.size();
             for (const SubPoly& sp : polys) {
+                // the volume point of the piece (polygon_3D.cpp:480-486): y n_y summed per cell
+                // (calc_density_in_cell_from_quadrature_point_list.cpp:135-156)
+                vacc += sp.pos[1] * (sp.n[1] * wgt);
                 if (P.use_integral) {
                     // polygon_3D.cpp:257-487
                     const real ry = snap_int((sp.pos[1] - origin[1]) / h);
@@ -625,11 +628,12 @@ static void pass_range(const Grid& G, const Velocity& vel, const Field& A, const
             }
         }
         out[cell] = acc;
+        if (vol) vol[cell] = vacc;
     }
 }
 
 static int run_pass(const Grid& G, const Velocity& vel, const Field& A, const PassParams& P,
-                    real* out, int nthreads, long c0, long c1, long* faces, long* polys) {
+                    real* out, int nthreads, long c0, long c1, long* faces, long* polys, real* vol = nullptr) {
     Gauss1D g = make_gauss(P.k);
     std::vector<real> psi;
     compute_psi(A, G.h, P.psi_mode, g, psi);
@@ -646,7 +650,7 @@ static int run_pass(const Grid& G, const Velocity& vel, const Field& A, const Pa
     long span = c1 - c0;
     for (int t = 0; t < nthreads; ++t) {
         long a = c0 + span * t / nthreads, b = c0 + span * (t + 1) / nthreads;
-        th.emplace_back([&, a, b, t]() { pass_range(G, vel, A, Psi, P, g, out, a, b, cnt[t]); });
+        th.emplace_back([&, a, b, t]() { pass_range(G, vel, A, Psi, P, g, out, a, b, cnt[t], vol); });
     }
     for (auto& x : th) x.join();
     int status = 0; long nf = 0, np = 0;
@@ -686,12 +690,41 @@ static void split_offsets(int comp, int error_pass, const real* density_main, re
     }
 }
 
+// CG on -A (the reference operator, last cell pinned): A p = b to a relative residual tol.
+static int solve_A(const int* N, const real* b, real* p, real tol, int maxit);
+
+// Cell-volume correction (move_substances_3d.cpp:243-493): A p = -(V - V0) on the pinned
+// operator, then density moves between face neighbours by -(p_hi - p_lo) / V0 times the mean
+// of their densities before the correction, x faces, then y, then z.  The reference stops
+// its AMG-CG at a relative residual of 0.1 (:363); here the solve is run to 1e-13, the
+// correction that the reference approximates.
+static void volume_correction(const Grid& G, real* rho, const real* vol) {
+    const int* N = G.N;
+    const long n = (long)N[0] * N[1] * N[2];
+    const real V0 = G.h * G.h * G.h;
+    std::vector<real> b(n), p(n), before(rho, rho + n);
+    for (long c = 0; c < n - 1; ++c) b[c] = -(vol[c] - V0);
+    b[n - 1] = 0.0;
+    solve_A(N, b.data(), p.data(), 1e-13, 100000);
+    const long st[3] = {(long)N[1] * N[2], (long)N[2], 1};
+    for (int a = 0; a < 3; ++a)
+        for (int ix = 0; ix < N[0]; ++ix) for (int iy = 0; iy < N[1]; ++iy) for (int iz = 0; iz < N[2]; ++iz) {
+            const int id[3] = {ix, iy, iz};
+            if (id[a] < 1) continue;
+            const long c = idx3(N, ix, iy, iz), cm = c - st[a];
+            const real flux = -(p[c] - p[cm]) / V0;
+            const real dens = (before[cm] * V0 + before[c] * V0) / (2.0 * V0);
+            rho[cm] -= 1.0 * flux * dens;
+            rho[c] += 1.0 * flux * dens;
+        }
+}
+
 // move_substances_3d.cpp:38-240 (density) and advect_velocity_..._3D_std_thread for one
 // velocity component: pass 1 (+ the zero-velocity / error-advection correction).
 static int advect_field(const Grid& G, const Velocity& vel, int comp, const real* in, real* out,
                         real dt, int interp_method, int k, int correction, int use_integral,
                         const real* density_split, real minimal_area, int nthreads,
-                        long* faces, long* polys, int maccormack) {
+                        long* faces, long* polys, int maccormack, int volume = 0) {
     Field A = make_field(in, G, comp);
     if (comp < 0) { for (int d = 0; d < 3; ++d) { A.M[d] = G.N[d]; A.off[d] = 0.5; } }
     long n = (long)A.M[0] * A.M[1] * A.M[2];
@@ -700,7 +733,9 @@ static int advect_field(const Grid& G, const Velocity& vel, int comp, const real
     P.psi_mode = use_integral ? (interp_method == I_WENO6 ? PSI_WENO6 : PSI_LINEAR) : PSI_PLAIN;
     P.use_integral = use_integral; P.zero_velocity = 0; P.maccormack = maccormack;
     split_offsets(comp, 0, density_split, P.color_off);
-    int status = run_pass(G, vel, A, P, out, nthreads, 0, n, faces, polys);
+    std::vector<real> vol(volume && comp < 0 ? n : 0);
+    int status = run_pass(G, vel, A, P, out, nthreads, 0, n, faces, polys, vol.empty() ? nullptr : vol.data());
+    if (!vol.empty()) volume_correction(G, out, vol.data());
     if (!correction) return status;
     // pass 2: zero velocity, no integral, plain psi
     std::vector<real> c(n);
@@ -808,13 +843,31 @@ int fo_flux_pass(int nx, int ny, int nz, double h, const double* u, const double
 int fo_move_substances_3D(int nx, int ny, int nz, double h, const double* u, const double* v,
                           const double* w, double* rho, double dt, int interp_method, int k,
                           int correction, int use_integral, const double* split_off,
-                          double minimal_area, int nthreads, int maccormack) {
+                          double minimal_area, int nthreads, int maccormack, int volume_correction) {
     Grid G; G.N[0] = nx; G.N[1] = ny; G.N[2] = nz; G.h = h;
     Velocity vel = make_velocity(G, u, v, w);
     long n = (long)nx * ny * nz;
     std::vector<double> in(rho, rho + n);
     return advect_field(G, vel, -1, in.data(), rho, dt, interp_method, k, correction, use_integral,
-                        split_off, minimal_area, nthreads, nullptr, nullptr, maccormack);
+                        split_off, minimal_area, nthreads, nullptr, nullptr, maccormack, volume_correction);
+}
+
+// The advected cell volumes of the density's main pass (the volume points of its pieces).
+int fo_cell_volumes(int nx, int ny, int nz, double h, const double* u, const double* v, const double* w,
+                    double dt, int interp_method, int k, int use_integral, const double* split_off,
+                    double minimal_area, int nthreads, int maccormack, double* vol) {
+    Grid G; G.N[0] = nx; G.N[1] = ny; G.N[2] = nz; G.h = h;
+    Velocity vel = make_velocity(G, u, v, w);
+    long n = (long)nx * ny * nz;
+    std::vector<double> zero(n, 0.0), out(n);
+    Field A = make_field(zero.data(), G, -1);
+    for (int d = 0; d < 3; ++d) { A.M[d] = G.N[d]; A.off[d] = 0.5; }
+    PassParams P;
+    P.comp = -1; P.interp = interp_method; P.k = k; P.minimal_area = minimal_area; P.dt = dt;
+    P.psi_mode = use_integral ? (interp_method == I_WENO6 ? PSI_WENO6 : PSI_LINEAR) : PSI_PLAIN;
+    P.use_integral = use_integral; P.zero_velocity = 0; P.maccormack = maccormack;
+    P.color_off[0] = split_off[0]; P.color_off[1] = split_off[1];
+    return run_pass(G, vel, A, P, out.data(), nthreads, 0, n, nullptr, nullptr, vol);
 }
 
 // advect_velocity_xyz_flux_advection_3D: all three components advected by the old
@@ -930,3 +983,10 @@ double fo_max_abs_velocity(int nx, int ny, int nz, const double* u, const double
 }
 
 }  // extern "C"
+
+namespace {
+static int solve_A(const int* N, const real* b, real* p, real tol, int maxit) {
+    double rr = 0.0;
+    return fo_pressure_solve(N[0], N[1], N[2], b, p, tol, maxit, &rr);
+}
+}  // namespace

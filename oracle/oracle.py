@@ -106,14 +106,26 @@ class Oracle:
 
     # ---- reference entry points ----
     def move_substances_3D(self, N, h, u, v, w, rho, dt, interp=0, k=3, correction=1, use_integral=1,
-                           split_off=(0.5, 0.5), minimal_area=1.0, nthreads=1, maccormack=0):
+                           split_off=(0.5, 0.5), minimal_area=1.0, nthreads=1, maccormack=0, volume_correction=0):
         u, v, w = _f64(u), _f64(v), _f64(w)
         r = _f64(rho).copy()
         so = (ctypes.c_double * 2)(*split_off)
         st = self.lib.fo_move_substances_3D(N[0], N[1], N[2], ctypes.c_double(h), _ptr(u), _ptr(v), _ptr(w),
                                             _ptr(r), ctypes.c_double(dt), interp, k, correction, use_integral,
-                                            so, ctypes.c_double(minimal_area), nthreads, int(maccormack))
+                                            so, ctypes.c_double(minimal_area), nthreads, int(maccormack),
+                                            int(volume_correction))
         return r, st
+
+    def cell_volumes(self, N, h, u, v, w, dt, interp=0, k=3, use_integral=1, split_off=(0.5, 0.5), minimal_area=1.0,
+                     nthreads=1, maccormack=0):
+        """advected cell volumes of the density's main pass (sum of y n_y of the pieces)"""
+        u, v, w = _f64(u), _f64(v), _f64(w)
+        out = np.zeros(N[0] * N[1] * N[2])
+        so = (ctypes.c_double * 2)(*split_off)
+        st = self.lib.fo_cell_volumes(N[0], N[1], N[2], ctypes.c_double(h), _ptr(u), _ptr(v), _ptr(w),
+                                      ctypes.c_double(dt), interp, k, use_integral, so, ctypes.c_double(minimal_area),
+                                      nthreads, int(maccormack), _ptr(out))
+        return out, st
 
     def advect_velocity_3D(self, N, h, u, v, w, dt, interp=0, k=3, correction=1, use_integral=1,
                            minimal_area=1.0, nthreads=1, maccormack=0):
@@ -189,6 +201,15 @@ class Reference:
                                        _ptr(r), ctypes.c_double(dt), interp, split, k, correction, use_integral,
                                        ctypes.c_double(minimal_area), int(maccormack))
         return r
+
+    def cell_volumes(self, N, h, u, v, w, dt, interp=0, split=0, k=3, minimal_area=1.0, maccormack=0):
+        """advected cell volumes of the density's main pass (integral branch) from the reference's
+        own volume points and calc_cell_volumes_from_quadrature_point_list"""
+        out = np.zeros(N[0] * N[1] * N[2])
+        self.lib.fr_cell_volumes(N[0], N[1], N[2], ctypes.c_double(h), _ptr(_f64(u)), _ptr(_f64(v)), _ptr(_f64(w)),
+                                 ctypes.c_double(dt), interp, split, k, ctypes.c_double(minimal_area), int(maccormack),
+                                 _ptr(out))
+        return out
 
     def velocity_pass_linear(self, N, h, u, v, w, dim, dt, k, minimal_area=1.0):
         sizes = [(N[0] + 1) * N[1] * N[2], N[0] * (N[1] + 1) * N[2], N[0] * N[1] * (N[2] + 1)]

@@ -215,6 +215,24 @@ int fr_move_substances_3D(int nx, int ny, int nz, double h, const double* u, con
     return 0;
 }
 
+// Advected cell volumes of a density main pass (integral branch): the volume points the
+// reference collects with enable_cell_volume_correction, summed by its
+// calc_cell_volumes_from_quadrature_point_list (calc_density_in_cell_from_quadrature_point_list.cpp:135-156).
+int fr_cell_volumes(int nx, int ny, int nz, double h, const double* u, const double* v, const double* w, double dt,
+                    int interp, int split, int k, double minimal_area, int maccormack, double* out) {
+    Grid_3D g(nx, ny, nz, (MY_FLOAT_TYPE)h);
+    fill_velocity(g, u, v, w);
+    const size_t nface = (size_t)nx * ny * nz * 6;
+    std::vector<MY_FLOAT_TYPE> vol((size_t)nx * ny * nz, 0.0);
+    quadrature_point_vector qd, qp, qv;
+    backtrace_and_calc_all_quadrature_point_list_for_integrate_density(
+        -1, qd, qp, qv, 0, nface, maccormack != 0, g, (MY_FLOAT_TYPE)dt, split_name(split), "gauss", 1, 0,
+        interp_name(interp), false, k, true, "density", (MY_FLOAT_TYPE)minimal_area);
+    calc_cell_volumes_from_quadrature_point_list(qv, g, vol, 0);
+    for (size_t i = 0; i < vol.size(); ++i) out[i] = vol[i];
+    return 0;
+}
+
 // One velocity-component pass in the reference's defined ("linear") form, integral path:
 // advect_velocity_{x,y,z}_flux_advection_3D_std_thread with the correction off.
 int fr_velocity_pass_linear(int nx, int ny, int nz, double h, const double* u, const double* v, const double* w,

@@ -7,6 +7,7 @@ files by tests/test_oracle_golden.py; the GPU library is then checked against th
 
     python tests/golden/make_golden.py          (needs the reference checkout)
     python tests/golden/make_golden.py maccormack   (the MacCormack fixtures only)
+    python tests/golden/make_golden.py volumes      (the cell-volume fixtures only)
 """
 import os
 import sys
@@ -104,7 +105,21 @@ def main():
             out["vel_%d_%s" % (dim, p)] = R.velocity_pass_linear(N, h, u, v, w, dim, dt, 3)
     np.savez_compressed(os.path.join(HERE, "velocity.npz"), **out)
     maccormack(refs)
+    volumes(refs)
     print("golden fixtures written to", HERE)
+
+
+def volumes(refs):
+    """advected cell volumes of the density main pass of the 16^3 scene (the volume points of the
+    cell-volume correction), plain and with the flux MacCormack scheme"""
+    n = 16; N = (n, n, n); h = 1.0 / n
+    u, v, w = scenes.fourier_velocity(n, seed=1)
+    dt = 2.0 * h
+    out = {"N": np.array(N), "h": h, "u": u, "v": v, "w": w, "dt": dt}
+    for mc in (0, 1):
+        for p, R in refs.items():
+            out["vol_mc%d_%s" % (mc, p)] = R.cell_volumes(N, h, u, v, w, dt, maccormack=mc)
+    np.savez_compressed(os.path.join(HERE, "volumes.npz"), **out)
 
 
 def maccormack(refs):
@@ -132,9 +147,9 @@ def maccormack(refs):
 
 
 if __name__ == "__main__":
-    if sys.argv[1:] == ["maccormack"]:
+    if sys.argv[1:] in (["maccormack"], ["volumes"]):
         if not os.path.exists(os.path.join(orc.REF_DIR, "libfia_ref_double.so")):
             orc.build_reference()
-        maccormack({p: orc.Reference(p) for p in ("double", "float")})
+        {"maccormack": maccormack, "volumes": volumes}[sys.argv[1]]({p: orc.Reference(p) for p in ("double", "float")})
     else:
         main()
