@@ -274,7 +274,7 @@ __device__ __forceinline__ void centroid(const T* px, const T* py, int num, T& c
 template <typename T>
 __device__ __forceinline__ T piece_flux(const PassDesc& d, const FaceGeom<T>& g, const T* px, const T* py,
                                         int num, T cxi, T ceta, const T* __restrict__ a,
-                                        const T* __restrict__ psi) {
+                                        const T* __restrict__ psi, T* vol) {
     const T h = T(d.h);
     // 3D centroid and the y component of the scaled normal (split_face_3D.cpp:67-93)
     const T cx = bilin(g.x, cxi, ceta), cy = bilin(g.y, cxi, ceta), cz = bilin(g.z, cxi, ceta);
@@ -298,6 +298,8 @@ __device__ __forceinline__ T piece_flux(const PassDesc& d, const FaceGeom<T>& g,
         }
         ny = acc * T(0.5);
     }
+    // the piece's volume point (polygon_3D.cpp:480-486): y n_y
+    if (vol) *vol += cy * ny;
     if (ny == T(0)) return T(0);
     T F = T(0);
     if (d.use_integral) {
@@ -334,12 +336,12 @@ __device__ __forceinline__ T piece_flux(const PassDesc& d, const FaceGeom<T>& g,
 // Emits a polygon (optionally triangulated to minimal_area, facecutter.h:255-324).
 template <typename T>
 __device__ T emit_polygon(const PassDesc& d, const FaceGeom<T>& g, const T* px, const T* py, int num,
-                          const T* __restrict__ a, const T* __restrict__ psi, unsigned& st, int& npieces) {
+                          const T* __restrict__ a, const T* __restrict__ psi, unsigned& st, int& npieces, T* vol) {
     T cx, cy, area;
     centroid(px, py, num, cx, cy, area);
     const T minA = T(d.minimal_area);
     if (!(area > minA)) {
-        if (area != T(0)) { ++npieces; return piece_flux(d, g, px, py, num, cx, cy, a, psi); }
+        if (area != T(0)) { ++npieces; return piece_flux(d, g, px, py, num, cx, cy, a, psi, vol); }
         return T(0);
     }
     // triangulate: fan from the centroid (num > 3) then recursive longest-edge bisection
@@ -380,7 +382,7 @@ __device__ T emit_polygon(const PassDesc& d, const FaceGeom<T>& g, const T* px, 
             tri[top][4] = tx[i2]; tri[top][5] = ty[i2]; ++top;
         } else if (tarea != T(0)) {
             ++npieces;
-            F += piece_flux(d, g, tx, ty, 3, tcx, tcy, a, psi);
+            F += piece_flux(d, g, tx, ty, 3, tcx, tcy, a, psi, vol);
         }
     }
     return F;
@@ -392,7 +394,7 @@ __device__ T emit_polygon(const PassDesc& d, const FaceGeom<T>& g, const T* px, 
 // partition depends on the vertex order and the two adjacent cells see different pieces.
 template <typename T>
 __device__ T clip_face(const PassDesc& d, const FaceGeom<T>& g, const T* __restrict__ a,
-                       const T* __restrict__ psi, unsigned& st, int& npieces, bool& multi) {
+                       const T* __restrict__ psi, unsigned& st, int& npieces, bool& multi, T* vol = nullptr) {
     const T h = T(d.h);
     CV<T> pool[kPool];
     unsigned char sstart[kMaxStack], snum[kMaxStack], sdim[kMaxStack];
@@ -481,7 +483,7 @@ __device__ T clip_face(const PassDesc& d, const FaceGeom<T>& g, const T* __restr
                 if (num >= 3) {
                     T px[kMaxVerts], py[kMaxVerts];
                     for (int q = 0; q < num; ++q) { px[q] = poly[q].p0; py[q] = poly[q].p1; }
-                    F += emit_polygon(d, g, px, py, num, a, psi, st, npieces);
+                    F += emit_polygon(d, g, px, py, num, a, psi, st, npieces, vol);
                 }
                 top = pstart;
             }
@@ -519,7 +521,8 @@ template <typename T>
 __global__ void __launch_bounds__(128) k_faces(PassDesc d, int fam, const T* __restrict__ a,
                                                const T* __restrict__ psi, const T* __restrict__ verts,
                                                T* __restrict__ flux, T* __restrict__ flux_rev,
-                                               unsigned* status, unsigned long long* counters, T wgt, int acc) {
+                                               unsigned* status, unsigned long long* counters, T wgt, int acc,
+                                               T* __restrict__ fvol, T* __restrict__ fvol_rev) {
     const int Fx = d.A.Mx + (fam == 0), Fy = d.A.My + (fam == 1), Fz = d.A.Mz + (fam == 2);
     const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long nface = (long long)Fx * Fy * Fz;
@@ -544,8 +547,10 @@ __global__ void __launch_bounds__(128) k_faces(PassDesc d, int fam, const T* __r
             }
         }
         bool multi = false;
-        const T F = clip_face(d, g, a, psi, st, npieces, multi);
+        T V = T(0), Vr = T(0);
+        const T F = clip_face(d, g, a, psi, st, npieces, multi, fvol ? &V : nullptr);
         T Fr = -F;
+        Vr = -V;
         if (multi) {
             // the upper cell's own face: vertex order (v0, v3, v2, v1), which is the reference's
             // x-/y-/z- face order (backtrace_..._for_integrate_density.cpp:77-112)
@@ -553,12 +558,17 @@ __global__ void __launch_bounds__(128) k_faces(PassDesc d, int fam, const T* __r
             r.x[1] = g.x[3]; r.y[1] = g.y[3]; r.z[1] = g.z[3];
             r.x[3] = g.x[1]; r.y[3] = g.y[1]; r.z[3] = g.z[1];
             int np2 = 0; bool m2 = false;
-            Fr = clip_face(d, r, a, psi, st, np2, m2);
+            Vr = T(0);
+            Fr = clip_face(d, r, a, psi, st, np2, m2, fvol ? &Vr : nullptr);
             ++nmulti;
         }
         if (!isfinite(F) || !isfinite(Fr)) st |= ST_NONFINITE;
         flux[id] = acc ? flux[id] + wgt * F : wgt * F;
         flux_rev[id] = acc ? flux_rev[id] + wgt * Fr : wgt * Fr;
+        if (fvol) {
+            fvol[id] = acc ? fvol[id] + wgt * V : wgt * V;
+            fvol_rev[id] = acc ? fvol_rev[id] + wgt * Vr : wgt * Vr;
+        }
     }
     // warp-aggregated counters and status
     unsigned long long pc = (unsigned long long)npieces;
@@ -600,7 +610,8 @@ __global__ void k_gather(PassDesc d, const T* __restrict__ fx, const T* __restri
     const T val = s / V;
     if (mode == 0) out[id] = val;
     else if (mode == 1) out[id] = in[id] - val;
-    else out[id] = out[id] + val;
+    else if (mode == 2) out[id] = out[id] + val;
+    else out[id] = s;
 }
 
 // ------------------------------------------------------------------------------------
@@ -630,7 +641,9 @@ static cudaError_t launch_faces_from(const PassDesc& d, const T* a, const PassWo
         const long long n = (long long)(d.A.Mx + (fam == 0)) * (d.A.My + (fam == 1)) * (d.A.Mz + (fam == 2));
         prof_mark(w, 0, s);
         k_faces<T><<<blocks_for(n, 128), 128, 0, s>>>(d, fam, a, w.psi, verts, w.flux[fam], w.flux_rev[fam],
-                                                      w.status, w.counters, wgt, acc);
+                                                      w.status, w.counters, wgt, acc,
+                                                      d.volumes ? w.fvol[fam] : nullptr,
+                                                      d.volumes ? w.fvol_rev[fam] : nullptr);
         prof_mark(w, 1, s);
     }
     return cudaGetLastError();
@@ -674,6 +687,12 @@ cudaError_t run_pass(const PassDesc& d, const VelocityFields& vel, const T* a, c
         if (e == cudaSuccess) e = launch_faces_from<T>(d, a, w, w.verts2, T(-0.5), 1, s);   // traced back
     }
     if (e != cudaSuccess) return e;
+    if (d.volumes) {
+        if (!w.vol || !w.fvol[0]) return cudaErrorInvalidValue;
+        const long long n = (long long)d.A.Mx * d.A.My * d.A.Mz;
+        k_gather<T><<<blocks_for(n, 256), 256, 0, s>>>(d, w.fvol[0], w.fvol[1], w.fvol[2], w.fvol_rev[0],
+                                                       w.fvol_rev[1], w.fvol_rev[2], nullptr, w.vol, 3);
+    }
     return launch_gather<T>(d, w, in, out, mode, s);
 }
 

@@ -19,6 +19,7 @@ struct PassDesc {
     int use_integral;       // 1: y-integral quadrature per piece (polygon_3D.cpp:257-487)
     int zero_velocity;      // 1: faces are not moved (zero-velocity pass)
     int maccormack;         // flux MacCormack: faces at rest (0.5), backtraced (1), traced back (-0.5)
+    int volumes;            // also sum y n_y of the pieces per face into PassWork::fvol (cell volumes)
     double color_off[2];    // split method: colour = x/h - off0, z/h - off1
     int k;                  // Gauss points per half cell
     double gx[kMaxGauss];   // Gauss nodes on [-1,1] (centre first, then -/+ pairs)
@@ -67,6 +68,9 @@ struct PassWork {
     T* psi;            // P.Mx*P.My*P.Mz
     T* verts;          // 3 * (A.Mx+1)(A.My+1)(A.Mz+1)  backtraced vertex positions
     T* verts2 = nullptr;   // the same, traced back from verts (flux MacCormack only)
+    T* fvol[3] = {nullptr, nullptr, nullptr};      // per face: sum of y n_y of its pieces (PassDesc::volumes)
+    T* fvol_rev[3] = {nullptr, nullptr, nullptr};  // the same seen from the upper cell
+    T* vol = nullptr;  // cells: the advected cell volumes (PassDesc::volumes)
     T* flux[3];        // per face family: (Mx+1)MyMz, Mx(My+1)Mz, MxMy(Mz+1); lower cell's view
     T* flux_rev[3];    // the same faces seen from the upper cell (its own clip when needed)
     unsigned* status;  // one word
@@ -102,7 +106,7 @@ template <typename T>
 cudaError_t launch_backtrace(const PassDesc& d, const VelocityFields& vel, T* verts, cudaStream_t s);
 template <typename T>
 cudaError_t launch_faces(const PassDesc& d, const T* a, const PassWork<T>& w, cudaStream_t s);
-// mode 0: out = div F / V; 1: out = in - div F / V; 2: out += div F / V
+// mode 0: out = div F / V; 1: out = in - div F / V; 2: out += div F / V; 3: out = div F (raw)
 template <typename T>
 cudaError_t launch_gather(const PassDesc& d, const PassWork<T>& w, const T* in, T* out, int mode, cudaStream_t s);
 

@@ -34,6 +34,11 @@ struct fia_session {
     void* cbuf;                  // correction field (pass 2 result)
     void* psi; void* verts; void* flux[3]; void* flux_rev[3];
     void* verts2 = nullptr;      // flux MacCormack: the vertices traced back (allocated on first use)
+    // cell-volume correction (allocated on first use): per-face y n_y sums, cell volumes, the
+    // right-hand side and the potential of its Poisson solve
+    void* fvol[3] = {nullptr, nullptr, nullptr};
+    void* fvol_rev[3] = {nullptr, nullptr, nullptr};
+    void* vol = nullptr; void* vol_rhs = nullptr; void* vol_p = nullptr;
     size_t verts_bytes = 0;      // one coordinate of every vertex of the largest field
     void* pw[5];                 // pressure work vectors r z d q (+ spare)
     double* part; double* scal; double* sums;
@@ -177,7 +182,6 @@ void split_offsets(int comp, int error_pass, int density_split, double* off) {
 
 int check_params(const fia_advect_params* p) {
     if (!p) return FIA_ERR_INVALID;
-    if (p->enable_cell_volume_correction) return FIA_ERR_UNSUPPORTED;
     if (p->interpolation_method != FIA_INTERP_WENO6 && p->interpolation_method != FIA_INTERP_LINEAR) return FIA_ERR_INVALID;
     if (p->split_method < 0 || p->split_method > 3) return FIA_ERR_INVALID;
     const int k = p->num_gauss_quadrature_point_for_integrate_density;
@@ -202,6 +206,8 @@ template <typename T>
 PassWork<T> work(fia_session* s) {
     PassWork<T> w;
     w.psi = (T*)s->psi; w.verts = (T*)s->verts; w.verts2 = (T*)s->verts2;
+    for (int f = 0; f < 3; ++f) { w.fvol[f] = (T*)s->fvol[f]; w.fvol_rev[f] = (T*)s->fvol_rev[f]; }
+    w.vol = (T*)s->vol;
     for (int f = 0; f < 3; ++f) { w.flux[f] = (T*)s->flux[f]; w.flux_rev[f] = (T*)s->flux_rev[f]; }
     w.status = s->status; w.counters = s->counters;
     w.prof_ev = s->prof_ev.empty() ? nullptr : s->prof_ev.data();
@@ -216,6 +222,95 @@ VelocityFields velocity(fia_session* s, void* const* v) {
     vel.u = v[0]; vel.v = v[1]; vel.w = v[2];
     vel.fu = cell_field(s->N, 0); vel.fv = cell_field(s->N, 1); vel.fw = cell_field(s->N, 2);
     return vel;
+}
+
+// ------------------------------ cell-volume correction -----------------------------
+// move_substances_3d.cpp:243-493: A p = -(V - V0) on the reference operator (last cell pinned,
+// no solids), i.e. B p = V - V0 for B = -A; then density moves between face neighbours by
+// -(p_hi - p_lo) / V0 times the mean of their densities before the correction, x faces, then
+// y, then z (each cell gathers its six faces in that order).
+template <typename T>
+__global__ void k_volume_rhs(const T* __restrict__ vol, T* __restrict__ rhs, T* __restrict__ before,
+                             const T* __restrict__ rho, long long n, T V0) {
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        rhs[c] = c == n - 1 ? T(0) : vol[c] - V0;
+        before[c] = rho[c];
+    }
+}
+
+template <typename T>
+__global__ void k_volume_exchange(int nx, int ny, int nz, const T* __restrict__ p, const T* __restrict__ before,
+                                  T* __restrict__ rho, T V0) {
+    const long long n = (long long)nx * ny * nz;
+    const long long sx = (long long)ny * nz, sy = nz;
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        const int iz = (int)(c % nz), iy = (int)((c / nz) % ny), ix = (int)(c / sx);
+        const int id[3] = {ix, iy, iz}, lim[3] = {nx, ny, nz};
+        const long long st[3] = {sx, sy, 1};
+        T val = rho[c];
+        for (int a = 0; a < 3; ++a) {
+            if (id[a] >= 1) {            // the face below: this cell is its upper cell
+                const long long o = c - st[a];
+                const T flux = -(p[c] - p[o]) / V0;
+                const T dens = (before[o] * V0 + before[c] * V0) / (T(2) * V0);
+                val += T(1) * flux * dens;
+            }
+            if (id[a] < lim[a] - 1) {    // the face above: this cell is its lower cell
+                const long long o = c + st[a];
+                const T flux = -(p[o] - p[c]) / V0;
+                const T dens = (before[c] * V0 + before[o] * V0) / (T(2) * V0);
+                val -= T(1) * flux * dens;
+            }
+        }
+        rho[c] = val;
+    }
+}
+
+constexpr double kVolumeTol = 1e-12;   // relative residual of the volume solve (FP64 form)
+
+template <typename T>
+PressureWork<T> pressure_work(fia_session* s);
+
+// allocates the buffers of the cell-volume correction on first use
+cudaError_t volume_buffers(fia_session* s) {
+    if (s->vol) return cudaSuccess;
+    const size_t fb = s->verts_bytes;   // one value per node of the largest field
+    auto A = [&](void*& dst) -> cudaError_t {
+        cudaError_t e = cudaMalloc(&dst, fb);
+        if (e == cudaSuccess) { s->allocations.push_back(dst); cudaMemsetAsync(dst, 0, fb, s->stream); }
+        return e;
+    };
+    for (int f = 0; f < 3; ++f) {
+        cudaError_t e = A(s->fvol[f]);
+        if (e == cudaSuccess) e = A(s->fvol_rev[f]);
+        if (e != cudaSuccess) return e;
+    }
+    cudaError_t e = A(s->vol);
+    if (e == cudaSuccess) e = A(s->vol_rhs);
+    if (e == cudaSuccess) e = A(s->vol_p);
+    return e;
+}
+
+// rho (the main pass's result) corrected by the cell volumes in s->vol
+template <typename T>
+cudaError_t volume_correction(fia_session* s, T* rho) {
+    const int nx = s->N[0], ny = s->N[1], nz = s->N[2];
+    const long long n = (long long)nx * ny * nz;
+    const T V0 = T(s->h * s->h * s->h);
+    T* before = (T*)s->vol;   // the volumes are consumed by the right-hand side first
+    k_volume_rhs<T><<<1024, 256, 0, s->stream>>>((const T*)s->vol, (T*)s->vol_rhs, before, rho, n, V0);
+    PressureWork<T> W = pressure_work<T>(s);
+    W.p = (T*)s->vol_p;
+    const PoissonGrid g{nx, ny, nz, (int)(n - 1), nullptr};
+    cudaError_t e = cudaMemsetAsync(W.p, 0, n * sizeof(T), s->stream);
+    double rr = 0.0;
+    if (e == cudaSuccess) e = pressure_residual<T>(W, g, (const T*)s->vol_rhs, &rr, s->stream);
+    PressureReport rep;
+    if (e == cudaSuccess && rr > 0.0) e = pressure_pcg<T>(W, g, rr, rr, kVolumeTol, 50000, &rep, s->stream);
+    if (e != cudaSuccess) return e;
+    s->launches += 3 + (unsigned long long)rep.launches;
+    k_volume_exchange<T><<<1024, 256, 0, s->stream>>>(nx, ny, nz, (const T*)W.p, before, rho, V0);
+    return cudaGetLastError();
 }
 
 // One field through move_substances_3D's pass structure (move_substances_3d.cpp:58-226);
@@ -241,8 +336,14 @@ cudaError_t advect_field(fia_session* s, int comp, const T* in, T* out, double d
     d.psi_mode = p->use_integral ? (d.interp == INTERP_WENO6 ? PSI_WENO6 : PSI_LINEAR) : PSI_PLAIN;
     d.zero_velocity = 0;
     split_offsets(comp, 0, p->split_method, d.color_off);
+    // cell-volume correction of the density (move_substances_3d.cpp:106-112; the velocity
+    // version is commented out in the reference)
+    const bool volumes = p->enable_cell_volume_correction && comp < 0;
+    d.volumes = volumes ? 1 : 0;
     cudaError_t e = run_pass<T>(d, vel, in, w, in, out, 0, s->stream);
-    s->launches += pass_launches(d, s->precision);
+    s->launches += pass_launches(d, s->precision) + (volumes ? 1 : 0);
+    if (e == cudaSuccess && volumes) e = volume_correction<T>(s, out);
+    d.volumes = 0;
     if (e != cudaSuccess || !p->enable_eliminate_zero_velocity_false_diffusion) return e;
     // pass 2: zero velocity, psi at the piece centroid, plain psi; c = in - A2(in)
     T* c = (T*)s->cbuf;
@@ -275,6 +376,10 @@ int finish_status(fia_session* s) {
 
 template <typename T>
 int move_substances(fia_session* s, double dt, const fia_advect_params* p) {
+    if (p->enable_cell_volume_correction) {
+        if (s->precision != FIA_FP64) return FIA_ERR_UNSUPPORTED;
+        CK(volume_buffers(s));
+    }
     CK(reset_counters(s));
     CK(advect_field<T>(s, -1, (const T*)s->rho, (T*)s->rho_next, dt, p, s->vel));
     std::swap(s->rho, s->rho_next);

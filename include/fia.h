@@ -84,7 +84,13 @@ typedef struct fia_advect_params {
                                                                and traced back, weights 0.5, 1, -0.5
                                                                (backtrace_..._for_integrate_density.cpp:146-234);
                                                                not in fia_move_substances_3D_noalloc */
-    int enable_cell_volume_correction;                      /* must be 0 (FIA_ERR_UNSUPPORTED) */
+    int enable_cell_volume_correction;                      /* density: cell volumes from the pieces'
+                                                               y n_y, Poisson solve of -(V - V0), mass
+                                                               exchanged between neighbours
+                                                               (move_substances_3d.cpp:243-493); plain
+                                                               FP64 form only (FIA_ERR_UNSUPPORTED in
+                                                               FP32C sessions and the allocation-free
+                                                               entry point) */
     double minimal_area;                                    /* xi-eta triangulation threshold (main.cpp:82) */
 } fia_advect_params;
 
