@@ -1109,6 +1109,65 @@ int fia_wall_momentum_loss(fia_session* s, double* out3) {
     return FIA_OK;
 }
 
+int fia_total_momentum(fia_session* s, double* out3) {
+    if (!s || !out3) return FIA_ERR_INVALID;
+    const double V = s->h * s->h * s->h;
+    for (int c = 0; c < 3; ++c) {
+        const long long n = field_count(s, FIA_FIELD_U + c);
+        CK(s->precision == FIA_FP64 ? reduce<double>(s, s->vel[c], n, 0, false) : reduce<float>(s, s->vel[c], n, 0, false));
+        double m = 0.0;
+        CK(cudaMemcpyAsync(&m, s->red_out, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        out3[c] = m * V;
+    }
+    return FIA_OK;
+}
+
+int fia_write_density_frame(fia_session* s, const char* path, int frame) {
+    if (!s || !path) return FIA_ERR_INVALID;
+    static_assert(sizeof(fia_frame_header) == 64, "frame header layout");
+    fia_frame_header hd;
+    std::memset(&hd, 0, sizeof(hd));
+    std::memcpy(hd.magic, "FIAFRM1", 8);
+    hd.nx = s->N[0]; hd.ny = s->N[1]; hd.nz = s->N[2];
+    hd.frame = frame;
+    for (int c = 0; c < 3; ++c) hd.origin[c] = -0.5 * s->h * s->N[c];
+    hd.voxel_size = s->h;
+    const long long n = field_count(s, FIA_FIELD_DENSITY);
+    std::vector<float> data((size_t)n);
+    int r = fia_get_field(s, FIA_FIELD_DENSITY, data.data(), FIA_HOST_F32);
+    if (r != FIA_OK) return r;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) { g_last_error = std::string("fia_write_density_frame: cannot open ") + path; return FIA_ERR_INVALID; }
+    const bool ok = std::fwrite(&hd, sizeof(hd), 1, f) == 1 && std::fwrite(data.data(), sizeof(float), (size_t)n, f) == (size_t)n;
+    if (std::fclose(f) != 0 || !ok) { g_last_error = std::string("fia_write_density_frame: write failed: ") + path; return FIA_ERR_INVALID; }
+    return FIA_OK;
+}
+
+int fia_append_totals(fia_session* s, const char* prefix, double now_time) {
+    if (!s || !prefix) return FIA_ERR_INVALID;
+    double mass = 0.0, mom[3], loss[3];
+    int r = fia_total_mass(s, &mass);
+    if (r == FIA_OK) r = fia_total_momentum(s, mom);
+    if (r == FIA_OK) r = fia_wall_momentum_loss(s, loss);
+    if (r != FIA_OK) return r;
+    auto append = [&](const std::string& name, double v) -> bool {
+        FILE* f = std::fopen((std::string(prefix) + name).c_str(), "a");
+        if (!f) return false;
+        const bool ok = std::fprintf(f, "%.16g %.16g\n", now_time, v) > 0;
+        return std::fclose(f) == 0 && ok;
+    };
+    bool ok = append("total_mass.dat", mass);
+    static const char* ax[3] = {"x", "y", "z"};
+    for (int c = 0; c < 3 && ok; ++c) {
+        ok = append(std::string("total_momentum_") + ax[c] + ".dat", mom[c]) &&
+             append(std::string("total_loss_of_momentum_") + ax[c] + ".dat", loss[c]) &&
+             append(std::string("momentum_") + ax[c] + "_plus_total_loss_of_momentum_" + ax[c] + ".dat", mom[c] + loss[c]);
+    }
+    if (!ok) { g_last_error = std::string("fia_append_totals: cannot write under ") + prefix; return FIA_ERR_INVALID; }
+    return FIA_OK;
+}
+
 int fia_pass_counters(fia_session* s, unsigned long long* out5) {
     if (!s || !out5) return FIA_ERR_INVALID;
     if (s->counters_pending) {

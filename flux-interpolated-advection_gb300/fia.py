@@ -146,6 +146,9 @@ def _declare(lib):
     lib.fia_max_abs_velocity.argtypes = [vp, dp]
     lib.fia_total_mass.argtypes = [vp, dp]
     lib.fia_wall_momentum_loss.argtypes = [vp, dp]
+    lib.fia_total_momentum.argtypes = [vp, dp]
+    lib.fia_write_density_frame.argtypes = [vp, ctypes.c_char_p, ip]
+    lib.fia_append_totals.argtypes = [vp, ctypes.c_char_p, ctypes.c_double]
     lib.fia_pass_counters.argtypes = [vp, ctypes.POINTER(ctypes.c_ulonglong)]
     lib.fia_move_substances_3D_host.argtypes = [vp, ip, vp, vp, vp, vp, ctypes.c_double, ctypes.POINTER(AdvectParams)]
     lib.fia_advect_velocity_xyz_host.argtypes = [vp, ip, vp, vp, vp, ctypes.c_double, ctypes.POINTER(AdvectParams)]
@@ -354,6 +357,20 @@ class Grid3D:
         _check(self.lib.fia_wall_momentum_loss(self.s, out), "fia_wall_momentum_loss")
         return tuple(out)
 
+    def total_momentum(self):
+        out = (ctypes.c_double * 3)()
+        _check(self.lib.fia_total_momentum(self.s, out), "fia_total_momentum")
+        return tuple(out)
+
+    # ---- frame output (main.cpp:515-654) ----
+    def write_density_frame(self, path, frame):
+        """dense density frame (header + float32, see read_density_frame)"""
+        _check(self.lib.fia_write_density_frame(self.s, os.fsencode(path), int(frame)), "fia_write_density_frame")
+
+    def append_totals(self, prefix, now_time):
+        """one line per log: total mass, momenta, wall momentum losses and their sums"""
+        _check(self.lib.fia_append_totals(self.s, os.fsencode(prefix), ctypes.c_double(now_time)), "fia_append_totals")
+
     def pass_counters(self):
         """Cumulative (faces, pieces, faces clipped from both sides, FP32 point
         interpolations, kernel launches) since the session was created."""
@@ -494,3 +511,16 @@ class Grid3D:
         out = np.zeros(M[0] * (M[1] + 1) * M[2])
         _check(self.lib.fia_debug_psi(self.s, comp, _dp(f), mode, k, _dp(out)), "fia_debug_psi")
         return out
+
+
+def read_density_frame(path):
+    """(density array (nx, ny, nz) float32, header dict) of a frame written by
+    Grid3D.write_density_frame / fia_write_density_frame"""
+    raw = open(path, "rb").read()
+    if raw[:8] != b"FIAFRM1\0":
+        raise FiaError("%s: not a density frame" % path)
+    nx, ny, nz, frame = np.frombuffer(raw[8:24], dtype="<i4")
+    origin = np.frombuffer(raw[24:48], dtype="<f8")
+    voxel = float(np.frombuffer(raw[48:56], dtype="<f8")[0])
+    data = np.frombuffer(raw[64:], dtype="<f4").reshape(int(nx), int(ny), int(nz))
+    return data, {"frame": int(frame), "origin": tuple(float(x) for x in origin), "voxel_size": voxel}

@@ -185,6 +185,26 @@ int fia_max_abs_velocity(fia_session* s, double* out);
 int fia_total_mass(fia_session* s, double* out);
 /* total_loss_of_momentum_{x,y,z} accumulated by calc_pressure_gradient_term_3D. */
 int fia_wall_momentum_loss(fia_session* s, double* out3);
+/* Sum of face velocity * cell volume per component (the momenta of main.cpp:533-585), FP64. */
+int fia_total_momentum(fia_session* s, double* out3);
+
+/* Frame output of the reference's main loop (main.cpp:515-654).  The density frame the
+ * reference exports as an OpenVDB grid (vdbexport.cpp:43-98: origin -L/2 per axis, voxel size
+ * = cell length) is written as a dense little-endian file: the 64-byte header
+ * fia_frame_header, then nx*ny*nz float32 values in the grid's linear order (z fastest). */
+typedef struct fia_frame_header {
+    char magic[8];        /* "FIAFRM1" and a zero byte */
+    int nx, ny, nz;
+    int frame;            /* movie frame index (the %04d of substance_density_%04d.vdb) */
+    double origin[3];     /* world position of voxel (0,0,0)'s corner: -0.5 * cell length * n */
+    double voxel_size;    /* cell length */
+    int reserved[2];      /* zero */
+} fia_frame_header;
+int fia_write_density_frame(fia_session* s, const char* path, int frame);
+/* Appends one "time value" line (16 significant digits) to each of the reference's logs under
+ * the path prefix: total_mass.dat, total_momentum_{x,y,z}.dat, total_loss_of_momentum_{x,y,z}.dat
+ * and momentum_{x,y,z}_plus_total_loss_of_momentum_{x,y,z}.dat. */
+int fia_append_totals(fia_session* s, const char* prefix, double now_time);
 /* Work counters accumulated since fia_create: [0] faces visited, [1] pieces emitted,
  * [2] faces clipped from both sides (an iso-line crossed a piece more than twice, so the
  * two adjacent cells see different pieces; FP32 form only counts [3]), [3] point
