@@ -559,8 +559,10 @@ __global__ void __launch_bounds__(kQuadThreads) k_quad32(PassDesc d, const float
 
 // flux = wgt (F, N) (acc = 0) or flux + wgt (F, N) (acc = 1): the weighted faces of the flux
 // MacCormack scheme accumulate into one (flux, y-normal sum) pair per face
+// With fvol: (M, Mr) = sums of y n_y of the face's pieces in cells (y relative to the face
+// anchor), the same weighting, for the cell volumes of the cell-volume correction.
 __global__ void k_facesum32(PassDesc d, int fam, PieceStore ps, float2* __restrict__ flux, float2* __restrict__ flux_rev,
-                            unsigned* status, float wgt, int acc) {
+                            unsigned* status, float wgt, int acc, float2* __restrict__ fvol) {
     const long long nface = (long long)(d.A.Mx + (fam == 0)) * (d.A.My + (fam == 1)) * (d.A.Mz + (fam == 2));
     const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= nface) return;
@@ -580,6 +582,39 @@ __global__ void k_facesum32(PassDesc d, int fam, PieceStore ps, float2* __restri
     flux[id] = a;
     flux_rev[id] = b;
     if (!isfinite(f) || !isfinite(fr)) atomicOr(status, (unsigned)ST_NONFINITE);
+    if (fvol) {
+        Kahan M, Mr;
+        for (int q = 0; q < nf; ++q) { const float4 p = ps.rec[(long long)r.x + q]; M.add(p.y * p.w); }
+        for (int q = 0; q < nr; ++q) { const float4 p = ps.rec[(long long)r.x + nf + q]; Mr.add(p.y * p.w); }
+        const float m = M.value(), mr = multi ? Mr.value() : -m;
+        float2 v = make_float2(wgt * m, wgt * mr);
+        if (acc) { const float2 v0 = fvol[id]; v.x += v0.x; v.y += v0.y; }
+        fvol[id] = v;
+    }
+}
+
+// Advected cell volumes in cells (cell-volume correction, density only): the volume points
+// y n_y of a cell's pieces, from the per-face sums with y relative to each face's anchor.  The
+// faces of cell (i, j, k) are anchored at row j except its upper y-face (row j + 1), which
+// adds its y-normal sum; the term j sum_f s_f N_f of the common row is zero for a closed
+// surface and is dropped (in FP32 it would only carry rounding).
+__global__ void k_volume_gather32(PassDesc d, const float2* __restrict__ vx, const float2* __restrict__ vy,
+                                  const float2* __restrict__ vz, const float2* __restrict__ fy, float* __restrict__ vol) {
+    const int Mx = d.A.Mx, My = d.A.My, Mz = d.A.Mz;
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= (long long)Mx * My * Mz) return;
+    const int k = (int)(id % Mz);
+    const int j = (int)((id / Mz) % My);
+    const int i = (int)(id / ((long long)Mz * My));
+    Kahan s;
+    s.add(vx[((long long)(i + 1) * My + j) * Mz + k].x);
+    s.add(vx[((long long)i * My + j) * Mz + k].y);
+    s.add(vy[((long long)i * (My + 1) + j + 1) * Mz + k].x);
+    s.add(vy[((long long)i * (My + 1) + j) * Mz + k].y);
+    s.add(vz[((long long)i * My + j) * (Mz + 1) + k + 1].x);
+    s.add(vz[((long long)i * My + j) * (Mz + 1) + k].y);
+    s.add(fy[((long long)i * (My + 1) + j + 1) * Mz + k].y);
+    vol[id] = s.value();
 }
 
 // rho'(c) = sum_f s_f [Ft + (Psi0(f) - Psi_c) Ny], compensated
@@ -654,7 +689,8 @@ static cudaError_t face_stage32(const PassDesc& d, const float* a, const float2*
     }
     for (int fam = 0; fam < 3; ++fam)
         k_facesum32<<<nblk(nface[fam], 256), 256, 0, s>>>(d, fam, ps, (float2*)w.flux[fam], (float2*)w.flux_rev[fam],
-                                                          w.status, wgt, acc);
+                                                          w.status, wgt, acc,
+                                                          d.volumes ? (float2*)w.fvol[fam] : nullptr);
     return cudaGetLastError();
 }
 
@@ -688,6 +724,11 @@ cudaError_t run_pass<float>(const PassDesc& d64, const VelocityFields& vel64, co
     }
     if (e != cudaSuccess) return e;
     const long long nc = (long long)d.A.Mx * d.A.My * d.A.Mz;
+    if (d.volumes) {
+        if (!w.vol || !w.fvol[0] || d.comp >= 0) return cudaErrorInvalidValue;
+        k_volume_gather32<<<nblk(nc, 256), 256, 0, s>>>(d, (const float2*)w.fvol[0], (const float2*)w.fvol[1],
+                                                        (const float2*)w.fvol[2], (const float2*)w.flux[1], w.vol);
+    }
     k_gather32<<<nblk(nc, 256), 256, 0, s>>>(d, (const float2*)w.flux[0], (const float2*)w.flux[1],
                                              (const float2*)w.flux[2], (const float2*)w.flux_rev[0],
                                              (const float2*)w.flux_rev[1], (const float2*)w.flux_rev[2], psi, in, out,

@@ -266,7 +266,8 @@ __global__ void k_volume_exchange(int nx, int ny, int nz, const T* __restrict__ 
     }
 }
 
-constexpr double kVolumeTol = 1e-12;   // relative residual of the volume solve (FP64 form)
+// relative residual of the volume solve: FP64 form, FP32 form (FP32 Jacobi-PCG with FP64 dots)
+constexpr double kVolumeTol = 1e-12, kVolumeTol32 = 1e-6;
 
 template <typename T>
 PressureWork<T> pressure_work(fia_session* s);
@@ -274,29 +275,33 @@ PressureWork<T> pressure_work(fia_session* s);
 // allocates the buffers of the cell-volume correction on first use
 cudaError_t volume_buffers(fia_session* s) {
     if (s->vol) return cudaSuccess;
-    const size_t fb = s->verts_bytes;   // one value per node of the largest field
-    auto A = [&](void*& dst) -> cudaError_t {
-        cudaError_t e = cudaMalloc(&dst, fb);
-        if (e == cudaSuccess) { s->allocations.push_back(dst); cudaMemsetAsync(dst, 0, fb, s->stream); }
+    const size_t fb = s->verts_bytes;                    // one value per node of the largest field
+    const size_t pb = s->verts_bytes / s->es * 8;        // one double, or one float pair (FP32 form)
+    auto A = [&](void*& dst, size_t bytes) -> cudaError_t {
+        cudaError_t e = cudaMalloc(&dst, bytes);
+        if (e == cudaSuccess) { s->allocations.push_back(dst); cudaMemsetAsync(dst, 0, bytes, s->stream); }
         return e;
     };
     for (int f = 0; f < 3; ++f) {
-        cudaError_t e = A(s->fvol[f]);
-        if (e == cudaSuccess) e = A(s->fvol_rev[f]);
+        cudaError_t e = A(s->fvol[f], pb);
+        if (e == cudaSuccess) e = A(s->fvol_rev[f], pb);
         if (e != cudaSuccess) return e;
     }
-    cudaError_t e = A(s->vol);
-    if (e == cudaSuccess) e = A(s->vol_rhs);
-    if (e == cudaSuccess) e = A(s->vol_p);
+    cudaError_t e = A(s->vol, fb);
+    if (e == cudaSuccess) e = A(s->vol_rhs, fb);
+    if (e == cudaSuccess) e = A(s->vol_p, fb);
     return e;
 }
 
-// rho (the main pass's result) corrected by the cell volumes in s->vol
+// rho (the main pass's result) corrected by the cell volumes in s->vol (FP64 form: absolute
+// volumes, V0 = h^3; FP32 form: volumes in cells, V0 = 1: the potential scales with the
+// volumes and the exchanged fraction -(p_hi - p_lo) / V0 is the same)
 template <typename T>
 cudaError_t volume_correction(fia_session* s, T* rho) {
     const int nx = s->N[0], ny = s->N[1], nz = s->N[2];
     const long long n = (long long)nx * ny * nz;
-    const T V0 = T(s->h * s->h * s->h);
+    const bool fp64 = s->precision == FIA_FP64;
+    const T V0 = fp64 ? T(s->h * s->h * s->h) : T(1);
     T* before = (T*)s->vol;   // the volumes are consumed by the right-hand side first
     k_volume_rhs<T><<<1024, 256, 0, s->stream>>>((const T*)s->vol, (T*)s->vol_rhs, before, rho, n, V0);
     PressureWork<T> W = pressure_work<T>(s);
@@ -305,8 +310,9 @@ cudaError_t volume_correction(fia_session* s, T* rho) {
     cudaError_t e = cudaMemsetAsync(W.p, 0, n * sizeof(T), s->stream);
     double rr = 0.0;
     if (e == cudaSuccess) e = pressure_residual<T>(W, g, (const T*)s->vol_rhs, &rr, s->stream);
-    PressureReport rep;
-    if (e == cudaSuccess && rr > 0.0) e = pressure_pcg<T>(W, g, rr, rr, kVolumeTol, 50000, &rep, s->stream);
+    PressureReport rep{};
+    if (e == cudaSuccess && rr > 0.0)
+        e = pressure_pcg<T>(W, g, rr, rr, fp64 ? kVolumeTol : kVolumeTol32, 50000, &rep, s->stream);
     if (e != cudaSuccess) return e;
     s->launches += 3 + (unsigned long long)rep.launches;
     k_volume_exchange<T><<<1024, 256, 0, s->stream>>>(nx, ny, nz, (const T*)W.p, before, rho, V0);
@@ -376,10 +382,7 @@ int finish_status(fia_session* s) {
 
 template <typename T>
 int move_substances(fia_session* s, double dt, const fia_advect_params* p) {
-    if (p->enable_cell_volume_correction) {
-        if (s->precision != FIA_FP64) return FIA_ERR_UNSUPPORTED;
-        CK(volume_buffers(s));
-    }
+    if (p->enable_cell_volume_correction) CK(volume_buffers(s));
     CK(reset_counters(s));
     CK(advect_field<T>(s, -1, (const T*)s->rho, (T*)s->rho_next, dt, p, s->vel));
     std::swap(s->rho, s->rho_next);

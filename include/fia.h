@@ -87,10 +87,9 @@ typedef struct fia_advect_params {
     int enable_cell_volume_correction;                      /* density: cell volumes from the pieces'
                                                                y n_y, Poisson solve of -(V - V0), mass
                                                                exchanged between neighbours
-                                                               (move_substances_3d.cpp:243-493); plain
-                                                               FP64 form only (FIA_ERR_UNSUPPORTED in
-                                                               FP32C sessions and the allocation-free
-                                                               entry point) */
+                                                               (move_substances_3d.cpp:243-493); both
+                                                               forms (FIA_ERR_UNSUPPORTED in the
+                                                               allocation-free entry point) */
     double minimal_area;                                    /* xi-eta triangulation threshold (main.cpp:82) */
 } fia_advect_params;
 

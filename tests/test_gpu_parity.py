@@ -247,11 +247,9 @@ def test_move_substances_volume_correction(mc):
 
 
 def test_invalid_arguments_fail_loudly():
-    g32 = fia.Grid3D(8, 8, 8, 1.0 / 8, precision=fia.FIA_FP32C)
-    with pytest.raises(fia.FiaError):   # the cell-volume correction is implemented in the plain form only
-        g32.move_substances_3D(0.01, fia.advect_params(enable_cell_volume_correction=True))
-    g32.close()
     g = fia.Grid3D(8, 8, 8, 1.0 / 8)
+    with pytest.raises(fia.FiaError):
+        g.move_substances_3D(0.01, fia.advect_params(minimal_area=0.0))
     with pytest.raises(fia.FiaError):
         g.move_substances_3D(0.01, fia.advect_params(num_gauss_quadrature_point_for_integrate_density=2))
     with pytest.raises(fia.FiaError):
