@@ -277,9 +277,17 @@ __device__ int piece_quad32(const PassDesc& d, const int* anc, float cx, float c
         evals += n1d;
         F.add(v * (ny * invh));
     } else {
+        // psi at the centroid; on an unmoved y-face (the zero-velocity pass) the centroid lies
+        // on a psi node row
         const float qp[3] = {cx, cy, cz};
-        F.add(interp_loc(d.interp, pl, d.P, anc, qp) * (ny * invh));
-        if (d.interp == INTERP_WENO6) evals += 43;
+        float v;
+        const int n1d = d.interp == INTERP_WENO6 ? weno6_3d_noderow(pl, d.P, anc, qp, v) : 0;
+        if (n1d == 0) {
+            v = interp_loc(d.interp, pl, d.P, anc, qp);
+            if (d.interp == INTERP_WENO6) evals += 43;
+        }
+        evals += n1d;
+        F.add(v * (ny * invh));
     }
     return evals;
 }
