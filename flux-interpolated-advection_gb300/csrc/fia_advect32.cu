@@ -675,11 +675,23 @@ static cudaError_t face_stage32(const PassDesc& d, const float* a, const float2*
     for (int fam = 0; fam < 3; ++fam)
         nface[fam] = (long long)(d.A.Mx + (fam == 0)) * (d.A.My + (fam == 1)) * (d.A.Mz + (fam == 2));
     if (std::max(nface[0], std::max(nface[1], nface[2])) >= (1LL << 29)) return cudaErrorInvalidValue;
+    // Faces at rest (the zero-velocity pass, the MacCormack face at rest): an x- or z-face keeps
+    // its four corners at one x (z), so every piece's y-normal is exactly zero and the face
+    // emits no piece; its flux, normal and volume sums are zero and only the y-faces are clipped.
+    const bool rest = d.zero_velocity != 0;
+    if (rest && !acc) {
+        for (int fam = 0; fam < 3; fam += 2) {
+            cudaMemsetAsync(w.flux[fam], 0, nface[fam] * sizeof(float2), s);
+            cudaMemsetAsync(w.flux_rev[fam], 0, nface[fam] * sizeof(float2), s);
+            if (d.volumes) cudaMemsetAsync(w.fvol[fam], 0, nface[fam] * sizeof(float2), s);
+        }
+    }
     unsigned npc = 0;
     for (int attempt = 0; attempt < 2; ++attempt) {
         cudaMemsetAsync(ps.count, 0, sizeof(unsigned), s);
         for (int fam = 0; fam < 3; ++fam)
-            k_clip32<<<nblk(nface[fam], 128), 128, 0, s>>>(d, fam, disp, ps, w.status, w.counters);
+            if (!rest || fam == 1)
+                k_clip32<<<nblk(nface[fam], 128), 128, 0, s>>>(d, fam, disp, ps, w.status, w.counters);
         cudaError_t e = cudaMemcpyAsync(&npc, ps.count, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return e;
@@ -696,9 +708,10 @@ static cudaError_t face_stage32(const PassDesc& d, const float* a, const float2*
         prof_mark(w, 1, s);
     }
     for (int fam = 0; fam < 3; ++fam)
-        k_facesum32<<<nblk(nface[fam], 256), 256, 0, s>>>(d, fam, ps, (float2*)w.flux[fam], (float2*)w.flux_rev[fam],
-                                                          w.status, wgt, acc,
-                                                          d.volumes ? (float2*)w.fvol[fam] : nullptr);
+        if (!rest || fam == 1)
+            k_facesum32<<<nblk(nface[fam], 256), 256, 0, s>>>(d, fam, ps, (float2*)w.flux[fam], (float2*)w.flux_rev[fam],
+                                                              w.status, wgt, acc,
+                                                              d.volumes ? (float2*)w.fvol[fam] : nullptr);
     return cudaGetLastError();
 }
 

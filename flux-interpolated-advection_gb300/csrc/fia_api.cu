@@ -159,9 +159,11 @@ cudaError_t reduce(fia_session* s, const void* a, long long n, int kind, bool ac
 // face-family launches (FP64), or three clips, the per-piece quadrature and three per-face
 // sums (FP32 form).
 inline unsigned pass_launches(const PassDesc& d, int precision) {
-    const bool mc = d.maccormack && !d.zero_velocity;
-    const unsigned stage = precision == FIA_FP64 ? 3u : 7u;
-    return 2u + (d.zero_velocity ? 0u : 1u) + (mc ? 3u * stage + 1u : stage);
+    // FP32 form: faces at rest clip and sum the y-faces only (the others emit no piece)
+    const unsigned stage = precision == FIA_FP64 ? 3u : 7u, rest = precision == FIA_FP64 ? 3u : 3u;
+    if (d.zero_velocity) return 2u + rest;
+    if (d.maccormack) return 4u + rest + 2u * stage;
+    return 3u + stage;
 }
 
 // Split offsets (colour = pos/h - off) per field for the main and the error-advection pass
