@@ -25,9 +25,10 @@ constexpr int kCgBatch = 16;
 // scal layout
 enum : int {
     S_ALPHA = 0, S_BETA = 1, S_RZ = 2, S_RR = 3, S_THRESH = 4, S_DONE = 5, S_ITERS = 6, S_DQ = 7,
-    S_BETAJ = 8,    // flexible CG: beta of direction slot j
-    S_DQJ = 16      // flexible CG: d.q of direction slot j
+    S_BETAJ = 8,                        // flexible CG: beta of direction slot j
+    S_DQJ = S_BETAJ + kFcgMaxDirs + 1   // flexible CG: d.q of direction slot j
 };
+static_assert(S_DQJ + kFcgMaxDirs + 1 <= kScalDoubles, "scalar block too small for the FCG direction ring");
 
 // ---------------------------------------------------------------------------------
 // per-thread dot accumulators
@@ -936,7 +937,9 @@ cudaError_t subtract_gradient_p64(const double* p64, float* u, float* v, float* 
     return cudaGetLastError();
 }
 
-size_t pressure_partials() { return (size_t)kRedBlocks * 8; }
+// partial rows: the FCG dot kernel's kFcgMaxDirs + 1 and the direction kernel's 2 (the CG
+// kernels use fewer)
+size_t pressure_partials() { return (size_t)kRedBlocks * (kFcgMaxDirs + 4); }
 
 #define FIA_PRESSURE_INST(T)                                                                                       \
     template cudaError_t pressure_rhs<T>(const PressureWork<T>&, const PoissonGrid&, double, const T*, const T*,    \

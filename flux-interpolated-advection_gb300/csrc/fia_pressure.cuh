@@ -16,9 +16,9 @@ struct PoissonGrid {
 
 // index of r.r in PressureWork::scal (read by the learned preconditioner)
 constexpr int kScalRR = 3;
-constexpr int kScalDoubles = 32;
+constexpr int kScalDoubles = 48;
 // directions kept by flexible CG (FCG(m), m <= kFcgMaxDirs)
-constexpr int kFcgMaxDirs = 4;
+constexpr int kFcgMaxDirs = 8;
 
 // ring of m+1 direction vectors d and their images q = B d (N^3 each)
 template <typename T>
