@@ -89,11 +89,18 @@ __global__ void k_backtrace32(PassDesc d, const float* __restrict__ u, const flo
         pinned = (vi <= 1 || vi >= d.N[d.comp]);
     }
     if (!pinned) {
-        // dt/h converts the velocity to cells per step
+        // dt/h converts the velocity to cells per step; at the rest position WENO6 collapses
+        // along the axes on which it lies on a node plane of the component's lattice
         const float s = d.dthf;
-        dx[0] = -interp_loc(d.interp, PlainLoad{u}, fu, anc, q) * s;
-        dx[1] = -interp_loc(d.interp, PlainLoad{v}, fv, anc, q) * s;
-        dx[2] = -interp_loc(d.interp, PlainLoad{w}, fw, anc, q) * s;
+        if (d.interp == INTERP_WENO6) {
+            dx[0] = -weno6_3d_collapse(PlainLoad{u}, fu, anc, q) * s;
+            dx[1] = -weno6_3d_collapse(PlainLoad{v}, fv, anc, q) * s;
+            dx[2] = -weno6_3d_collapse(PlainLoad{w}, fw, anc, q) * s;
+        } else {
+            dx[0] = -interp_loc(d.interp, PlainLoad{u}, fu, anc, q) * s;
+            dx[1] = -interp_loc(d.interp, PlainLoad{v}, fv, anc, q) * s;
+            dx[2] = -interp_loc(d.interp, PlainLoad{w}, fw, anc, q) * s;
+        }
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {

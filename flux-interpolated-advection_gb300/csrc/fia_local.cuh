@@ -283,6 +283,52 @@ __device__ int weno6_3d_noderow(const L& load, const NodeField& F, const int* an
     return 7;
 }
 
+// WENO6 in which every axis whose fractional offset is exactly 0 is collapsed to its centre
+// node (all candidate polynomials interpolate the node and the weights sum to one, so the pass
+// along that axis returns the node value): the vertices' rest positions lie on node planes of
+// the staggered fields along one or two axes.  Equal to weno6_3d_loc in exact arithmetic.
+template <class L>
+__device__ float weno6_3d_collapse(const L& load, const NodeField& F, const int* anc, const float* q) {
+    int bx, by, bz;
+    float sx, sy, sz;
+    locate(anc[0], q[0], F.oxf, bx, sx);
+    locate(anc[1], q[1], F.oyf, by, sy);
+    locate(anc[2], q[2], F.ozf, bz, sz);
+    const bool cxn = sx == 0.f, cyn = sy == 0.f, czn = sz == 0.f;
+    float tx[6], ty[6], tz[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        tx[i] = sx + float(2 - i);
+        ty[i] = sy + float(2 - i);
+        tz[i] = sz + float(2 - i);
+    }
+    const WenoCoef<float> cx = weno_coef(tx), cy = weno_coef(ty), cz = weno_coef(tz);
+    int kk[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) kk[i] = clampi(bz - 2 + i, F.Mz - 1);
+    const int x0 = cxn ? 2 : 0, x1 = cxn ? 3 : 6, y0 = cyn ? 2 : 0, y1 = cyn ? 3 : 6;
+    float yv[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll 1
+    for (int ix = x0; ix < x1; ++ix) {
+        const long long ii = clampi(bx - 2 + ix, F.Mx - 1);
+        float zv[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll 1
+        for (int iy = y0; iy < y1; ++iy) {
+            const long long row = F.Mz * (F.My * ii + clampi(by - 2 + iy, F.My - 1));
+            if (czn) {
+                zv[iy] = load(row + kk[2]);
+            } else {
+                float f[6];
+#pragma unroll
+                for (int iz = 0; iz < 6; ++iz) f[iz] = load(row + kk[iz]);
+                zv[iy] = weno6_call(f, cz);
+            }
+        }
+        yv[ix] = cyn ? zv[2] : weno6_call(zv, cy);
+    }
+    return cxn ? yv[2] : weno6_call(yv, cx);
+}
+
 template <class L>
 __device__ __forceinline__ float interp_loc(int method, const L& load, const NodeField& F, const int* anc,
                                             const float* q) {
