@@ -55,8 +55,10 @@ struct PieceStore {
     float* flux = nullptr;       // flux of each piece
     int2* range[3] = {nullptr, nullptr, nullptr};   // per face: start, nfwd | nrev << 15 | multi << 30
     float2* normal[3] = {nullptr, nullptr, nullptr};  // per face: y-normal sums of both clips (lower, upper cell)
-    unsigned* count = nullptr;   // device counter of pieces
+    unsigned* count = nullptr;   // device counters: [0] pieces, [1] faces listed for the local-memory clipper
+    int* deferred = nullptr;     // those faces (family << 29 | face index), room for every face
     long long cap = 0;           // pieces the buffers hold
+    int clip_fast = 1;           // 0: every face through the local-memory clipper
 };
 // (re)allocates the piece buffers for at least `pieces` pieces; ranges for `faces` per family
 cudaError_t piece_store_reserve(PieceStore& p, long long pieces, long long faces_per_family);

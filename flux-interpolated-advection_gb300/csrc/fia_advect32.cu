@@ -184,49 +184,68 @@ struct PieceSink {
     }
 };
 
-__device__ __forceinline__ void centroidf(const float* px, const float* py, int num, float& cx, float& cy, float& area) {
+// Polygon vertices (xi, eta) as two arrays, for the clipper in local memory.
+struct ArrayVerts {
+    const float* px;
+    const float* py;
+    __device__ __forceinline__ float x(int n) const { return px[n]; }
+    __device__ __forceinline__ float y(int n) const { return py[n]; }
+};
+
+template <class V>
+__device__ __forceinline__ void centroid_v(const V& v, int num, float& cx, float& cy, float& area) {
     float a = 0.f, sx = 0.f, sy = 0.f;
     for (int n = 0; n < num; ++n) {
         const int m = (n + 1 == num) ? 0 : n + 1;
-        const float c = px[n] * py[m] - px[m] * py[n];
-        a += c; sx += c * (px[n] + px[m]); sy += c * (py[n] + py[m]);
+        const float xn = v.x(n), yn = v.y(n), xm = v.x(m), ym = v.y(m);
+        const float c = xn * ym - xm * yn;
+        a += c; sx += c * (xn + xm); sy += c * (yn + ym);
     }
     a = fabsf(0.5f * a);
     if (a != 0.f) { const float s = 1.0f / (6.0f * a); cx = sx * s; cy = sy * s; }
     else {
         sx = 0.f; sy = 0.f;
-        for (int n = 0; n < num; ++n) { sx += px[n]; sy += py[n]; }
+        for (int n = 0; n < num; ++n) { sx += v.x(n); sy += v.y(n); }
         cx = sx / float(num); cy = sy / float(num);
     }
     area = a;
 }
+__device__ __forceinline__ void centroidf(const float* px, const float* py, int num, float& cx, float& cy, float& area) {
+    centroid_v(ArrayVerts{px, py}, num, cx, cy, area);
+}
 
-// 3D centroid and scaled y-normal of a piece (split_face_3D.cpp:67-93), emitted to the sink
-// unless the normal vanishes.
-__device__ void piece_geom32(const LocalFace& g, const float* px, const float* py, int num, float cxi, float ceta,
-                             PieceSink& sink, unsigned& st) {
+// 3D centroid and scaled y-normal of a piece (split_face_3D.cpp:67-93); false when the
+// normal vanishes (the piece is not emitted).
+template <class V>
+__device__ __forceinline__ bool piece_geom_v(const LocalFace& g, const V& v, int num, float cxi, float ceta,
+                                             float4& out) {
     const float cx = bilinf(g.x, cxi, ceta), cy = bilinf(g.y, cxi, ceta), cz = bilinf(g.z, cxi, ceta);
     float ny;
     if (num == 3) {
-        const float x0 = bilinf(g.x, px[0], py[0]), z0 = bilinf(g.z, px[0], py[0]);
-        const float ax = bilinf(g.x, px[1], py[1]) - x0, az = bilinf(g.z, px[1], py[1]) - z0;
-        const float bx = bilinf(g.x, px[2], py[2]) - x0, bz = bilinf(g.z, px[2], py[2]) - z0;
+        const float x0 = bilinf(g.x, v.x(0), v.y(0)), z0 = bilinf(g.z, v.x(0), v.y(0));
+        const float ax = bilinf(g.x, v.x(1), v.y(1)) - x0, az = bilinf(g.z, v.x(1), v.y(1)) - z0;
+        const float bx = bilinf(g.x, v.x(2), v.y(2)) - x0, bz = bilinf(g.z, v.x(2), v.y(2)) - z0;
         ny = 0.5f * (az * bx - ax * bz);
     } else {
         float acc = 0.f;
-        float x0 = bilinf(g.x, px[0], py[0]) - cx, z0 = bilinf(g.z, px[0], py[0]) - cz;
+        float x0 = bilinf(g.x, v.x(0), v.y(0)) - cx, z0 = bilinf(g.z, v.x(0), v.y(0)) - cz;
         const float xs = x0, zs = z0;
         for (int n = 0; n < num; ++n) {
             float x1, z1;
             if (n + 1 == num) { x1 = xs; z1 = zs; }
-            else { x1 = bilinf(g.x, px[n + 1], py[n + 1]) - cx; z1 = bilinf(g.z, px[n + 1], py[n + 1]) - cz; }
+            else { x1 = bilinf(g.x, v.x(n + 1), v.y(n + 1)) - cx; z1 = bilinf(g.z, v.x(n + 1), v.y(n + 1)) - cz; }
             acc += z0 * x1 - x0 * z1;
             x0 = x1; z0 = z1;
         }
         ny = acc * 0.5f;
     }
-    if (ny == 0.f) return;
-    sink.add(cx, cy, cz, ny, st);
+    out = make_float4(cx, cy, cz, ny);
+    return ny != 0.f;
+}
+__device__ void piece_geom32(const LocalFace& g, const float* px, const float* py, int num, float cxi, float ceta,
+                             PieceSink& sink, unsigned& st) {
+    float4 p;
+    if (piece_geom_v(g, ArrayVerts{px, py}, num, cxi, ceta, p)) sink.add(p.x, p.y, p.z, p.w, st);
 }
 
 // The quadrature of one piece (polygon_3D.cpp:257-487): density points on the y-interval
@@ -348,6 +367,18 @@ __device__ void emit32(const PassDesc& d, const LocalFace& g, const float* px, c
 
 constexpr int kPool32 = 144, kMaxV32 = 32, kStack32 = 48;
 
+// The point where edge a -> b crosses the iso-line (v0, v1: the edge ends' cut coordinate
+// minus the iso value, of opposite signs); returns the edge parameter t1 of b.
+__device__ __forceinline__ float cross_point(const CVf& a, const CVf& b, float v0, float v1, float iso, int dim, CVf& X) {
+    const float inv = 1.0f / (v1 - v0);
+    const float t0 = v1 * inv, t1 = -v0 * inv;
+    X.p0 = t0 * a.p0 + t1 * b.p0;
+    X.p1 = t0 * a.p1 + t1 * b.p1;
+    const float other = snap_int(t0 * cvc(a, 1 - dim) + t1 * cvc(b, 1 - dim));
+    if (dim == 0) { X.c0 = iso; X.c1 = other; } else { X.c1 = iso; X.c0 = other; }
+    return t1;
+}
+
 // The clipper of fia_advect.cu (facecutter.h:59-224) on local colours.
 __device__ void clip32(const PassDesc& d, const LocalFace& g, unsigned& st, int& npieces, bool& multi,
                        PieceSink& sink) {
@@ -383,14 +414,9 @@ __device__ void clip32(const PassDesc& d, const LocalFace& g, unsigned& st, int&
                 const int m = (n + 1 == num) ? 0 : n + 1;
                 const float v0 = cvc(poly[n], dim) - iso, v1 = cvc(poly[m], dim) - iso;
                 if ((v0 < 0.f) != (v1 < 0.f)) {
-                    const float inv = 1.0f / (v1 - v0);
-                    const float t0 = v1 * inv, t1 = -v0 * inv;
                     cut = true;
                     CVf X;
-                    X.p0 = t0 * poly[n].p0 + t1 * poly[m].p0;
-                    X.p1 = t0 * poly[n].p1 + t1 * poly[m].p1;
-                    const float other = snap_int(t0 * cvc(poly[n], 1 - dim) + t1 * cvc(poly[m], 1 - dim));
-                    if (dim == 0) { X.c0 = iso; X.c1 = other; } else { X.c1 = iso; X.c0 = other; }
+                    const float t1 = cross_point(poly[n], poly[m], v0, v1, iso, dim, X);
                     if (slot == 0) {
                         tmp0[h0++] = X;
                         slot = 1; h1 = 0; p1start = wpos;
@@ -454,10 +480,152 @@ __device__ __forceinline__ long long psi_node(const NodeField& P, int i, int j, 
     return idx3(P, clampi(i, P.Mx - 1), clampi(j, P.My - 1), clampi(k, P.Mz - 1));
 }
 
-// Face pipeline of the chosen form, three kernels per pass:
-//  k_clip32     one thread per unique face: backtraced corners, clip (twice when an iso-line
-//               crosses a piece more than twice), pieces appended contiguously per face
-//               (warp prefix sum + one atomic per warp), y-normal sums;
+// The clipper in shared memory.  Each thread owns kFastR vertex slots (xi, eta and the two
+// colours, one word each) and kFastS stack words of the CTA's dynamic shared memory, laid
+// out word-major ([word][thread]): a warp's access to one word of its threads' slots is one
+// conflict-free wavefront however far apart the threads' polygons are, where the same pool
+// in local memory costs a line per thread and, with 36 warps per SM, is written back to
+// DRAM (about 360 bytes per face).  The pool grows upward from slot 0 and the face's pieces
+// downward from the top slot.  It is clip32 -- the same cuts, pieces, emission order and
+// arithmetic -- except that a face needing more room (about 0.2% of the faces of a developed
+// flow at CFL 2), cutting a polygon an odd number of times, or holding a piece above the
+// triangulation area returns false and is clipped again by clip32 in local memory.
+constexpr int kFastR = 26, kFastS = 6, kClipThreads = 128;
+constexpr int kFastWords = 4 * kFastR + kFastS;
+constexpr int kClipSmem = kFastWords * kClipThreads * (int)sizeof(float);   // 56,320 B: 4 CTAs per SM
+static_assert(4 * (kClipSmem + 1024) <= 233472, "four clip CTAs per SM");
+
+struct FastPool {
+    float* w;   // this thread's word 0
+    __device__ __forceinline__ float& at(int e, int c) const { return w[(4 * e + c) * kClipThreads]; }
+    __device__ __forceinline__ CVf get(int e) const { return CVf{at(e, 0), at(e, 1), at(e, 2), at(e, 3)}; }
+    __device__ __forceinline__ void put(int e, const CVf& v) const {
+        at(e, 0) = v.p0; at(e, 1) = v.p1; at(e, 2) = v.c0; at(e, 3) = v.c1;
+    }
+    __device__ __forceinline__ unsigned& stk(int i) const {
+        return reinterpret_cast<unsigned*>(w)[(4 * kFastR + i) * kClipThreads];
+    }
+};
+struct PoolVerts {
+    FastPool P;
+    int s;
+    __device__ __forceinline__ float x(int n) const { return P.at(s + n, 0); }
+    __device__ __forceinline__ float y(int n) const { return P.at(s + n, 1); }
+};
+__device__ __forceinline__ unsigned stack_word(int start, int num, int dim) {
+    return (unsigned)start | ((unsigned)num << 8) | ((unsigned)dim << 16);
+}
+
+// One clip of a face (facecutter.h:59-224) in the shared pool.  nst pieces are stored so far
+// (slot kFastR - 1 - q holds piece q as cx, cy, cz, ny); ny sums the y-normals of this clip.
+__device__ bool clip32_fast(const PassDesc& d, const LocalFace& g, int& npieces, bool& multi, int& nst, Kahan& ny,
+                            const FastPool& P) {
+    if (4 > kFastR - nst) return false;
+    const float xi[4] = {0.f, 1.f, 1.f, 0.f}, eta[4] = {0.f, 0.f, 1.f, 1.f};
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        P.put(q, CVf{xi[q], eta[q], snap_int(g.x[q] - d.color_off_f[0]), snap_int(g.z[q] - d.color_off_f[1])});
+    P.stk(0) = stack_word(0, 4, 0);
+    int sp = 1;
+    const float minA = d.minimal_area_f;
+    while (sp > 0) {
+        --sp;
+        const unsigned e = P.stk(sp);
+        const int pstart = (int)(e & 0xffu), num = (int)((e >> 8) & 0xffu), dim = (int)(e >> 16);
+        const int cc = 2 + dim;
+        float mn = P.at(pstart, cc), mx = mn;
+        for (int n = 1; n < num; ++n) { const float c = P.at(pstart + n, cc); mn = fminf(mn, c); mx = fmaxf(mx, c); }
+        int start = (int)ceilf(mn), end = (int)floorf(mx);
+        if (mn - float(start) == 0.f) start += 1;
+        if (mx - float(end) == 0.f) end -= 1;
+        bool cut = false;
+        if (start <= end) {
+            const float iso = float(start);
+            // the crossings bound what the cut writes: the parts away from vertex 0 (at most
+            // num - 1 + ncross vertices) from pstart + num, the part holding vertex 0 (at most
+            // num + ncross) from b0, after them
+            int ncross = 0;
+            bool sprev = (P.at(pstart + num - 1, cc) - iso) < 0.f;
+            for (int n = 0; n < num; ++n) {
+                const bool sn = (P.at(pstart + n, cc) - iso) < 0.f;
+                ncross += sn != sprev ? 1 : 0;
+                sprev = sn;
+            }
+            const int b0 = pstart + 2 * num - 1 + ncross;
+            if (b0 + num + ncross > kFastR - nst) return false;
+            int h0 = 0, h1 = 0, slot = 0, wpos = pstart + num, p1start = wpos, nchild = 0;
+            const CVf V0 = P.get(pstart);
+            CVf A = V0;
+            P.put(b0 + h0++, V0);
+            for (int n = 0; n < num; ++n) {
+                const CVf B = (n + 1 == num) ? V0 : P.get(pstart + n + 1);
+                const float v0 = cvc(A, dim) - iso, v1 = cvc(B, dim) - iso;
+                if ((v0 < 0.f) != (v1 < 0.f)) {
+                    cut = true;
+                    CVf X;
+                    const float t1 = cross_point(A, B, v0, v1, iso, dim, X);
+                    if (slot == 0) {
+                        P.put(b0 + h0++, X);
+                        slot = 1; h1 = 0; p1start = wpos;
+                        if (t1 < 1.0f) P.put(p1start + h1++, X);
+                    } else {
+                        P.put(p1start + h1++, X);
+                        // the part is complete: pushed where it lands after the parent is dropped
+                        if (sp >= kFastS) return false;
+                        P.stk(sp++) = stack_word(p1start - num, h1, dim);
+                        ++nchild;
+                        wpos = p1start + h1;
+                        slot = 0;
+                        if (t1 < 1.0f) P.put(b0 + h0++, X);
+                    }
+                }
+                if (n < num - 1) {
+                    if (slot == 0) P.put(b0 + h0++, B);
+                    else P.put(p1start + h1++, B);
+                }
+                A = B;
+            }
+            if (nchild > 1) multi = true;
+            if (cut) {
+                if (slot != 0 || sp >= kFastS) return false;
+                // drop the parent: the parts move down by num, the part of vertex 0 follows them
+                for (int q = pstart + num; q < wpos; ++q) P.put(q - num, P.get(q));
+                for (int q = 0; q < h0; ++q) P.put(wpos - num + q, P.get(b0 + q));
+                P.stk(sp++) = stack_word(wpos - num, h0, dim);
+            }
+        }
+        if (!cut) {
+            if (dim == 0) {
+                if (sp >= kFastS) return false;
+                P.stk(sp++) = stack_word(pstart, num, 1);
+            } else if (num >= 3) {
+                const PoolVerts V{P, pstart};
+                float cx, cy, area;
+                centroid_v(V, num, cx, cy, area);
+                if (area > minA) return false;      // triangulated by clip32
+                if (area != 0.f) {
+                    ++npieces;
+                    float4 pc;
+                    if (piece_geom_v(g, V, num, cx, cy, pc)) {
+                        ny.add(pc.w);
+                        const int slotp = kFastR - 1 - nst;
+                        if (slotp < pstart) return false;   // the polygon above pstart is spent
+                        P.at(slotp, 0) = pc.x; P.at(slotp, 1) = pc.y; P.at(slotp, 2) = pc.z; P.at(slotp, 3) = pc.w;
+                        ++nst;
+                    }
+                }
+            }
+        }
+    }
+    return true;
+}
+
+// Face pipeline of the chosen form, per pass:
+//  k_clip32     one thread per unique face: backtraced corners, clip in shared memory (twice
+//               when an iso-line crosses a piece more than twice), pieces appended
+//               contiguously per face (warp prefix sum + one atomic per warp), y-normal sums;
+//               a face the shared pool cannot hold goes to a list
+//  k_clip32_deferred  the listed faces, clipped in local memory, appended the same way
 //  k_quad32     one thread per piece: quadrature + WENO6 (uniform work per thread, no clip
 //               code, so fewer registers and no divergence from the piece count);
 //  k_facesum32  one thread per face: compensated sum of its pieces in emission order.
@@ -468,55 +636,39 @@ __device__ __forceinline__ void face_of(int fam, const NodeField& A, long long i
     i = (int)(id / ((long long)Fz * Fy));
 }
 
-__global__ void __launch_bounds__(128) k_clip32(PassDesc d, int fam, const float* __restrict__ disp, PieceStore ps,
-                                                unsigned* status, unsigned long long* counters) {
-    const int Fx = d.A.Mx + (fam == 0), Fy = d.A.My + (fam == 1), Fz = d.A.Mz + (fam == 2);
-    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long nface = (long long)Fx * Fy * Fz;
-    const int lane = threadIdx.x & 31;
-    unsigned st = 0;
-    int npieces = 0, nmulti = 0;
-    PieceSink sink;
-    int nfwd = 0;
-    bool multi = false;
-    if (id < nface) {
-        int i, j, k;
-        face_of(fam, d.A, id, i, j, k);
-        int ci[4], cj[4], ck[4];
-        corners(fam, i, j, k, ci, cj, ck);
-        LocalFace g;
-        g.anc[0] = i; g.anc[1] = j; g.anc[2] = k;
-        const int Ly = d.A.My + 1, Lz = d.A.Mz + 1;
-        const float sx = d.comp == 0 ? -0.5f : 0.f, sy = d.comp == 1 ? -0.5f : 0.f, sz = d.comp == 2 ? -0.5f : 0.f;
-        for (int q = 0; q < 4; ++q) {
-            float dx = 0.f, dy = 0.f, dz = 0.f;
-            if (!d.zero_velocity) {
-                const long long vid = ((long long)ci[q] * Ly + cj[q]) * Lz + ck[q];
-                dx = disp[3 * vid]; dy = disp[3 * vid + 1]; dz = disp[3 * vid + 2];
-            }
-            g.x[q] = float(ci[q] - i) + sx + dx;
-            g.y[q] = float(cj[q] - j) + sy + dy;
-            g.z[q] = float(ck[q] - k) + sz + dz;
+// corners of face id of family fam, in cells relative to its anchor, backtraced by disp
+__device__ __forceinline__ void face_geometry(const PassDesc& d, int fam, long long id, const float* __restrict__ disp,
+                                              LocalFace& g) {
+    int i, j, k;
+    face_of(fam, d.A, id, i, j, k);
+    int ci[4], cj[4], ck[4];
+    corners(fam, i, j, k, ci, cj, ck);
+    g.anc[0] = i; g.anc[1] = j; g.anc[2] = k;
+    const int Ly = d.A.My + 1, Lz = d.A.Mz + 1;
+    const float sx = d.comp == 0 ? -0.5f : 0.f, sy = d.comp == 1 ? -0.5f : 0.f, sz = d.comp == 2 ? -0.5f : 0.f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        float dx = 0.f, dy = 0.f, dz = 0.f;
+        if (!d.zero_velocity) {
+            const long long vid = ((long long)ci[q] * Ly + cj[q]) * Lz + ck[q];
+            dx = disp[3 * vid]; dy = disp[3 * vid + 1]; dz = disp[3 * vid + 2];
         }
-        clip32(d, g, st, npieces, multi, sink);
-        nfwd = sink.n;
-        const float N = sink.ny.value();
-        float Nr = -N;
-        if (multi) {
-            // the upper cell's vertex order (v0, v3, v2, v1): its own pieces follow
-            LocalFace r = g;
-            r.x[1] = g.x[3]; r.y[1] = g.y[3]; r.z[1] = g.z[3];
-            r.x[3] = g.x[1]; r.y[3] = g.y[1]; r.z[3] = g.z[1];
-            int np2 = 0; bool m2 = false;
-            sink.ny = Kahan();
-            clip32(d, r, st, np2, m2, sink);
-            Nr = sink.ny.value();
-            ++nmulti;
-        }
-        ps.normal[fam][id] = make_float2(N, Nr);
+        g.x[q] = float(ci[q] - i) + sx + dx;
+        g.y[q] = float(cj[q] - j) + sy + dy;
+        g.z[q] = float(ck[q] - k) + sz + dz;
     }
-    // contiguous slots for this thread's pieces: warp prefix sum, one atomic per warp
-    const int cnt = sink.n;
+}
+
+// the upper cell's vertex order (v0, v3, v2, v1)
+__device__ __forceinline__ LocalFace reversed_face(const LocalFace& g) {
+    LocalFace r = g;
+    r.x[1] = g.x[3]; r.y[1] = g.y[3]; r.z[1] = g.z[3];
+    r.x[3] = g.x[1]; r.y[3] = g.y[1]; r.z[3] = g.z[1];
+    return r;
+}
+
+// contiguous store slots for the warp's pieces: warp prefix sum, one atomic per warp
+__device__ __forceinline__ long long warp_slots(unsigned* count, int cnt, int lane) {
     int pre = cnt;
     for (int o = 1; o < 32; o <<= 1) {
         const int t = __shfl_up_sync(0xffffffffu, pre, o);
@@ -524,20 +676,13 @@ __global__ void __launch_bounds__(128) k_clip32(PassDesc d, int fam, const float
     }
     const int total = __shfl_sync(0xffffffffu, pre, 31);
     unsigned base = 0;
-    if (lane == 31 && total > 0) base = atomicAdd(ps.count, (unsigned)total);
+    if (lane == 31 && total > 0) base = atomicAdd(count, (unsigned)total);
     base = __shfl_sync(0xffffffffu, base, 31);
-    const long long start = (long long)base + pre - cnt;
-    if (id < nface) {
-        if (start + cnt <= ps.cap) {
-            const int tag = (fam << 29) | (int)id;
-            for (int q = 0; q < cnt; ++q) { ps.rec[start + q] = sink.p[q]; ps.face[start + q] = tag; }
-        }
-        // a range beyond the capacity is kept as it is: the host sees the count, grows the
-        // store and runs the pass again
-        ps.range[fam][id] = make_int2((int)start, nfwd | ((cnt - nfwd) << 15) | ((multi ? 1 : 0) << 30));
-    }
-    unsigned long long pc = (unsigned long long)npieces;
-    unsigned fc = id < nface ? 1u : 0u, mc = (unsigned)nmulti;
+    return (long long)base + pre - cnt;
+}
+
+__device__ __forceinline__ void warp_counters(unsigned long long pc, unsigned fc, unsigned mc, unsigned st, int lane,
+                                              unsigned* status, unsigned long long* counters) {
     for (int o = 16; o > 0; o >>= 1) {
         pc += __shfl_down_sync(0xffffffffu, pc, o);
         fc += __shfl_down_sync(0xffffffffu, fc, o);
@@ -548,6 +693,107 @@ __global__ void __launch_bounds__(128) k_clip32(PassDesc d, int fam, const float
         if (fc) { atomicAdd(&counters[0], (unsigned long long)fc); atomicAdd(&counters[1], pc); }
         if (mc) atomicAdd(&counters[2], (unsigned long long)mc);
         if (st) atomicOr(status, st);
+    }
+}
+
+// fast = 0 sends every face to the list (the local-memory clipper alone)
+__global__ void __launch_bounds__(kClipThreads, 4) k_clip32(PassDesc d, int fam, const float* __restrict__ disp,
+                                                            PieceStore ps, unsigned* status,
+                                                            unsigned long long* counters, int fast) {
+    extern __shared__ float clip_smem[];
+    const FastPool P{clip_smem + threadIdx.x};
+    const int Fx = d.A.Mx + (fam == 0), Fy = d.A.My + (fam == 1), Fz = d.A.Mz + (fam == 2);
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long nface = (long long)Fx * Fy * Fz;
+    const int lane = threadIdx.x & 31;
+    int npieces = 0, nst = 0, nfwd = 0;
+    bool multi = false, ok = false;
+    if (id < nface) {
+        LocalFace g;
+        face_geometry(d, fam, id, disp, g);
+        Kahan ny;
+        ok = fast != 0 && clip32_fast(d, g, npieces, multi, nst, ny, P);
+        float N = 0.f, Nr = 0.f;
+        if (ok) {
+            nfwd = nst;
+            N = ny.value();
+            Nr = -N;
+            if (multi) {
+                ny = Kahan();
+                int np2 = 0;
+                bool m2 = false;
+                ok = clip32_fast(d, reversed_face(g), np2, m2, nst, ny, P);
+                Nr = ny.value();
+            }
+        }
+        if (ok) {
+            ps.normal[fam][id] = make_float2(N, Nr);
+        } else {
+            const unsigned q = atomicAdd(ps.count + 1, 1u);
+            ps.deferred[q] = (fam << 29) | (int)id;
+            npieces = 0; nst = 0; multi = false;
+        }
+    }
+    const int cnt = nst;
+    const long long start = warp_slots(ps.count, cnt, lane);
+    if (ok) {
+        if (start + cnt <= ps.cap) {
+            const int tag = (fam << 29) | (int)id;
+            for (int q = 0; q < cnt; ++q) {
+                const int e = kFastR - 1 - q;
+                ps.rec[start + q] = make_float4(P.at(e, 0), P.at(e, 1), P.at(e, 2), P.at(e, 3));
+                ps.face[start + q] = tag;
+            }
+        }
+        // a range beyond the capacity is kept as it is: the host sees the count, grows the
+        // store and runs the pass again
+        ps.range[fam][id] = make_int2((int)start, nfwd | ((cnt - nfwd) << 15) | ((multi ? 1 : 0) << 30));
+    }
+    warp_counters((unsigned long long)npieces, ok ? 1u : 0u, (ok && multi) ? 1u : 0u, 0u, lane, status, counters);
+}
+
+// The faces k_clip32 listed (all families), clipped by clip32 in local memory; grid-stride
+// over the list length the clip kernels left in ps.count[1].
+__global__ void __launch_bounds__(128) k_clip32_deferred(PassDesc d, const float* __restrict__ disp, PieceStore ps,
+                                                         unsigned* status, unsigned long long* counters) {
+    const long long nd = (long long)ps.count[1];
+    const int lane = threadIdx.x & 31;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && nd > 0) atomicAdd(&counters[4], (unsigned long long)nd);
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < nd; base += (long long)gridDim.x * blockDim.x) {
+        const long long t = base + threadIdx.x;
+        const bool valid = t < nd;
+        const int tag = valid ? ps.deferred[t] : 0;
+        const int fam = tag >> 29;
+        const long long id = tag & ((1 << 29) - 1);
+        unsigned st = 0;
+        int npieces = 0, nmulti = 0, nfwd = 0;
+        bool multi = false;
+        PieceSink sink;
+        if (valid) {
+            LocalFace g;
+            face_geometry(d, fam, id, disp, g);
+            clip32(d, g, st, npieces, multi, sink);
+            nfwd = sink.n;
+            const float N = sink.ny.value();
+            float Nr = -N;
+            if (multi) {
+                int np2 = 0;
+                bool m2 = false;
+                sink.ny = Kahan();
+                clip32(d, reversed_face(g), st, np2, m2, sink);
+                Nr = sink.ny.value();
+                ++nmulti;
+            }
+            ps.normal[fam][id] = make_float2(N, Nr);
+        }
+        const int cnt = sink.n;
+        const long long start = warp_slots(ps.count, cnt, lane);
+        if (valid) {
+            if (start + cnt <= ps.cap)
+                for (int q = 0; q < cnt; ++q) { ps.rec[start + q] = sink.p[q]; ps.face[start + q] = tag; }
+            ps.range[fam][id] = make_int2((int)start, nfwd | ((cnt - nfwd) << 15) | ((multi ? 1 : 0) << 30));
+        }
+        warp_counters((unsigned long long)npieces, valid ? 1u : 0u, (unsigned)nmulti, st, lane, status, counters);
     }
 }
 
@@ -694,11 +940,17 @@ static cudaError_t face_stage32(const PassDesc& d, const float* a, const float2*
         }
     }
     unsigned npc = 0;
+    cudaError_t ea = cudaFuncSetAttribute(k_clip32, cudaFuncAttributeMaxDynamicSharedMemorySize, kClipSmem);
+    if (ea == cudaSuccess)
+        ea = cudaFuncSetAttribute(k_clip32, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    if (ea != cudaSuccess) return ea;
     for (int attempt = 0; attempt < 2; ++attempt) {
-        cudaMemsetAsync(ps.count, 0, sizeof(unsigned), s);
+        cudaMemsetAsync(ps.count, 0, 2 * sizeof(unsigned), s);
         for (int fam = 0; fam < 3; ++fam)
             if (!rest || fam == 1)
-                k_clip32<<<nblk(nface[fam], 128), 128, 0, s>>>(d, fam, disp, ps, w.status, w.counters);
+                k_clip32<<<nblk(nface[fam], kClipThreads), kClipThreads, kClipSmem, s>>>(d, fam, disp, ps, w.status,
+                                                                                         w.counters, ps.clip_fast);
+        k_clip32_deferred<<<152 * 8, 128, 0, s>>>(d, disp, ps, w.status, w.counters);
         cudaError_t e = cudaMemcpyAsync(&npc, ps.count, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return e;
@@ -776,7 +1028,7 @@ cudaError_t piece_store_reserve(PieceStore& p, long long pieces, long long faces
         p.cap = pieces;
     }
     if (!p.count) {
-        cudaError_t e = cudaMalloc(&p.count, sizeof(unsigned));
+        cudaError_t e = cudaMalloc(&p.count, 2 * sizeof(unsigned));
         if (e != cudaSuccess) return e;
     }
     if (!p.range[0]) {
@@ -785,12 +1037,14 @@ cudaError_t piece_store_reserve(PieceStore& p, long long pieces, long long faces
             if (e == cudaSuccess) e = cudaMalloc(&p.normal[f], faces_per_family * sizeof(float2));
             if (e != cudaSuccess) return e;
         }
+        cudaError_t e = cudaMalloc(&p.deferred, 3 * faces_per_family * sizeof(int));
+        if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
 }
 
 void piece_store_free(PieceStore& p) {
-    cudaFree(p.rec); cudaFree(p.face); cudaFree(p.flux); cudaFree(p.count);
+    cudaFree(p.rec); cudaFree(p.face); cudaFree(p.flux); cudaFree(p.count); cudaFree(p.deferred);
     for (int f = 0; f < 3; ++f) { cudaFree(p.range[f]); cudaFree(p.normal[f]); }
     p = PieceStore();
 }

@@ -23,7 +23,7 @@ struct fia_session {
     int last_status;
     bool status_pending;
     bool counters_pending;
-    unsigned long long counters_host[4];
+    unsigned long long counters_host[5];
     unsigned long long launches;   // kernels launched by this session (host-side count)
     std::vector<cudaEvent_t> prof_ev;   // face-kernel timing (fia_profile_faces)
     int prof_n;
@@ -160,7 +160,7 @@ cudaError_t reduce(fia_session* s, const void* a, long long n, int kind, bool ac
 // sums (FP32 form).
 inline unsigned pass_launches(const PassDesc& d, int precision) {
     // FP32 form: faces at rest clip and sum the y-faces only (the others emit no piece)
-    const unsigned stage = precision == FIA_FP64 ? 3u : 7u, rest = precision == FIA_FP64 ? 3u : 3u;
+    const unsigned stage = precision == FIA_FP64 ? 3u : 8u, rest = precision == FIA_FP64 ? 3u : 4u;
     if (d.zero_velocity) return 2u + rest;
     if (d.maccormack) return 4u + rest + 2u * stage;
     return 3u + stage;
@@ -913,7 +913,7 @@ fia_session* fia_create(int nx, int ny, int nz, double cell_length, int precisio
     s->N[0] = nx; s->N[1] = ny; s->N[2] = nz; s->h = cell_length; s->precision = precision;
     s->es = precision == FIA_FP64 ? sizeof(double) : sizeof(float);
     s->last_status = 0; s->status_pending = false; s->counters_pending = false; s->launches = 0;
-    s->counters_host[0] = s->counters_host[1] = s->counters_host[2] = s->counters_host[3] = 0;
+    s->counters_host[0] = s->counters_host[1] = s->counters_host[2] = s->counters_host[3] = s->counters_host[4] = 0;
     s->pin = nx * ny * nz - 1;
     s->n_free = (long long)nx * ny * nz - 1;
     if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -942,7 +942,7 @@ fia_session* fia_create(int nx, int ny, int nz, double cell_length, int precisio
     A(t, kScalDoubles * sizeof(double)); s->scal = (double*)t;
     A(t, 8 * sizeof(double)); s->sums = (double*)t;
     A(t, sizeof(unsigned)); s->status = (unsigned*)t;
-    A(t, 4 * sizeof(unsigned long long)); s->counters = (unsigned long long*)t;
+    A(t, 5 * sizeof(unsigned long long)); s->counters = (unsigned long long*)t;
     A(t, kRedBlocks * sizeof(double)); s->red_part = (double*)t;
     A(t, 4 * sizeof(double)); s->red_out = (double*)t;
     if (ok && precision == FIA_FP32C) {
@@ -1437,8 +1437,20 @@ int fia_debug_set_piece_capacity(fia_session* s, long long pieces) {
     if (!s || s->precision != FIA_FP32C || pieces < 1) return FIA_ERR_INVALID;
     CK(cudaStreamSynchronize(s->stream));
     const long long big = (long long)(s->N[0] + 2) * (s->N[1] + 2) * (s->N[2] + 2);
+    const int fast = s->pieces.clip_fast;
     piece_store_free(s->pieces);
+    s->pieces.clip_fast = fast;
     CK(piece_store_reserve(s->pieces, pieces, big));
+    return FIA_OK;
+}
+
+int fia_debug_clip_fast(fia_session* s, int enable, unsigned long long* deferred) {
+    if (!s || s->precision != FIA_FP32C || enable < -1 || enable > 1) return FIA_ERR_INVALID;
+    if (enable >= 0) s->pieces.clip_fast = enable;
+    if (deferred) {
+        CK(cudaMemcpyAsync(deferred, s->counters + 4, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
     return FIA_OK;
 }
 

@@ -181,6 +181,7 @@ def _declare(lib):
     lib.fia_debug_unet_backward.argtypes = [vp, fp, fp, fp]
     lib.fia_debug_precondition.argtypes = [vp, fp, fp]
     lib.fia_debug_learned_tc.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_uint)]
+    lib.fia_debug_clip_fast.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_ulonglong)]
     lib.fia_debug_learned_grad.argtypes = [vp, ip, fp, dp]
     lib.fia_debug_grid_op.argtypes = [vp, ip, fp, fp]
     lib.fia_debug_solve_rhs.argtypes = [vp, fp, fp, ctypes.POINTER(SolverParams), ctypes.POINTER(SolverReport)]
@@ -481,6 +482,13 @@ class Grid3D:
         st = ctypes.c_uint(0)
         _check(self.lib.fia_debug_learned_tc(self.s, enable, ctypes.byref(st)), "fia_debug_learned_tc")
         return st.value
+
+    def debug_clip_fast(self, enable=-1):
+        """switch the face clipper's shared-memory path (1 on, 0 off, -1 leave); returns the
+        number of faces the local-memory clipper took so far"""
+        n = ctypes.c_ulonglong(0)
+        _check(self.lib.fia_debug_clip_fast(self.s, enable, ctypes.byref(n)), "fia_debug_clip_fast")
+        return n.value
 
     def debug_precondition(self, r):
         a = np.ascontiguousarray(r, dtype=np.float32).ravel()

@@ -298,6 +298,11 @@ int fia_debug_learned_grad(fia_session* s, int pair, float* grads, double* loss)
  * (on by default; off runs every layer on the mma.sync kernel), -1 leaves it; *status (if
  * not null) receives the path's error bits (bit 0: a bounded wait ran out) */
 int fia_debug_learned_tc(fia_session* s, int enable, unsigned* status);
+/* FP32 form: the face clipper's shared-memory path: enable 1 / 0 switches it on / off (on
+ * by default; off clips every face in local memory, with the same pieces), -1 leaves it;
+ * *deferred (if not null) receives the faces the local-memory clipper took since fia_create
+ * (faces the shared pool cannot hold, or all faces while the path is off). */
+int fia_debug_clip_fast(fia_session* s, int enable, unsigned long long* deferred);
 
 /* Test hooks: single pieces of the path on host data (FP64 buffers), mirroring the oracle. */
 /* one flux pass of a node field (comp -1 density, 0..2 velocity) with the session velocity */

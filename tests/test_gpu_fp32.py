@@ -160,3 +160,34 @@ def test_fp32_piece_store_grows_and_is_deterministic():
     # atomics place each face's block of pieces
     assert np.array_equal(ref, again)
     assert np.array_equal(ref, grown)
+
+
+@pytest.mark.parametrize("cfl,minimal_area", [(2.0, 1.0), (4.0, 1.0), (2.0, 0.05)])
+def test_fp32_clip_shared_pool_matches_local_pool(cfl, minimal_area):
+    """The face clipper's shared-memory path against the local-memory clipper alone: the same
+    pieces in the same order, so bit-identical fields.  At CFL 4 some faces outgrow the
+    shared pool, and at minimal area 0.05 pieces are triangulated: those faces go to the
+    local-memory clipper within the same pass."""
+    out = []
+    for fast in (1, 0):
+        g, h, u, v, w, rho, dt = make(32, fia.FIA_FP32C, seed=5, cfl=cfl)
+        n_before = g.debug_clip_fast(fast)
+        p = fia.advect_params(minimal_area=minimal_area)
+        g.move_substances_3D(dt, p)
+        g.advect_velocity_xyz_flux_advection_3D(dt, p)
+        listed = g.debug_clip_fast() - n_before
+        out.append(([g.get(c) for c in ("density", "u", "v", "w")], listed, list(g.pass_counters())))
+        g.close()
+    (f1, n1, c1), (f0, n0, c0) = out
+    for a, b in zip(f1, f0):
+        assert np.array_equal(a, b)
+    assert c1[:3] == c0[:3]     # faces, pieces, faces clipped from both sides
+    assert n0 == c0[0]          # path off: every face through the local-memory clipper
+    if minimal_area < 1.0:
+        assert 0 < n1 <= n0     # nearly every face holds a piece above 0.05 of its area
+    elif cfl > 2.0:
+        assert 0 < n1 < n0
+    else:
+        # 1.5% on GB300: at 32^3 the flow's shortest wavelength is four cells, so faces deform
+        # far more than in the 256^3 plume
+        assert n1 < 0.05 * n0
