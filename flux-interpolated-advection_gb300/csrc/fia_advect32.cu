@@ -295,7 +295,7 @@ __device__ int piece_quad32(const PassDesc& d, const int* anc, float cx, float c
         // the psi point lies on the psi node row of the y-face below the centroid
         const float qp[3] = {cx, ylo, cz};
         float v;
-        const int n1d = d.interp == INTERP_WENO6 ? weno6_3d_noderow(pl, d.P, anc, qp, v) : 0;
+        const int n1d = d.interp == INTERP_WENO6 ? weno6_3d_noderow<kQuadThreads>(pl, d.P, anc, qp, v, zs) : 0;
         if (n1d == 0) {
             v = interp_loc(d.interp, pl, d.P, anc, qp);
             if (d.interp == INTERP_WENO6) evals += 43;
@@ -307,7 +307,7 @@ __device__ int piece_quad32(const PassDesc& d, const int* anc, float cx, float c
         // on a psi node row
         const float qp[3] = {cx, cy, cz};
         float v;
-        const int n1d = d.interp == INTERP_WENO6 ? weno6_3d_noderow(pl, d.P, anc, qp, v) : 0;
+        const int n1d = d.interp == INTERP_WENO6 ? weno6_3d_noderow<kQuadThreads>(pl, d.P, anc, qp, v, zs) : 0;
         if (n1d == 0) {
             v = interp_loc(d.interp, pl, d.P, anc, qp);
             if (d.interp == INTERP_WENO6) evals += 43;
@@ -797,10 +797,10 @@ __global__ void __launch_bounds__(128) k_clip32_deferred(PassDesc d, const float
     }
 }
 
-__global__ void __launch_bounds__(kQuadThreads) k_quad32(PassDesc d, const float* __restrict__ a,
+__global__ void __launch_bounds__(kQuadThreads, 4) k_quad32(PassDesc d, const float* __restrict__ a,
                                                          const float2* __restrict__ psi, PieceStore ps, long long npc,
                                                          unsigned long long* counters) {
-    __shared__ float zcol[42 * kQuadThreads];   // each thread's z-pass column (weno6_ycolumn)
+    __shared__ float zcol[48 * kQuadThreads];   // each thread's z- and y-pass column (weno6_ycolumn)
     unsigned long long ec = 0;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < npc; t += (long long)gridDim.x * blockDim.x) {
         const float4 p = ps.rec[t];

@@ -38,6 +38,13 @@ __device__ __forceinline__ float2 weno6_call2(const float* a, const float* b, co
     return weno6_f2(a[0], a[1], a[2], a[3], a[4], a[5], b[0], b[1], b[2], b[3], b[4], b[5], w);
 }
 
+// Two evaluations with shared coefficients, inlined: for a loop whose body is one pair (the
+// z-pass of the quadrature kernel), so one copy of the code serves the whole loop and the
+// coefficients stay in registers across its iterations.
+__device__ __forceinline__ float2 weno6_pair(const float* a, const float* b, const WenoCoef<float>& w) {
+    return make_float2(weno6_eval<float, true>(a, w), weno6_eval<float, true>(b, w));
+}
+
 // error-free sum of two floats (Knuth TwoSum)
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     s = a + b;
@@ -128,8 +135,8 @@ __device__ float weno6_3d_loc(const L& load, const NodeField& F, const int* anc,
 // come from point(m, y, w) and lie in [ya, yb]; returns the number of 1D evaluations made, or
 // 0 (nothing accumulated) if [ya, yb] spans more than one cell of the field.
 // The 6 x 7 z-pass results live in shared memory, zs[(7 ix + r) * stride] (the calling
-// thread's column of a block-wide array, stride = threads per block): in registers they held
-// 42 of the face kernel's 128.
+// thread's column of a block-wide array, stride = threads per block, 48 words: in registers
+// they held 42 of the face kernel's 128), a point's six y-pass results in words 42-47.
 template <int STRIDE, class L, class P>
 __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, float qx, float qz, float ya,
                              float yb, int npts, const P& point, Kahan& acc, float* zs) {
@@ -148,20 +155,20 @@ __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, 
     int kk[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) kk[i] = clampi(bz - 2 + i, F.Mz - 1);
+    const int nr = seven ? 7 : 6;
 #pragma unroll 1
     for (int ix = 0; ix < 6; ix += 2) {
         const long long i0 = clampi(bx - 2 + ix, F.Mx - 1), i1 = clampi(bx - 1 + ix, F.Mx - 1);
         float* z0 = zs + 7 * ix * STRIDE;
         float* z1 = z0 + 7 * STRIDE;
-#pragma unroll
-        for (int r = 0; r < 7; ++r) {
-            if (r == 6 && !seven) break;
+#pragma unroll 1
+        for (int r = 0; r < nr; ++r) {
             const long long jj = clampi(by0 - 2 + r, F.My - 1);
             const long long row0 = F.Mz * (F.My * i0 + jj), row1 = F.Mz * (F.My * i1 + jj);
             float f0[6], f1[6];
 #pragma unroll
             for (int iz = 0; iz < 6; ++iz) { f0[iz] = load(row0 + kk[iz]); f1[iz] = load(row1 + kk[iz]); }
-            const float2 v = weno6_call2(f0, f1, cz);
+            const float2 v = weno6_pair(f0, f1, cz);
             z0[r * STRIDE] = v.x; z1[r * STRIDE] = v.y;
         }
     }
@@ -176,9 +183,8 @@ __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, 
 #pragma unroll
         for (int i = 0; i < 6; ++i) ty[i] = sy + float(2 - i);
         const WenoCoef<float> cy = weno_coef(ty);
-        float yv[6];
         const float* zb = zs + (up ? STRIDE : 0);
-#pragma unroll
+#pragma unroll 1
         for (int ix = 0; ix < 6; ix += 2) {
             float f0[6], f1[6];
 #pragma unroll
@@ -186,10 +192,13 @@ __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, 
                 f0[i] = zb[(7 * ix + i) * STRIDE];
                 f1[i] = zb[(7 * ix + 7 + i) * STRIDE];
             }
-            const float2 v = weno6_call2(f0, f1, cy);
-            yv[ix] = v.x; yv[ix + 1] = v.y;
+            const float2 v = weno6_pair(f0, f1, cy);
+            zs[(42 + ix) * STRIDE] = v.x; zs[(43 + ix) * STRIDE] = v.y;
         }
-        acc.add(weno6_call(yv, cx) * w);
+        float yv[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) yv[i] = zs[(42 + i) * STRIDE];
+        acc.add(weno6_eval<float, true>(yv, cx) * w);
     }
     return (seven ? 42 : 36) + 7 * npts;
 }
@@ -251,9 +260,11 @@ __device__ float lin1dy_loc(const L& load, const NodeField& F, const int* anc, c
 // polynomial of the y-pass interpolates that node and the weights sum to one, so the y-pass
 // returns the row's value: the interpolant is the (x, z) WENO6 of the row, 7 evaluations
 // instead of 43, equal to the full form in exact arithmetic.  Returns the number of 1D
-// evaluations, or 0 (out untouched) if y is not on a node row.
-template <class L>
-__device__ int weno6_3d_noderow(const L& load, const NodeField& F, const int* anc, const float* q, float& out) {
+// evaluations, or 0 (out untouched) if y is not on a node row.  The six z-pass results pass
+// through words 42-47 of the thread's shared column zs (as in weno6_ycolumn).
+template <int STRIDE, class L>
+__device__ int weno6_3d_noderow(const L& load, const NodeField& F, const int* anc, const float* q, float& out,
+                                float* zs) {
     int bx, by, bz;
     float sx, sy, sz;
     locate(anc[1], q[1], F.oyf, by, sy);
@@ -268,18 +279,20 @@ __device__ int weno6_3d_noderow(const L& load, const NodeField& F, const int* an
 #pragma unroll
     for (int i = 0; i < 6; ++i) kk[i] = clampi(bz - 2 + i, F.Mz - 1);
     const long long jj = clampi(by, F.My - 1);
-    float xv[6];
-#pragma unroll
+#pragma unroll 1
     for (int ix = 0; ix < 6; ix += 2) {
         const long long i0 = clampi(bx - 2 + ix, F.Mx - 1), i1 = clampi(bx - 1 + ix, F.Mx - 1);
         const long long row0 = F.Mz * (F.My * i0 + jj), row1 = F.Mz * (F.My * i1 + jj);
         float f0[6], f1[6];
 #pragma unroll
         for (int iz = 0; iz < 6; ++iz) { f0[iz] = load(row0 + kk[iz]); f1[iz] = load(row1 + kk[iz]); }
-        const float2 v = weno6_call2(f0, f1, cz);
-        xv[ix] = v.x; xv[ix + 1] = v.y;
+        const float2 v = weno6_pair(f0, f1, cz);
+        zs[(42 + ix) * STRIDE] = v.x; zs[(43 + ix) * STRIDE] = v.y;
     }
-    out = weno6_call(xv, cx);
+    float xv[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) xv[i] = zs[(42 + i) * STRIDE];
+    out = weno6_eval<float, true>(xv, cx);
     return 7;
 }
 
