@@ -57,6 +57,7 @@ struct PieceStore {
     float2* normal[3] = {nullptr, nullptr, nullptr};  // per face: y-normal sums of both clips (lower, upper cell)
     unsigned* count = nullptr;   // device counters: [0] pieces, [1] faces listed for the local-memory clipper
     int* deferred = nullptr;     // those faces (family << 29 | face index), room for every face
+    float4* rest = nullptr;      // the pieces of a face at rest (same for every face of a family)
     long long cap = 0;           // pieces the buffers hold
     int clip_fast = 1;           // 0: every face through the local-memory clipper
 };

@@ -495,6 +495,15 @@ constexpr int kFastWords = 4 * kFastR + kFastS;
 constexpr int kClipSmem = kFastWords * kClipThreads * (int)sizeof(float);   // 56,320 B: 4 CTAs per SM
 static_assert(4 * (kClipSmem + 1024) <= 233472, "four clip CTAs per SM");
 
+// a family's arrays of the store, selected without indexing the kernel parameter (an indexed
+// parameter array is copied to the stack frame)
+__device__ __forceinline__ int2* range_of(const PieceStore& ps, int fam) {
+    return fam == 0 ? ps.range[0] : (fam == 1 ? ps.range[1] : ps.range[2]);
+}
+__device__ __forceinline__ float2* normal_of(const PieceStore& ps, int fam) {
+    return fam == 0 ? ps.normal[0] : (fam == 1 ? ps.normal[1] : ps.normal[2]);
+}
+
 struct FastPool {
     float* w;   // this thread's word 0
     __device__ __forceinline__ float& at(int e, int c) const { return w[(4 * e + c) * kClipThreads]; }
@@ -727,7 +736,7 @@ __global__ void __launch_bounds__(kClipThreads, 4) k_clip32(PassDesc d, int fam,
             }
         }
         if (ok) {
-            ps.normal[fam][id] = make_float2(N, Nr);
+            normal_of(ps, fam)[id] = make_float2(N, Nr);
         } else {
             const unsigned q = atomicAdd(ps.count + 1, 1u);
             ps.deferred[q] = (fam << 29) | (int)id;
@@ -747,7 +756,7 @@ __global__ void __launch_bounds__(kClipThreads, 4) k_clip32(PassDesc d, int fam,
         }
         // a range beyond the capacity is kept as it is: the host sees the count, grows the
         // store and runs the pass again
-        ps.range[fam][id] = make_int2((int)start, nfwd | ((cnt - nfwd) << 15) | ((multi ? 1 : 0) << 30));
+        range_of(ps, fam)[id] = make_int2((int)start, nfwd | ((cnt - nfwd) << 15) | ((multi ? 1 : 0) << 30));
     }
     warp_counters((unsigned long long)npieces, ok ? 1u : 0u, (ok && multi) ? 1u : 0u, 0u, lane, status, counters);
 }
@@ -784,17 +793,71 @@ __global__ void __launch_bounds__(128) k_clip32_deferred(PassDesc d, const float
                 Nr = sink.ny.value();
                 ++nmulti;
             }
-            ps.normal[fam][id] = make_float2(N, Nr);
+            normal_of(ps, fam)[id] = make_float2(N, Nr);
         }
         const int cnt = sink.n;
         const long long start = warp_slots(ps.count, cnt, lane);
         if (valid) {
             if (start + cnt <= ps.cap)
                 for (int q = 0; q < cnt; ++q) { ps.rec[start + q] = sink.p[q]; ps.face[start + q] = tag; }
-            ps.range[fam][id] = make_int2((int)start, nfwd | ((cnt - nfwd) << 15) | ((multi ? 1 : 0) << 30));
+            range_of(ps, fam)[id] = make_int2((int)start, nfwd | ((cnt - nfwd) << 15) | ((multi ? 1 : 0) << 30));
         }
         warp_counters((unsigned long long)npieces, valid ? 1u : 0u, (unsigned)nmulti, st, lane, status, counters);
     }
+}
+
+// Faces at rest (the zero-velocity pass, the MacCormack face at rest) are the same square in
+// every face's local coordinates, so they all have the same pieces: k_rest_clip32 clips one
+// with clip32 (one thread) into ps.rest -- [0] (count, range bits, pieces with area, status)
+// as ints, [1] (N, Nr), [2..] the pieces -- and k_rest_fill32 gives every face of the family a
+// copy, face-major (face id's pieces at id * count): the pieces, order and sums of a clip per
+// face.  Only y-faces emit pieces at rest.
+__global__ void k_rest_clip32(PassDesc d, int fam, PieceStore ps) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    LocalFace g;
+    face_geometry(d, fam, 0, nullptr, g);
+    unsigned st = 0;
+    int npieces = 0;
+    bool multi = false;
+    PieceSink sink;
+    clip32(d, g, st, npieces, multi, sink);
+    const int nfwd = sink.n;
+    const float N = sink.ny.value();
+    float Nr = -N;
+    if (multi) {
+        int np2 = 0;
+        bool m2 = false;
+        sink.ny = Kahan();
+        clip32(d, reversed_face(g), st, np2, m2, sink);
+        Nr = sink.ny.value();
+    }
+    reinterpret_cast<int4*>(ps.rest)[0] =
+        make_int4(sink.n, nfwd | ((sink.n - nfwd) << 15) | ((multi ? 1 : 0) << 30), npieces, (int)st);
+    ps.rest[1] = make_float4(N, Nr, 0.f, 0.f);
+    for (int q = 0; q < sink.n; ++q) ps.rest[2 + q] = sink.p[q];
+}
+
+__global__ void k_rest_fill32(PassDesc d, int fam, PieceStore ps, unsigned* status, unsigned long long* counters) {
+    const long long nface = (long long)(d.A.Mx + (fam == 0)) * (d.A.My + (fam == 1)) * (d.A.Mz + (fam == 2));
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int4 hd = reinterpret_cast<const int4*>(ps.rest)[0];
+    const int cnt = hd.x;
+    if (id == 0) {
+        atomicAdd(ps.count, (unsigned)(cnt * nface));
+        atomicAdd(&counters[0], (unsigned long long)nface);
+        atomicAdd(&counters[1], (unsigned long long)hd.z * (unsigned long long)nface);
+        if ((hd.y >> 30) & 1) atomicAdd(&counters[2], (unsigned long long)nface);
+        if (hd.w) atomicOr(status, (unsigned)hd.w);
+    }
+    if (id >= nface) return;
+    const long long start = id * cnt;
+    if (start + cnt <= ps.cap) {
+        const int tag = (fam << 29) | (int)id;
+        for (int q = 0; q < cnt; ++q) { ps.rec[start + q] = ps.rest[2 + q]; ps.face[start + q] = tag; }
+    }
+    range_of(ps, fam)[id] = make_int2((int)start, hd.y);
+    const float4 nr = ps.rest[1];
+    normal_of(ps, fam)[id] = make_float2(nr.x, nr.y);
 }
 
 __global__ void __launch_bounds__(kQuadThreads, 4) k_quad32(PassDesc d, const float* __restrict__ a,
@@ -827,14 +890,14 @@ __global__ void k_facesum32(PassDesc d, int fam, PieceStore ps, float2* __restri
     const long long nface = (long long)(d.A.Mx + (fam == 0)) * (d.A.My + (fam == 1)) * (d.A.Mz + (fam == 2));
     const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= nface) return;
-    const int2 r = ps.range[fam][id];
+    const int2 r = range_of(ps, fam)[id];
     const int nf = r.y & 0x7fff, nr = (r.y >> 15) & 0x7fff;
     const bool multi = (r.y >> 30) & 1;
     Kahan F, Fr;
     for (int q = 0; q < nf; ++q) F.add(ps.flux[(long long)r.x + q]);
     for (int q = 0; q < nr; ++q) Fr.add(ps.flux[(long long)r.x + nf + q]);
     const float f = F.value(), fr = multi ? Fr.value() : -f;
-    const float2 nrm = ps.normal[fam][id];
+    const float2 nrm = normal_of(ps, fam)[id];
     float2 a = make_float2(wgt * f, wgt * nrm.x), b = make_float2(wgt * fr, wgt * nrm.y);
     if (acc) {
         const float2 a0 = flux[id], b0 = flux_rev[id];
@@ -946,11 +1009,16 @@ static cudaError_t face_stage32(const PassDesc& d, const float* a, const float2*
     if (ea != cudaSuccess) return ea;
     for (int attempt = 0; attempt < 2; ++attempt) {
         cudaMemsetAsync(ps.count, 0, 2 * sizeof(unsigned), s);
-        for (int fam = 0; fam < 3; ++fam)
-            if (!rest || fam == 1)
-                k_clip32<<<nblk(nface[fam], kClipThreads), kClipThreads, kClipSmem, s>>>(d, fam, disp, ps, w.status,
-                                                                                         w.counters, ps.clip_fast);
-        k_clip32_deferred<<<152 * 8, 128, 0, s>>>(d, disp, ps, w.status, w.counters);
+        if (rest && ps.clip_fast) {
+            k_rest_clip32<<<1, 32, 0, s>>>(d, 1, ps);
+            k_rest_fill32<<<nblk(nface[1], 256), 256, 0, s>>>(d, 1, ps, w.status, w.counters);
+        } else {
+            for (int fam = 0; fam < 3; ++fam)
+                if (!rest || fam == 1)
+                    k_clip32<<<nblk(nface[fam], kClipThreads), kClipThreads, kClipSmem, s>>>(d, fam, disp, ps, w.status,
+                                                                                             w.counters, ps.clip_fast);
+            k_clip32_deferred<<<152 * 8, 128, 0, s>>>(d, disp, ps, w.status, w.counters);
+        }
         cudaError_t e = cudaMemcpyAsync(&npc, ps.count, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return e;
@@ -1038,13 +1106,14 @@ cudaError_t piece_store_reserve(PieceStore& p, long long pieces, long long faces
             if (e != cudaSuccess) return e;
         }
         cudaError_t e = cudaMalloc(&p.deferred, 3 * faces_per_family * sizeof(int));
+        if (e == cudaSuccess) e = cudaMalloc(&p.rest, (2 + kMaxPieces32) * sizeof(float4));
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
 }
 
 void piece_store_free(PieceStore& p) {
-    cudaFree(p.rec); cudaFree(p.face); cudaFree(p.flux); cudaFree(p.count); cudaFree(p.deferred);
+    cudaFree(p.rec); cudaFree(p.face); cudaFree(p.flux); cudaFree(p.count); cudaFree(p.deferred); cudaFree(p.rest);
     for (int f = 0; f < 3; ++f) { cudaFree(p.range[f]); cudaFree(p.normal[f]); }
     p = PieceStore();
 }
