@@ -65,9 +65,13 @@ struct Kahan {
 };
 
 // Loads node values as floats: plain array, or psi pairs relative to a base pair.
+// row(i) gives a row pointer; at(row, k) the value k nodes further along the row (k a
+// compile-time constant in an unrolled loop, so one load with an immediate offset)
 struct PlainLoad {
     const float* __restrict__ a;
     __device__ __forceinline__ float operator()(long long i) const { return __ldg(a + i); }
+    __device__ __forceinline__ const float* row(long long i) const { return a + i; }
+    __device__ __forceinline__ float at(const float* p, int k) const { return __ldg(p + k); }
 };
 struct PsiLoad {
     const float2* __restrict__ a;
@@ -76,7 +80,27 @@ struct PsiLoad {
         const float2 v = __ldg(a + i);
         return (v.x - hi0) + (v.y - lo0);
     }
+    __device__ __forceinline__ const float2* row(long long i) const { return a + i; }
+    __device__ __forceinline__ float at(const float2* p, int k) const {
+        const float2 v = __ldg(p + k);
+        return (v.x - hi0) + (v.y - lo0);
+    }
 };
+
+// the six z-values of two stencil rows: row pointers and immediate offsets when the z-stencil
+// lies inside the field (zin), else the clamped indices kk
+template <class L>
+__device__ __forceinline__ void load_rows(const L& load, long long row0, long long row1, bool zin, int bz,
+                                          const int* kk, float* f0, float* f1) {
+    if (zin) {
+        const auto p0 = load.row(row0 + bz - 2), p1 = load.row(row1 + bz - 2);
+#pragma unroll
+        for (int iz = 0; iz < 6; ++iz) { f0[iz] = load.at(p0, iz); f1[iz] = load.at(p1, iz); }
+    } else {
+#pragma unroll
+        for (int iz = 0; iz < 6; ++iz) { f0[iz] = load(row0 + kk[iz]); f1[iz] = load(row1 + kk[iz]); }
+    }
+}
 
 // stencil base and fractional offset of the local position along one axis
 __device__ __forceinline__ void locate(int anchor, float q, float off, int& base, float& s) {
@@ -156,6 +180,7 @@ __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, 
 #pragma unroll
     for (int i = 0; i < 6; ++i) kk[i] = clampi(bz - 2 + i, F.Mz - 1);
     const int nr = seven ? 7 : 6;
+    const bool zin = bz >= 2 && bz + 3 <= F.Mz - 1;
 #pragma unroll 1
     for (int ix = 0; ix < 6; ix += 2) {
         const long long i0 = clampi(bx - 2 + ix, F.Mx - 1), i1 = clampi(bx - 1 + ix, F.Mx - 1);
@@ -166,8 +191,7 @@ __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, 
             const long long jj = clampi(by0 - 2 + r, F.My - 1);
             const long long row0 = F.Mz * (F.My * i0 + jj), row1 = F.Mz * (F.My * i1 + jj);
             float f0[6], f1[6];
-#pragma unroll
-            for (int iz = 0; iz < 6; ++iz) { f0[iz] = load(row0 + kk[iz]); f1[iz] = load(row1 + kk[iz]); }
+            load_rows(load, row0, row1, zin, bz, kk, f0, f1);
             const float2 v = weno6_pair(f0, f1, cz);
             z0[r * STRIDE] = v.x; z1[r * STRIDE] = v.y;
         }
@@ -279,13 +303,13 @@ __device__ int weno6_3d_noderow(const L& load, const NodeField& F, const int* an
 #pragma unroll
     for (int i = 0; i < 6; ++i) kk[i] = clampi(bz - 2 + i, F.Mz - 1);
     const long long jj = clampi(by, F.My - 1);
+    const bool zin = bz >= 2 && bz + 3 <= F.Mz - 1;
 #pragma unroll 1
     for (int ix = 0; ix < 6; ix += 2) {
         const long long i0 = clampi(bx - 2 + ix, F.Mx - 1), i1 = clampi(bx - 1 + ix, F.Mx - 1);
         const long long row0 = F.Mz * (F.My * i0 + jj), row1 = F.Mz * (F.My * i1 + jj);
         float f0[6], f1[6];
-#pragma unroll
-        for (int iz = 0; iz < 6; ++iz) { f0[iz] = load(row0 + kk[iz]); f1[iz] = load(row1 + kk[iz]); }
+        load_rows(load, row0, row1, zin, bz, kk, f0, f1);
         const float2 v = weno6_pair(f0, f1, cz);
         zs[(42 + ix) * STRIDE] = v.x; zs[(43 + ix) * STRIDE] = v.y;
     }

@@ -162,17 +162,19 @@ def test_fp32_piece_store_grows_and_is_deterministic():
     assert np.array_equal(ref, grown)
 
 
-@pytest.mark.parametrize("cfl,minimal_area", [(2.0, 1.0), (4.0, 1.0), (2.0, 0.05)])
-def test_fp32_clip_shared_pool_matches_local_pool(cfl, minimal_area):
-    """The face clipper's shared-memory path against the local-memory clipper alone: the same
-    pieces in the same order, so bit-identical fields.  At CFL 4 some faces outgrow the
-    shared pool, and at minimal area 0.05 pieces are triangulated: those faces go to the
-    local-memory clipper within the same pass."""
+@pytest.mark.parametrize("cfl,minimal_area,maccormack", [(2.0, 1.0, False), (4.0, 1.0, False), (2.0, 0.05, False),
+                                                         (2.0, 1.0, True)])
+def test_fp32_clip_shared_pool_matches_local_pool(cfl, minimal_area, maccormack):
+    """The face clipper's shared-memory path (with one clip per family for the faces at rest)
+    against the local-memory clipper on every face: the same pieces in the same order, so
+    bit-identical fields.  At CFL 4 some faces outgrow the shared pool, and at minimal area
+    0.05 pieces are triangulated: those faces go to the local-memory clipper within the same
+    pass.  The MacCormack case adds its face at rest and its traced-back faces."""
     out = []
     for fast in (1, 0):
         g, h, u, v, w, rho, dt = make(32, fia.FIA_FP32C, seed=5, cfl=cfl)
         n_before = g.debug_clip_fast(fast)
-        p = fia.advect_params(minimal_area=minimal_area)
+        p = fia.advect_params(minimal_area=minimal_area, use_MacCormack_scheme=maccormack)
         g.move_substances_3D(dt, p)
         g.advect_velocity_xyz_flux_advection_3D(dt, p)
         listed = g.debug_clip_fast() - n_before
