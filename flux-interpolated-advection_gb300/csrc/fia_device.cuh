@@ -32,7 +32,7 @@ __device__ __forceinline__ double snap_int(double x) {
     const double tol = 8.0 * 2.220446049250313e-16 * fmax(1.0, fabs(x));
     return fabs(x - r) <= tol ? r : x;
 }
-__device__ __forceinline__ float snap_int(float x) {
+__host__ __device__ __forceinline__ float snap_int(float x) {
     const float r = rintf(x);
     const float tol = 8.0f * 1.1920928955078125e-7f * fmaxf(1.0f, fabsf(x));
     return fabsf(x - r) <= tol ? r : x;

@@ -46,7 +46,7 @@ __device__ __forceinline__ float2 weno6_pair(const float* a, const float* b, con
 }
 
 // error-free sum of two floats (Knuth TwoSum)
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+__host__ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     s = a + b;
     const float bb = s - a;
     e = (a - (s - bb)) + (b - bb);
@@ -55,13 +55,13 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
 // running sum with a compensation term
 struct Kahan {
     float s = 0.f, c = 0.f;
-    __device__ __forceinline__ void add(float x) {
+    __host__ __device__ __forceinline__ void add(float x) {
         float t, e;
         two_sum(s, x, t, e);
         s = t;
         c += e;
     }
-    __device__ __forceinline__ float value() const { return s + c; }
+    __host__ __device__ __forceinline__ float value() const { return s + c; }
 };
 
 // Loads node values as floats: plain array, or psi pairs relative to a base pair.

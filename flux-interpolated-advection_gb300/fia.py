@@ -25,7 +25,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libfia_%s.so" % platform.machine())
 SOURCES = ["fia_api.cu", "fia_advect.cu", "fia_advect32.cu", "fia_pressure.cu", "fia_noalloc.cu", "fia_unet.cu"]
-HEADERS = ["fia_device.cuh", "fia_advect.cuh", "fia_local.cuh", "fia_pressure.cuh", "fia_unet.cuh"]
+HEADERS = ["fia_device.cuh", "fia_advect.cuh", "fia_local.cuh", "fia_clip32.cuh", "fia_pressure.cuh", "fia_unet.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 FIA_OK, FIA_ERR_INVALID, FIA_ERR_CUDA, FIA_ERR_UNSUPPORTED, FIA_ERR_NOMEM = 0, -1, -2, -3, -4

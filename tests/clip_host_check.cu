@@ -1,0 +1,145 @@
+// Host check of the FP32 face clipper (csrc/fia_clip32.cuh): the shared-pool clipper
+// (clip32_fast, as k_clip32 runs it) against the local-memory clipper (clip32, as
+// k_clip32_deferred runs it) on seeded random faces, compiled for the host from the library's
+// own header.  For every face the fast clipper accepts, the pieces, their order, the
+// piece count, the both-sides flag and the y-normal sums must be bitwise equal; a slot or
+// stack word outside the shared pool stops the program (the host bounds checks of FastPool).
+//
+// Faces: the three face families and four staggerings, corners displaced by a common
+// translation of up to `cfl` cells plus a per-corner perturbation (rigid, mildly deformed,
+// strongly deformed so that polygons turn non-convex), translations rounded to half cells in a
+// share of the cases (iso-lines through vertices and edges), both colour offsets, and
+// minimal areas that triangulate pieces in a share of the cases.
+//
+// usage: clip_host_check [faces] [seed]; prints one summary line, exit status 1 on a mismatch.
+#include "../flux-interpolated-advection_gb300/csrc/fia_clip32.cuh"
+
+#include <cstdint>
+#include <cstring>
+#include <random>
+#include <vector>
+
+using namespace fia;
+
+namespace {
+
+struct Result {
+    bool ok = true;
+    int npieces = 0, n = 0, nfwd = 0;
+    bool multi = false;
+    unsigned st = 0;
+    float N = 0.f, Nr = 0.f;
+    float4 p[kMaxPieces32];
+};
+
+LocalFace make_face(std::mt19937_64& rng, int fam, int comp, float cfl, float def, bool half) {
+    std::uniform_real_distribution<float> U(-1.f, 1.f);
+    static const int cx[3][4] = {{0, 0, 0, 0}, {0, 0, 1, 1}, {0, 1, 1, 0}};
+    static const int cy[3][4] = {{0, 1, 1, 0}, {0, 0, 0, 0}, {0, 0, 1, 1}};
+    static const int cz[3][4] = {{0, 0, 1, 1}, {0, 1, 1, 0}, {0, 0, 0, 0}};
+    float T[3] = {cfl * U(rng), cfl * U(rng), cfl * U(rng)};
+    if (half)
+        for (float& t : T) t = 0.5f * std::nearbyint(2.f * t);
+    const float s[3] = {comp == 0 ? -0.5f : 0.f, comp == 1 ? -0.5f : 0.f, comp == 2 ? -0.5f : 0.f};
+    LocalFace g;
+    g.anc[0] = g.anc[1] = g.anc[2] = 0;
+    for (int q = 0; q < 4; ++q) {
+        g.x[q] = float(cx[fam][q]) + s[0] + T[0] + def * U(rng);
+        g.y[q] = float(cy[fam][q]) + s[1] + T[1] + def * U(rng);
+        g.z[q] = float(cz[fam][q]) + s[2] + T[2] + def * U(rng);
+    }
+    return g;
+}
+
+// k_clip32_deferred's sequence
+Result slow(const PassDesc& d, const LocalFace& g) {
+    Result r;
+    PieceSink sink;
+    clip32(d, g, r.st, r.npieces, r.multi, sink);
+    r.nfwd = sink.n;
+    r.N = sink.ny.value();
+    r.Nr = -r.N;
+    if (r.multi) {
+        int np2 = 0;
+        bool m2 = false;
+        sink.ny = Kahan();
+        clip32(d, reversed_face(g), r.st, np2, m2, sink);
+        r.Nr = sink.ny.value();
+    }
+    r.n = sink.n;
+    for (int q = 0; q < sink.n; ++q) r.p[q] = sink.p[q];
+    return r;
+}
+
+// k_clip32's sequence on thread 0's slice of a CTA's pool
+Result fast(const PassDesc& d, const LocalFace& g, std::vector<float>& pool) {
+    Result r;
+    const FastPool P{pool.data()};
+    Kahan ny;
+    int nst = 0;
+    r.ok = clip32_fast(d, g, r.npieces, r.multi, nst, ny, P);
+    if (r.ok) {
+        r.nfwd = nst;
+        r.N = ny.value();
+        r.Nr = -r.N;
+        if (r.multi) {
+            ny = Kahan();
+            int np2 = 0;
+            bool m2 = false;
+            r.ok = clip32_fast(d, reversed_face(g), np2, m2, nst, ny, P);
+            r.Nr = ny.value();
+        }
+    }
+    r.n = nst;
+    for (int q = 0; q < nst && r.ok; ++q) {
+        const int e = kFastR - 1 - q;
+        r.p[q] = make_float4(P.at(e, 0), P.at(e, 1), P.at(e, 2), P.at(e, 3));
+    }
+    return r;
+}
+
+bool same_bits(float a, float b) { return std::memcmp(&a, &b, sizeof(float)) == 0; }
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    const long long faces = argc > 1 ? std::atoll(argv[1]) : 200000;
+    const unsigned long long seed = argc > 2 ? std::strtoull(argv[2], nullptr, 10) : 1;
+    std::mt19937_64 rng(seed);
+    std::vector<float> pool((size_t)kFastWords * kClipThreads, 0.f);
+    long long accepted = 0, listed = 0, mismatches = 0, multi = 0, pieces = 0, flagged = 0;
+    static const float cfls[4] = {0.f, 1.f, 2.f, 4.f};
+    static const float defs[4] = {0.f, 0.02f, 0.2f, 0.8f};
+    for (long long t = 0; t < faces; ++t) {
+        PassDesc d;
+        std::memset(&d, 0, sizeof(d));
+        d.color_off_f[0] = (rng() & 1) ? 0.5f : 0.f;
+        d.color_off_f[1] = (rng() & 1) ? 0.5f : 0.f;
+        d.minimal_area_f = (rng() % 8 == 0) ? 0.05f : 1.0f;
+        const int fam = (int)(rng() % 3), comp = (int)(rng() % 4) - 1;
+        const float cfl = cfls[rng() % 4], def = defs[rng() % 4];
+        const bool half = rng() % 4 == 0;
+        const LocalFace g = make_face(rng, fam, comp, cfl, def, half);
+        const Result a = slow(d, g);
+        const Result b = fast(d, g, pool);
+        if (!b.ok) { ++listed; continue; }
+        ++accepted;
+        multi += a.multi ? 1 : 0;
+        pieces += a.n;
+        flagged += a.st != 0 ? 1 : 0;
+        bool eq = a.npieces == b.npieces && a.n == b.n && a.nfwd == b.nfwd && a.multi == b.multi && a.st == 0 &&
+                  same_bits(a.N, b.N) && same_bits(a.Nr, b.Nr);
+        for (int q = 0; eq && q < a.n; ++q)
+            eq = same_bits(a.p[q].x, b.p[q].x) && same_bits(a.p[q].y, b.p[q].y) && same_bits(a.p[q].z, b.p[q].z) &&
+                 same_bits(a.p[q].w, b.p[q].w);
+        if (!eq) {
+            if (mismatches < 5)
+                std::fprintf(stderr, "mismatch at face %lld: fam %d comp %d pieces %d/%d multi %d/%d st %u\n", t, fam,
+                             comp, a.n, b.n, (int)a.multi, (int)b.multi, a.st);
+            ++mismatches;
+        }
+    }
+    std::printf("faces %lld accepted %lld listed %lld mismatches %lld multi %lld pieces %lld flagged %lld\n", faces,
+                accepted, listed, mismatches, multi, pieces, flagged);
+    return mismatches == 0 ? 0 : 1;
+}
