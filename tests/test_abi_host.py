@@ -1,0 +1,85 @@
+"""Host-side logic of the C-ABI that runs before any device call (no GPU): parameter defaults,
+argument validation of every session entry point, grid checks of fia_create, error strings."""
+import ctypes
+import os
+import shutil
+
+import pytest
+
+pytestmark = pytest.mark.skipif(shutil.which("nvcc") is None and not os.path.exists("/usr/local/cuda/bin/nvcc"),
+                                reason="nvcc not available")
+
+fia = pytest.importorskip("fia")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    fia.build()
+    return fia.load()
+
+
+def test_default_advect_params_match_the_python_defaults(lib):
+    c = fia.AdvectParams()
+    lib.fia_default_advect_params(ctypes.byref(c))
+    py = fia.advect_params()
+    for name, _ in fia.AdvectParams._fields_:
+        assert getattr(c, name) == getattr(py, name), name
+    # the benchmark's settings: WENO6, cell-face-aligned split, k = 3, y-integral, zero-velocity
+    # correction, no MacCormack, no volume correction, no triangulation
+    assert (c.interpolation_method, c.split_method, c.num_gauss_quadrature_point_for_integrate_density) == (0, 0, 3)
+    assert (c.use_integral, c.enable_eliminate_zero_velocity_false_diffusion) == (1, 1)
+    assert (c.use_MacCormack_scheme, c.enable_cell_volume_correction, c.minimal_area) == (0, 0, 1.0)
+
+
+def test_default_solver_params_match_the_python_defaults(lib):
+    c = fia.SolverParams()
+    lib.fia_default_solver_params(ctypes.byref(c))
+    py = fia.solver_params()
+    for name, _ in fia.SolverParams._fields_:
+        assert getattr(c, name) == getattr(py, name), name
+
+
+def test_null_session_is_rejected_by_every_entry_point(lib):
+    p = fia.advect_params()
+    sp = fia.solver_params()
+    rep = fia.SolverReport()
+    step = fia.step_params()
+    srep = fia.StepReport()
+    d = ctypes.c_double(0.0)
+    buf = (ctypes.c_double * 8)()
+    u64 = (ctypes.c_ulonglong * 5)()
+    n = ctypes.c_ulonglong(0)
+    calls = {
+        "fia_move_substances_3D": lambda: lib.fia_move_substances_3D(None, 0.01, ctypes.byref(p)),
+        "fia_advect_velocity_xyz": lambda: lib.fia_advect_velocity_xyz(None, 0.01, ctypes.byref(p)),
+        "fia_calc_pressure_3D": lambda: lib.fia_calc_pressure_3D(None, ctypes.byref(sp), ctypes.byref(rep)),
+        "fia_calc_pressure_gradient_term_3D": lambda: lib.fia_calc_pressure_gradient_term_3D(
+            None, ctypes.byref(sp), ctypes.byref(rep)),
+        "fia_max_abs_velocity": lambda: lib.fia_max_abs_velocity(None, ctypes.byref(d)),
+        "fia_step": lambda: lib.fia_step(None, ctypes.byref(step), ctypes.byref(srep)),
+        "fia_set_field": lambda: lib.fia_set_field(None, 0, buf, fia.FIA_HOST_F64),
+        "fia_get_field": lambda: lib.fia_get_field(None, 0, buf, fia.FIA_HOST_F64),
+        "fia_pass_counters": lambda: lib.fia_pass_counters(None, u64),
+        "fia_total_momentum": lambda: lib.fia_total_momentum(None, buf),
+        "fia_write_density_frame": lambda: lib.fia_write_density_frame(None, b"/nonexistent/frame.fia", 0),
+        "fia_append_totals": lambda: lib.fia_append_totals(None, b"/nonexistent/run_", 0.0),
+        "fia_debug_clip_fast": lambda: lib.fia_debug_clip_fast(None, 1, ctypes.byref(n)),
+    }
+    for name, call in calls.items():
+        assert call() == fia.FIA_ERR_INVALID, name
+    lib.fia_destroy(None)   # a no-op
+
+
+@pytest.mark.parametrize("args", [(1, 8, 8, 0.1, 0), (8, 8, 0, 0.1, 1), (8, 8, 8, 0.0, 0), (8, 8, 8, -1.0, 1),
+                                  (8, 8, 8, 0.1, 7), (2048, 2048, 1024, 1e-3, 1)])
+def test_create_rejects_bad_grids_before_touching_the_device(lib, args):
+    nx, ny, nz, h, prec = args
+    assert not lib.fia_create(nx, ny, nz, ctypes.c_double(h), prec)
+    msg = lib.fia_error_string(fia.FIA_ERR_CUDA).decode()
+    assert msg.startswith("fia_create:")
+
+
+def test_error_strings(lib):
+    for code in (fia.FIA_OK, fia.FIA_ERR_INVALID, fia.FIA_ERR_UNSUPPORTED, fia.FIA_ERR_NOMEM, 5, -99):
+        assert lib.fia_error_string(code)
+    assert lib.fia_error_string(fia.FIA_ERR_INVALID).decode() == "invalid argument"
