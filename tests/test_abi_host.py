@@ -83,3 +83,35 @@ def test_error_strings(lib):
     for code in (fia.FIA_OK, fia.FIA_ERR_INVALID, fia.FIA_ERR_UNSUPPORTED, fia.FIA_ERR_NOMEM, 5, -99):
         assert lib.fia_error_string(code)
     assert lib.fia_error_string(fia.FIA_ERR_INVALID).decode() == "invalid argument"
+
+
+def test_noalloc_entry_point_validates_before_the_device(lib):
+    """fia_move_substances_3D_noalloc checks sizes, buffers and flags before it looks up its
+    scratch; host addresses stand in for device buffers here, none is dereferenced."""
+    f = lib.fia_move_substances_3D_noalloc
+    f.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] + [ctypes.c_void_p] * 5 + \
+        [ctypes.c_double, ctypes.POINTER(fia.AdvectParams), ctypes.c_void_p]
+    lib.fia_noalloc_error_string.restype = ctypes.c_char_p
+    a, b, u, v, w = (ctypes.addressof(x) for x in [(ctypes.c_double * 1)() for _ in range(5)])
+    p = fia.advect_params()
+
+    def call(n=(16, 16, 16), h=1.0 / 16, rho_in=a, rho_out=b, vel=(u, v, w), dt=0.01, params=p):
+        return f(*n, h, rho_in, rho_out, *vel, dt, ctypes.byref(params), None)
+
+    cases = [
+        (dict(n=(1, 16, 16)), fia.FIA_ERR_INVALID, b"bad grid"),
+        (dict(h=0.0), fia.FIA_ERR_INVALID, b"bad grid"),
+        (dict(dt=-1.0), fia.FIA_ERR_INVALID, b"time step"),
+        (dict(n=(65, 16, 16)), fia.FIA_ERR_INVALID, b"64 cells per axis"),
+        (dict(rho_in=None), fia.FIA_ERR_INVALID, b"null buffer"),
+        (dict(vel=(u, None, w)), fia.FIA_ERR_INVALID, b"null buffer"),
+        (dict(rho_out=a), fia.FIA_ERR_INVALID, b"alias"),
+        (dict(params=fia.advect_params(use_MacCormack_scheme=True)), fia.FIA_ERR_UNSUPPORTED, b"MacCormack"),
+        (dict(params=fia.advect_params(enable_cell_volume_correction=True)), fia.FIA_ERR_UNSUPPORTED, b"cell-volume"),
+        (dict(params=fia.advect_params(num_gauss_quadrature_point_for_integrate_density=2)), fia.FIA_ERR_INVALID,
+         b"invalid advection parameters"),
+        (dict(params=fia.advect_params(minimal_area=0.0)), fia.FIA_ERR_INVALID, b"invalid advection parameters"),
+    ]
+    for kw, code, why in cases:
+        assert call(**kw) == code, kw
+        assert why in lib.fia_noalloc_error_string(), kw
