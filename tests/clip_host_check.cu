@@ -12,6 +12,7 @@
 // minimal areas that triangulate pieces in a share of the cases.
 //
 // usage: clip_host_check [faces] [seed]; prints one summary line, exit status 1 on a mismatch.
+// clip_host_check dump <faces file> <pieces file>: the local-memory clipper on given faces.
 #include "../flux-interpolated-advection_gb300/csrc/fia_clip32.cuh"
 
 #include <cstdint>
@@ -102,7 +103,36 @@ bool same_bits(float a, float b) { return std::memcmp(&a, &b, sizeof(float)) == 
 
 }  // namespace
 
+// dump mode: faces from a file (per face 12 floats: x, y, z of the four corners in cells, then
+// the two colour offsets and the minimal area), the local-memory clipper's result to a file
+// (per face: int pieces, int both-sides flag, float N, float Nr, then cx, cy, cz, ny per piece)
+int dump(const char* in_path, const char* out_path) {
+    FILE* fi = std::fopen(in_path, "rb");
+    FILE* fo = std::fopen(out_path, "wb");
+    if (!fi || !fo) return 2;
+    float rec[15];
+    while (std::fread(rec, sizeof(float), 15, fi) == 15) {
+        PassDesc d;
+        std::memset(&d, 0, sizeof(d));
+        d.color_off_f[0] = rec[12];
+        d.color_off_f[1] = rec[13];
+        d.minimal_area_f = rec[14];
+        LocalFace g;
+        g.anc[0] = g.anc[1] = g.anc[2] = 0;
+        for (int q = 0; q < 4; ++q) { g.x[q] = rec[3 * q]; g.y[q] = rec[3 * q + 1]; g.z[q] = rec[3 * q + 2]; }
+        const Result r = slow(d, g);
+        const int hd[2] = {r.n, r.multi ? 1 : 0};
+        const float nn[2] = {r.N, r.Nr};
+        std::fwrite(hd, sizeof(int), 2, fo);
+        std::fwrite(nn, sizeof(float), 2, fo);
+        std::fwrite(r.p, sizeof(float4), r.n, fo);
+    }
+    std::fclose(fi);
+    return std::fclose(fo) == 0 ? 0 : 2;
+}
+
 int main(int argc, char** argv) {
+    if (argc == 4 && std::strcmp(argv[1], "dump") == 0) return dump(argv[2], argv[3]);
     const long long faces = argc > 1 ? std::atoll(argv[1]) : 200000;
     const unsigned long long seed = argc > 2 ? std::strtoull(argv[2], nullptr, 10) : 1;
     std::mt19937_64 rng(seed);

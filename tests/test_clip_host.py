@@ -42,3 +42,55 @@ def test_shared_pool_clipper_matches_local_clipper(checker, seed):
     assert f["accepted"] > 0.7 * f["faces"]
     assert f["multi"] > 0
     assert f["listed"] > 0
+
+
+def test_fp32_clipper_pieces_match_the_oracle(checker, tmp_path):
+    """The FP32 clipper's pieces (local-memory store; the shared store is bitwise equal to it,
+    above) against the FP64 oracle's split_face (the reference's facecutter restated) on seeded
+    faces of all three families, rigid and mildly deformed, up to CFL 2.  The same pieces in
+    reverse order: the kernels' explicit stack pops the last part of a cut first, the
+    reference's recursion finishes the first part first; each face's piece fluxes are summed
+    with compensation, so the order changes a flux by rounding only.  Y-normals to FP32
+    rounding; centroids to FP32 rounding where they carry weight (a sliver piece near a corner
+    has an ill-conditioned centroid and a y-normal near zero, so its error is weighted by its
+    y-normal, as in the flux it contributes to)."""
+    np = pytest.importorskip("numpy")
+    from oracle import Oracle
+    O = Oracle()
+    rng = np.random.default_rng(11)
+    corners = {0: [(0, 0, 0), (0, 1, 0), (0, 1, 1), (0, 0, 1)], 1: [(0, 0, 0), (0, 0, 1), (1, 0, 1), (1, 0, 0)],
+               2: [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0)]}
+    faces, recs = [], []
+    for t in range(3000):
+        fam = t % 3
+        T = rng.uniform(-2.0, 2.0, size=3)
+        v = np.array(corners[fam], float) + T + rng.uniform(-0.1, 0.1, size=(4, 3))
+        v = v.astype(np.float32).astype(np.float64)       # the same corners in both
+        off = (0.5, 0.5) if rng.integers(2) else (0.0, 0.0)
+        faces.append((v, off))
+        recs.append(np.concatenate([v.ravel(), off, [1.0]]).astype(np.float32))
+    fin, fout = str(tmp_path / "faces.bin"), str(tmp_path / "pieces.bin")
+    np.concatenate(recs).tofile(fin)
+    subprocess.check_call([checker, "dump", fin, fout])
+    raw = open(fout, "rb").read()
+    pos, compared, pieces = 0, 0, 0
+    for v, off in faces:
+        n, multi = np.frombuffer(raw, np.int32, 2, pos)
+        pos += 16
+        p32 = np.frombuffer(raw, np.float32, 4 * n, pos).reshape(n, 4).astype(np.float64)
+        pos += 16 * n
+        if multi:
+            continue       # clipped from both sides: the oracle's split_face returns one side
+        p64, st = O.split_face(v, 1.0, off)
+        assert st == 0
+        p64 = p64[p64[:, 4] != 0.0][::-1]        # no piece with a zero y-normal; reverse order
+        assert len(p64) == n
+        ny64 = p64[:, 4]
+        np.testing.assert_allclose(p32[:, 3], ny64, rtol=0, atol=2e-5)
+        err = np.abs(p32[:, :3] - p64[:, :3]).max(axis=1)
+        assert np.all(err * np.abs(ny64) < 1e-6)
+        assert np.all(err[np.abs(ny64) > 1e-2] < 2e-5)
+        compared += 1
+        pieces += n
+    assert pos == len(raw)
+    assert compared > 2900 and pieces > 2 * compared
