@@ -43,10 +43,12 @@ static void legendre(int n, double x, double* p, double* dp) {
 
 // Gauss-Legendre rule on [-1,1]: Newton iteration on P_k from Chebyshev-like starting
 // points; nodes ordered centre first then -/+ pairs by increasing |x| (the order of
-// gauss_quadrature_points.cpp:18-60); weights normalised to sum 1.
+// gauss_quadrature_points.cpp:18-60); weights normalised to sum 1.  Fixed arrays only (no
+// heap), so the allocation-free entry point shares it.
 void make_gauss(int k, double* x, double* w) {
-    std::vector<std::pair<double, double>> nodes;
     const double pi = 3.14159265358979323846;
+    double nx[kMaxGauss + 1], nw[kMaxGauss + 1];
+    int n = 0;
     for (int i = 0; i < (k + 1) / 2; ++i) {
         double z = std::cos(pi * (i + 0.75) / (k + 0.5));
         for (int it = 0; it < 100; ++it) {
@@ -56,14 +58,15 @@ void make_gauss(int k, double* x, double* w) {
         }
         double p, dp; legendre(k, z, &p, &dp);
         double wt = 2.0 / ((1.0 - z * z) * dp * dp);
-        if (std::fabs(z) < 1e-15) nodes.push_back({0.0, wt});
-        else { nodes.push_back({-std::fabs(z), wt}); nodes.push_back({std::fabs(z), wt}); }
+        if (std::fabs(z) < 1e-15) { nx[n] = 0.0; nw[n++] = wt; }
+        else { nx[n] = -std::fabs(z); nw[n++] = wt; nx[n] = std::fabs(z); nw[n++] = wt; }
     }
-    std::stable_sort(nodes.begin(), nodes.end(),
-                     [](const std::pair<double, double>& a, const std::pair<double, double>& b) {
-                         return std::fabs(a.first) < std::fabs(b.first);
-                     });
-    for (int i = 0; i < k; ++i) { x[i] = nodes[i].first; w[i] = nodes[i].second / 2.0; }
+    // stable insertion sort by |x|
+    for (int i = 1; i < n; ++i)
+        for (int j = i; j > 0 && std::fabs(nx[j]) < std::fabs(nx[j - 1]); --j) {
+            std::swap(nx[j], nx[j - 1]); std::swap(nw[j], nw[j - 1]);
+        }
+    for (int i = 0; i < k; ++i) { x[i] = nx[i]; w[i] = nw[i] / 2.0; }
 }
 
 NodeField cell_field(const int* N, int comp) {
@@ -400,11 +403,16 @@ __device__ T clip_face(const PassDesc& d, const FaceGeom<T>& g, const T* __restr
     unsigned char sstart[kMaxStack], snum[kMaxStack], sdim[kMaxStack];
     int sp = 0, top = 4;
     const T xi[4] = {T(0), T(1), T(1), T(0)}, eta[4] = {T(0), T(0), T(1), T(1)};
+    bool finite = true;
     for (int q = 0; q < 4; ++q) {
         pool[q].p0 = xi[q]; pool[q].p1 = eta[q];
         pool[q].c0 = snap_int(g.x[q] / h - T(d.color_off[0]));
         pool[q].c1 = snap_int(g.z[q] / h - T(d.color_off[1]));
+        finite = finite && isfinite(pool[q].c0) && isfinite(pool[q].c1) && isfinite(g.y[q]);
     }
+    // every cut narrows the range of a polygon's finite colours, which bounds the loop below;
+    // a face with a non-finite vertex (NaN or infinite velocity upstream) is not clipped
+    if (!finite) { st |= ST_NONFINITE; return T(0); }
     sstart[0] = 0; snum[0] = 4; sdim[0] = 0; sp = 1;
     T F = T(0);
     CV<T> tmp0[kMaxVerts + 2];

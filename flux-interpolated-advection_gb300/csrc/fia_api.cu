@@ -873,6 +873,12 @@ int fia_step(fia_session* s, const fia_step_params* p, fia_step_report* rep) {
 
 int fia_api_version(void) { return FIA_API_VERSION; }
 
+int fia_gauss_rule(int k, double* nodes, double* weights) {
+    if (!nodes || !weights || k < 1 || k > kMaxGauss || (k % 2) == 0) return FIA_ERR_INVALID;
+    make_gauss(k, nodes, weights);
+    return FIA_OK;
+}
+
 const char* fia_error_string(int code) {
     switch (code) {
         case FIA_OK: return "ok";

@@ -33,13 +33,25 @@ constexpr int kMaxPieces32 = 64;   // pieces of one face, both clips (CFL 4 need
 struct PieceSink {
     float4 p[kMaxPieces32];
     int n = 0;
+    bool full = false;   // a piece was dropped: the clip stops (its flux is flagged anyway)
     Kahan ny;
     __host__ __device__ __forceinline__ void add(float cx, float cy, float cz, float nyv, unsigned& st) {
         ny.add(nyv);
-        if (n >= kMaxPieces32) { st |= ST_CLIP_OVERFLOW; return; }
+        if (n >= kMaxPieces32) { st |= ST_CLIP_OVERFLOW; full = true; return; }
         p[n++] = make_float4(cx, cy, cz, nyv);
     }
 };
+
+// The clippers' loops are bounded by the colours: every cut strictly narrows the range of a
+// polygon's finite colours.  A non-finite vertex (a NaN or infinite velocity upstream) would
+// break that bound, so a face with one is not clipped: it emits no piece and is flagged.  The
+// y coordinates are checked too, so no piece with a non-finite centroid reaches the quadrature.
+__host__ __device__ __forceinline__ bool colours_finite(const float* c0, const float* c1, const float* y) {
+    bool ok = true;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) ok = ok && isfinite(c0[q]) && isfinite(c1[q]) && isfinite(y[q]);
+    return ok;
+}
 
 // Polygon vertices (xi, eta) as two arrays, for the clipper in local memory.
 struct ArrayVerts {
@@ -172,15 +184,19 @@ static __host__ __device__ void clip32(const PassDesc& d, const LocalFace& g, un
     CVf pool[kPool32];
     unsigned char sstart[kStack32], snum[kStack32], sdim[kStack32];
     const float xi[4] = {0.f, 1.f, 1.f, 0.f}, eta[4] = {0.f, 0.f, 1.f, 1.f};
+    float col0[4], col1[4];
     for (int q = 0; q < 4; ++q) {
+        col0[q] = snap_int(g.x[q] - d.color_off_f[0]);
+        col1[q] = snap_int(g.z[q] - d.color_off_f[1]);
         pool[q].p0 = xi[q]; pool[q].p1 = eta[q];
-        pool[q].c0 = snap_int(g.x[q] - d.color_off_f[0]);
-        pool[q].c1 = snap_int(g.z[q] - d.color_off_f[1]);
+        pool[q].c0 = col0[q];
+        pool[q].c1 = col1[q];
     }
+    if (!colours_finite(col0, col1, g.y)) { st |= ST_NONFINITE; return; }
     sstart[0] = 0; snum[0] = 4; sdim[0] = 0;
     int sp = 1;
     CVf tmp0[kMaxV32 + 2];
-    while (sp > 0) {
+    while (sp > 0 && !sink.full) {
         --sp;
         const int pstart = sstart[sp], num = snum[sp], dim = sdim[sp];
         const CVf* poly = pool + pstart;
@@ -308,9 +324,15 @@ static __host__ __device__ bool clip32_fast(const PassDesc& d, const LocalFace& 
                             const FastPool& P) {
     if (4 > kFastR - nst) return false;
     const float xi[4] = {0.f, 1.f, 1.f, 0.f}, eta[4] = {0.f, 0.f, 1.f, 1.f};
+    float col0[4], col1[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
-        P.put(q, CVf{xi[q], eta[q], snap_int(g.x[q] - d.color_off_f[0]), snap_int(g.z[q] - d.color_off_f[1])});
+    for (int q = 0; q < 4; ++q) {
+        col0[q] = snap_int(g.x[q] - d.color_off_f[0]);
+        col1[q] = snap_int(g.z[q] - d.color_off_f[1]);
+    }
+    if (!colours_finite(col0, col1, g.y)) return false;    // flagged by clip32
+#pragma unroll
+    for (int q = 0; q < 4; ++q) P.put(q, CVf{xi[q], eta[q], col0[q], col1[q]});
     P.stk(0) = stack_word(0, 4, 0);
     int sp = 1;
     const float minA = d.minimal_area_f;

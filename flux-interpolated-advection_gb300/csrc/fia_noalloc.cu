@@ -7,8 +7,17 @@
 // that it fails mid-run, are not acceptable.  Such a caller passes its density and velocity
 // buffers and gets the advected density back; the scratch the pass needs (psi, the
 // backtraced vertex lattice, the face fluxes, the zero-velocity correction field, the status
-// word) lives in a file-scope device array of fixed size, reserved once when the library is
-// loaded and held by every GPU that loads it until the process exits.
+// word) lives in a file-scope device array of fixed size, held by every GPU that has loaded
+// this module until the process exits.
+//
+// When the scratch is reserved: CUDA loads a module's device code lazily by default, so the
+// driver reserves the 23.6 MB on a device when this module is first used there, i.e. during
+// the first call on that device (which also looks up the array's device address).  A caller
+// whose memory budget must be settled up front makes one call at initialisation (any small
+// grid), or sets CUDA_MODULE_LOADING=EAGER so that the reservation happens when the context
+// is created; that first call must come before any stream capture.  The looked-up address
+// is kept for the life of the process: a cudaDeviceReset after the first call on a device is
+// not supported.
 //
 // Limit: at most kMaxCells cells per axis (64, i.e. up to 64^3 cells; 23.6 MB of scratch).
 // Calls share the scratch: two calls whose work overlaps on the GPU (different streams, or
@@ -62,39 +71,6 @@ int device_scratch(DeviceScratch* out) {
     }
     *out = d;
     return FIA_OK;
-}
-
-// Gauss-Legendre rule into fixed arrays (no heap): nodes centre first, then -/+ pairs by
-// increasing |x|, weights normalised to sum 1 (gauss_quadrature_points.cpp:18-60).
-void gauss_fixed(int k, double* x, double* w) {
-    const double pi = 3.14159265358979323846;
-    int n = 0;
-    double nx[kMaxGauss], nw[kMaxGauss];
-    for (int i = 0; i < (k + 1) / 2; ++i) {
-        double z = std::cos(pi * (i + 0.75) / (k + 0.5));
-        double p0 = 1.0, p1 = z, dp = 0.0;
-        for (int it = 0; it < 100; ++it) {
-            p0 = 1.0; p1 = z;
-            for (int m = 2; m <= k; ++m) { const double p2 = ((2.0 * m - 1.0) * z * p1 - (m - 1.0) * p0) / m; p0 = p1; p1 = p2; }
-            if (k == 1) { p1 = z; p0 = 1.0; }
-            dp = k * (z * p1 - p0) / (z * z - 1.0);
-            const double dz = p1 / dp;
-            z -= dz;
-            if (std::fabs(dz) < 1e-17) break;
-        }
-        p0 = 1.0; p1 = z;
-        for (int m = 2; m <= k; ++m) { const double p2 = ((2.0 * m - 1.0) * z * p1 - (m - 1.0) * p0) / m; p0 = p1; p1 = p2; }
-        dp = k * (z * p1 - p0) / (z * z - 1.0);
-        const double wt = 2.0 / ((1.0 - z * z) * dp * dp);
-        if (std::fabs(z) < 1e-15) { nx[n] = 0.0; nw[n++] = wt; }
-        else { nx[n] = -std::fabs(z); nw[n++] = wt; nx[n] = std::fabs(z); nw[n++] = wt; }
-    }
-    // stable insertion sort by |x|
-    for (int i = 1; i < n; ++i)
-        for (int j = i; j > 0 && std::fabs(nx[j]) < std::fabs(nx[j - 1]); --j) {
-            std::swap(nx[j], nx[j - 1]); std::swap(nw[j], nw[j - 1]);
-        }
-    for (int i = 0; i < k; ++i) { x[i] = nx[i]; w[i] = nw[i] / 2.0; }
 }
 
 int fail(int code, const char* msg) {
@@ -152,7 +128,7 @@ int fia_move_substances_3D_noalloc(int nx, int ny, int nz, double cell_length, c
     d.P = d.A; d.P.My = ny + 1; d.P.oy = 0.0;
     d.h = cell_length; d.dt = time_step_length;
     d.k = k;
-    gauss_fixed(k, d.gx, d.gw);
+    make_gauss(k, d.gx, d.gw);   // the session's rule (fixed arrays, no heap)
     d.minimal_area = p->minimal_area;
     static const double split_tbl[4][2] = {{0.5, 0.5}, {0.0, 0.0}, {0.5, 0.0}, {0.0, 0.5}};
 

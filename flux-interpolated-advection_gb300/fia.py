@@ -157,6 +157,7 @@ def _declare(lib):
     lib.fia_debug_flux_pass.argtypes = [vp, ip, dp, ctypes.c_double, ip, ip, ip, ip, dp, ip, ctypes.c_double, dp]
     lib.fia_debug_backtrace.argtypes = [vp, ip, ctypes.c_double, ip, dp]
     lib.fia_debug_psi.argtypes = [vp, ip, dp, ip, ip, dp]
+    lib.fia_gauss_rule.argtypes = [ip, dp, dp]
     lib.fia_default_advect_params.argtypes = [ctypes.POINTER(AdvectParams)]
     lib.fia_default_solver_params.argtypes = [ctypes.POINTER(SolverParams)]
     lib.fia_default_step_params.argtypes = [ctypes.POINTER(StepParams)]
@@ -236,6 +237,13 @@ def step_params(**kw):
         else:
             setattr(p, k, v)
     return p
+
+
+def gauss_rule(k):
+    """(nodes, weights) of the library's Gauss rule for k points per half cell (host only)"""
+    x, w = np.zeros(k), np.zeros(k)
+    _check(load().fia_gauss_rule(k, _dp(x), _dp(w)), "fia_gauss_rule")
+    return x, w
 
 
 def _dp(a):

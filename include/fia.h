@@ -13,8 +13,8 @@
  * Errors: every function returns FIA_OK (0) or a negative FIA_ERR_* code; a positive
  * return is a set of FIA_STATUS_* bits (the call completed, with numerical warnings).
  * The reference itself has no error convention (void functions, exit(0) in the face
- * clipper at facecutter.h:191-204); see INTEGRATION.md for the shim that keeps the
- * reference's void signatures.
+ * clipper at facecutter.h:191-204); the C++ shim with the reference's void signatures
+ * (fia_shim.hpp in the library's shim directory) exits on an error code.
  */
 #ifndef FIA_H
 #define FIA_H
@@ -77,7 +77,7 @@ typedef struct fia_session fia_session;
 typedef struct fia_advect_params {
     int interpolation_method;                               /* FIA_INTERP_* */
     int split_method;                                       /* FIA_SPLIT_*, density main pass */
-    int num_gauss_quadrature_point_for_integrate_density;   /* odd, 1..13 */
+    int num_gauss_quadrature_point_for_integrate_density;   /* odd, 1..15 */
     int use_integral;                                       /* y-integral quadrature (main.cpp:64) */
     int enable_eliminate_zero_velocity_false_diffusion;     /* passes 2 and 3 (main.cpp:70) */
     int use_MacCormack_scheme;                              /* flux MacCormack: each face at rest, backtraced
@@ -143,6 +143,12 @@ typedef struct fia_step_report {
     int solver_fcg_iterations;    /* flexible-CG iterations of the learned solver */
     double precond_ms;            /* device time in the learned preconditioner */
 } fia_step_report;
+
+/* The Gauss rule of the y-integral quadrature for k points per half cell (odd, 1..15; k = 1
+ * is the reference's default, main.cpp:69): nodes on [-1, 1] centre first, then -/+ pairs by
+ * increasing |x| (the order of gauss_quadrature_points.cpp:18-60), weights normalised to sum
+ * 1.  Host only (no device call). */
+int fia_gauss_rule(int k, double* nodes, double* weights);
 
 /* Reference defaults for the flags (main.cpp:48-83) with WENO6, xz-CellFaceAligned, k = 3. */
 void fia_default_advect_params(fia_advect_params* p);
@@ -236,9 +242,12 @@ int fia_calc_pressure_gradient_term_3D_host(fia_session* s, int host_dtype, void
  * FIA_ERR_INVALID; fia_noalloc_error_string says why).  density_in and density_out must be
  * distinct; stream is a cudaStream_t (NULL: the legacy default stream); the call returns
  * after the pass has finished, with FIA_STATUS_* bits or an error code.  The first call on a
- * device looks up the scratch's device address (cudaGetSymbolAddress), so make it before any
- * stream capture.  All calls share the one scratch array: calls that overlap on the GPU
- * (other streams or host threads) race on it. */
+ * device looks up the scratch's device address (cudaGetSymbolAddress), and with CUDA's default
+ * lazy module loading that is also when the driver reserves the 23.6 MB there: make one call
+ * at initialisation (or set CUDA_MODULE_LOADING=EAGER), before any stream capture.  The
+ * address is kept for the process's lifetime (no cudaDeviceReset after the first call).
+ * All calls share the one scratch array: calls that overlap on the GPU (other streams or
+ * host threads) race on it. */
 int fia_move_substances_3D_noalloc(int nx, int ny, int nz, double cell_length, const double* density_in,
                                    double* density_out, const double* u, const double* v, const double* w,
                                    double time_step_length, const fia_advect_params* p, void* stream);

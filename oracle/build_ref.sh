@@ -1,7 +1,7 @@
 #!/usr/bin/env bash
 # Builds oracle/_ref/libfia_ref_float.so and libfia_ref_double.so from the reference's
-# own hot-path sources, compiled where they lie in the reference checkout (default
-# /root/reference, override with FIA_REFERENCE_DIR), plus the self-written Eigen subset
+# own hot-path sources, compiled where they lie in the reference checkout (FIA_REFERENCE_DIR;
+# default: a directory named "reference" beside this repository), plus the self-written Eigen subset
 # (oracle/ref_shim) and the C entry points of oracle/ref_harness.cpp.
 #   float  : the reference as shipped (define_float_type.h selects float)
 #   double : the same sources seen through an include directory of symbolic links to the
@@ -10,7 +10,7 @@
 # Test infrastructure only; outputs go to oracle/_ref/ (git-ignored).
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${FIA_REFERENCE_DIR:-/root/reference}"
+REF="${FIA_REFERENCE_DIR:-$(cd "$HERE/../.." && pwd)/reference}"
 OUT="$HERE/_ref"
 if [ ! -d "$REF/src" ]; then echo "reference checkout not found at $REF" >&2; exit 2; fi
 TUS="grid_3d grid utils physical_const cell_face cell_face_3D cell_vertex cell_vertex_3D triangle_3D

@@ -13,10 +13,12 @@
 //
 // usage: clip_host_check [faces] [seed]; prints one summary line, exit status 1 on a mismatch.
 // clip_host_check dump <faces file> <pieces file>: the local-memory clipper on given faces.
+// clip_host_check status: faces that must set a status bit (non-finite, overflowing).
 #include "../flux-interpolated-advection_gb300/csrc/fia_clip32.cuh"
 
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <random>
 #include <vector>
 
@@ -131,8 +133,43 @@ int dump(const char* in_path, const char* out_path) {
     return std::fclose(fo) == 0 ? 0 : 2;
 }
 
+// status mode: faces that must set a status bit, each clipped by both stores; prints per face
+// "name st pieces fast_ok" (fast_ok: the shared-pool clipper accepted the face).  The process
+// ending at all is part of the check: no clip loop may depend on a non-finite colour.
+int status_cases() {
+    const float nan = std::numeric_limits<float>::quiet_NaN(), inf = std::numeric_limits<float>::infinity();
+    struct Case { const char* name; float x[4], y[4], z[4]; };
+    // y-faces (corners in the order of face family 1) in cells
+    const Case cases[] = {
+        {"normal", {0.3f, 0.3f, 1.3f, 1.3f}, {0.f, 0.f, 0.f, 0.f}, {0.2f, 1.2f, 1.2f, 0.2f}},
+        {"nan_x", {0.3f, 0.3f, nan, 1.3f}, {0.f, 0.f, 0.f, 0.f}, {0.2f, 1.2f, 1.2f, 0.2f}},
+        {"nan_y", {0.3f, 0.3f, 1.3f, 1.3f}, {0.f, nan, 0.f, 0.f}, {0.2f, 1.2f, 1.2f, 0.2f}},
+        {"inf_z", {0.3f, 0.3f, 1.3f, 1.3f}, {0.f, 0.f, 0.f, 0.f}, {0.2f, inf, 1.2f, 0.2f}},
+        {"neg_inf_x", {-inf, 0.3f, 1.3f, 1.3f}, {0.f, 0.f, 0.f, 0.f}, {0.2f, 1.2f, 1.2f, 0.2f}},
+        {"all_nan", {nan, nan, nan, nan}, {nan, nan, nan, nan}, {nan, nan, nan, nan}},
+        // 12 x 12 cells: 144 pieces, more than a face's piece store holds
+        {"stretched", {0.f, 0.f, 12.f, 12.f}, {0.f, 0.f, 0.f, 0.f}, {0.f, 12.f, 12.f, 0.f}},
+        // finite but absurd colours (10^7 cells): the clip stops when the store is full
+        {"huge", {0.f, 0.f, 1.e7f, 1.e7f}, {0.f, 0.f, 0.f, 0.f}, {0.f, 0.6f, 0.6f, 0.f}},
+    };
+    std::vector<float> pool((size_t)kFastWords * kClipThreads, 0.f);
+    for (const Case& c : cases) {
+        PassDesc d;
+        std::memset(&d, 0, sizeof(d));
+        d.color_off_f[0] = 0.5f; d.color_off_f[1] = 0.5f; d.minimal_area_f = 1.0f;
+        LocalFace g;
+        g.anc[0] = g.anc[1] = g.anc[2] = 0;
+        for (int q = 0; q < 4; ++q) { g.x[q] = c.x[q]; g.y[q] = c.y[q]; g.z[q] = c.z[q]; }
+        const Result a = slow(d, g);
+        const Result b = fast(d, g, pool);
+        std::printf("%s %u %d %d\n", c.name, a.st, a.n, b.ok ? 1 : 0);
+    }
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc == 4 && std::strcmp(argv[1], "dump") == 0) return dump(argv[2], argv[3]);
+    if (argc == 2 && std::strcmp(argv[1], "status") == 0) return status_cases();
     const long long faces = argc > 1 ? std::atoll(argv[1]) : 200000;
     const unsigned long long seed = argc > 2 ? std::strtoull(argv[2], nullptr, 10) : 1;
     std::mt19937_64 rng(seed);

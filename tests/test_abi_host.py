@@ -115,3 +115,29 @@ def test_noalloc_entry_point_validates_before_the_device(lib):
     for kw, code, why in cases:
         assert call(**kw) == code, kw
         assert why in lib.fia_noalloc_error_string(), kw
+
+
+@pytest.mark.parametrize("k", [1, 3, 5, 7, 9, 11, 13, 15])
+def test_gauss_rule_is_gauss_legendre_in_the_reference_order(lib, k):
+    """The one Gauss rule of the library (the session passes and the allocation-free entry
+    point both use it): Gauss-Legendre nodes and weights (numpy's leggauss, weights halved to
+    sum 1), ordered centre first then -/+ pairs by increasing |x|, and the oracle's rule."""
+    np = pytest.importorskip("numpy")
+    x, w = fia.gauss_rule(k)
+    lx, lw = np.polynomial.legendre.leggauss(k)
+    order = sorted(range(k), key=lambda i: (abs(lx[i]) if abs(lx[i]) > 1e-15 else 0.0, lx[i]))
+    np.testing.assert_allclose(x, lx[order], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(w, lw[order] / 2.0, rtol=1e-13, atol=0)
+    assert abs(w.sum() - 1.0) < 1e-14
+    from oracle import Oracle
+    ox, ow = Oracle().gauss(k)
+    np.testing.assert_allclose(x, ox, rtol=0, atol=1e-15)
+    np.testing.assert_allclose(w, ow, rtol=1e-14, atol=0)
+
+
+@pytest.mark.parametrize("k", [0, 2, 16, 17, -1])
+def test_gauss_rule_rejects_even_and_out_of_range_counts(lib, k):
+    import numpy as np
+    x = np.zeros(20); w = np.zeros(20)
+    assert lib.fia_gauss_rule(k, x.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                              w.ctypes.data_as(ctypes.POINTER(ctypes.c_double))) == fia.FIA_ERR_INVALID

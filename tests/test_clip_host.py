@@ -94,3 +94,28 @@ def test_fp32_clipper_pieces_match_the_oracle(checker, tmp_path):
         pieces += n
     assert pos == len(raw)
     assert compared > 2900 and pieces > 2 * compared
+
+
+def test_status_words_of_the_clipper(checker):
+    """The status bits that replace the reference's exit(0) in the face clipper
+    (facecutter.h:191-204) and its fixed-size arrays (facecutter.h:29), on the host:
+    a NaN or infinite vertex coordinate (a non-finite velocity upstream) gives
+    FIA_STATUS_NONFINITE and no piece, without clipping (the clip loops are bounded by the
+    range of finite colours, which such a vertex would break); a face spanning more pieces
+    than a face's store holds gives FIA_STATUS_CLIP_OVERFLOW and stops at the full store,
+    also for absurd finite colours (10^7 cells).  The shared-pool clipper hands every such
+    face to the local-memory clipper, which sets the bits.  FIA_STATUS_CLIP_ODD_CUT cannot
+    arise from these clippers' sign test (every vertex lies on one side of an iso-line, so a
+    closed polygon crosses it an even number of times); its check is defensive.  The run
+    ending within the timeout is part of the test."""
+    r = subprocess.run([checker, "status"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
+    rows = {f[0]: tuple(int(x) for x in f[1:]) for f in (line.split() for line in r.stdout.splitlines())}
+    NONFINITE, OVERFLOW = 4, 1
+    assert rows["normal"] == (0, 4, 1)
+    for name in ("nan_x", "nan_y", "inf_z", "neg_inf_x", "all_nan"):
+        st, pieces, fast_ok = rows[name]
+        assert st == NONFINITE and pieces == 0 and fast_ok == 0, (name, rows[name])
+    for name in ("stretched", "huge"):
+        st, pieces, fast_ok = rows[name]
+        assert st & OVERFLOW and pieces == 64 and fast_ok == 0, (name, rows[name])
