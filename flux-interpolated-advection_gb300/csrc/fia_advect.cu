@@ -143,6 +143,16 @@ __global__ void k_psi(PassDesc d, const T* __restrict__ a, T* __restrict__ psi) 
 // ------------------------------------------------------------------------------------
 // vertex positions
 // ------------------------------------------------------------------------------------
+// interp with WENO6 collapsed along the axes on which the point lies on a node plane of F
+// (equal in exact arithmetic; the vertices at rest and the psi points of the pieces sit there)
+// (PassDesc::full_weno switches it off, to measure what it saves)
+template <typename T>
+__device__ __forceinline__ T interp_c(const PassDesc& d, int method, const T* __restrict__ a, const NodeField& F, T h,
+                                      T px, T py, T pz) {
+    if (method == INTERP_WENO6 && !d.full_weno) return weno6_3d_collapse(a, F, h, px, py, pz);
+    return interp(method, a, F, h, px, py, pz);
+}
+
 template <typename T>
 __device__ __forceinline__ void vertex_rest_position(const PassDesc& d, int i, int j, int k, T* p) {
     const T h = T(d.h);
@@ -169,9 +179,11 @@ __global__ void k_backtrace(PassDesc d, const T* __restrict__ u, const T* __rest
         pinned = (vi <= 1 || vi >= d.N[d.comp]);
     }
     if (!pinned) {
-        const T vx = interp(d.interp, u, fu, h, p[0], p[1], p[2]);
-        const T vy = interp(d.interp, v, fv, h, p[0], p[1], p[2]);
-        const T vz = interp(d.interp, w, fw, h, p[0], p[1], p[2]);
+        // at the rest position WENO6 collapses along the axes on which the vertex lies on a node
+        // plane of the component's lattice (weno6_3d_collapse)
+        const T vx = interp_c(d, d.interp, u, fu, h, p[0], p[1], p[2]);
+        const T vy = interp_c(d, d.interp, v, fv, h, p[0], p[1], p[2]);
+        const T vz = interp_c(d, d.interp, w, fw, h, p[0], p[1], p[2]);
         const T dt = T(d.dt);
         p[0] -= vx * dt; p[1] -= vy * dt; p[2] -= vz * dt;
     }
@@ -315,23 +327,23 @@ __device__ __forceinline__ T piece_flux(const PassDesc& d, const FaceGeom<T>& g,
             const T lo = T(iy0) * h + oy, L = cy - lo;
             for (int q = 0; q < d.k; ++q) {
                 const T yq = (L / T(2)) * T(d.gx[q]) + (L / T(2)) + lo;
-                F += interp(d.interp, a, d.A, h, cx, yq, cz) * (ny * f * h * T(d.gw[q]));
+                F += interp_c(d, d.interp, a, d.A, h, cx, yq, cz) * (ny * f * h * T(d.gw[q]));
             }
         } else {
             T lo = T(iy0) * h + oy, hi = (T(iy0) + T(0.5)) * h + oy, L = hi - lo;
             for (int q = 0; q < d.k; ++q) {
                 const T yq = (L / T(2)) * T(d.gx[q]) + (L / T(2)) + lo;
-                F += interp(d.interp, a, d.A, h, cx, yq, cz) * (ny * T(0.5) * h * T(d.gw[q]));
+                F += interp_c(d, d.interp, a, d.A, h, cx, yq, cz) * (ny * T(0.5) * h * T(d.gw[q]));
             }
             lo = (T(iy0) + T(0.5)) * h + oy; hi = (T(iy0) + f) * h + oy; L = hi - lo;
             for (int q = 0; q < d.k; ++q) {
                 const T yq = (L / T(2)) * T(d.gx[q]) + (L / T(2)) + lo;
-                F += interp(d.interp, a, d.A, h, cx, yq, cz) * (ny * (f - T(0.5)) * h * T(d.gw[q]));
+                F += interp_c(d, d.interp, a, d.A, h, cx, yq, cz) * (ny * (f - T(0.5)) * h * T(d.gw[q]));
             }
         }
-        F += interp(d.interp, psi, d.P, h, cx, T(iy0) * h + oy, cz) * ny;
+        F += interp_c(d, d.interp, psi, d.P, h, cx, T(iy0) * h + oy, cz) * ny;
     } else {
-        F += interp(d.interp, psi, d.P, h, cx, cy, cz) * ny;
+        F += interp_c(d, d.interp, psi, d.P, h, cx, cy, cz) * ny;
     }
     return F;
 }

@@ -20,6 +20,7 @@ struct PassDesc {
     int zero_velocity;      // 1: faces are not moved (zero-velocity pass)
     int maccormack;         // flux MacCormack: faces at rest (0.5), backtraced (1), traced back (-0.5)
     int volumes;            // also sum y n_y of the pieces per face into PassWork::fvol (cell volumes)
+    int full_weno;          // FP64 form: evaluate every WENO6 in full (no collapse on node planes)
     double color_off[2];    // split method: colour = x/h - off0, z/h - off1
     int k;                  // Gauss points per half cell
     double gx[kMaxGauss];   // Gauss nodes on [-1,1] (centre first, then -/+ pairs)

@@ -59,6 +59,7 @@ struct fia_session {
     FcgBuffers<float> fcg{};
     bool fcg_ready = false;
     double* p64 = nullptr;       // FP32 form: pressure accumulated in FP64 by the refinement
+    int full_weno = 0;           // FP64 form: no WENO6 collapse on node planes (fia_debug_full_weno)
 };
 
 namespace {
@@ -201,6 +202,7 @@ PassDesc base_desc(const fia_session* s, int comp, double dt) {
     d.P = psi_field(d.A);
     d.h = s->h;
     d.dt = dt;
+    d.full_weno = s->full_weno;
     return d;
 }
 
@@ -1448,6 +1450,12 @@ int fia_debug_set_piece_capacity(fia_session* s, long long pieces) {
     s->pieces.clip_fast = fast;
     CK(piece_store_reserve(s->pieces, pieces, big));
     return FIA_OK;
+}
+
+int fia_debug_full_weno(fia_session* s, int enable) {
+    if (!s || enable < -1 || enable > 1) return FIA_ERR_INVALID;
+    if (enable >= 0) s->full_weno = enable;
+    return s->full_weno;
 }
 
 int fia_debug_clip_fast(fia_session* s, int enable, unsigned long long* deferred) {

@@ -165,6 +165,57 @@ __device__ T weno6_3d(const T* __restrict__ a, const NodeField& F, T h, T px, T 
     return weno6_eval(yv, cx);
 }
 
+// weno6_3d with every axis on which p lies on a node plane of F (its offset from the lattice,
+// in cells, is an integer up to the snap tolerance) collapsed to that node: every candidate
+// polynomial along such an axis interpolates the node and the weights sum to one, so the pass
+// along it returns the node's value.  Equal to weno6_3d in exact arithmetic, with fewer 1D
+// evaluations: a vertex at rest lies on node planes of the staggered velocity components
+// along one or two axes (21 evaluations instead of 129 for a density vertex), the psi point of
+// a piece lies on a node row of psi (7 instead of 43), and a face at rest has its centroid on
+// node planes.  The remaining axes use weno6_3d's arithmetic.
+template <typename T>
+__device__ T weno6_3d_collapse(const T* __restrict__ a, const NodeField& F, T h, T px, T py, T pz) {
+    const T rx = (px - T(F.ox) * h) / h, ry = (py - T(F.oy) * h) / h, rz = (pz - T(F.oz) * h) / h;
+    const T sx = snap_int(rx), sy = snap_int(ry), sz = snap_int(rz);
+    const bool cxn = sx == rint(sx), cyn = sy == rint(sy), czn = sz == rint(sz);
+    const int bx = cxn ? (int)sx : (int)floor(rx);
+    const int by = cyn ? (int)sy : (int)floor(ry);
+    const int bz = czn ? (int)sz : (int)floor(rz);
+    T tx[6], ty[6], tz[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        tx[i] = (px - (T(bx - 2 + i) + T(F.ox)) * h) / h;
+        ty[i] = (py - (T(by - 2 + i) + T(F.oy)) * h) / h;
+        tz[i] = (pz - (T(bz - 2 + i) + T(F.oz)) * h) / h;
+    }
+    const WenoCoef<T> cx = weno_coef(tx), cy = weno_coef(ty), cz = weno_coef(tz);
+    int kk[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) kk[i] = clampi(bz - 2 + i, F.Mz - 1);
+    const int x0 = cxn ? 2 : 0, x1 = cxn ? 3 : 6, y0 = cyn ? 2 : 0, y1 = cyn ? 3 : 6;
+    T yv[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+#pragma unroll 1
+    for (int ix = x0; ix < x1; ++ix) {
+        const int ii = clampi(bx - 2 + ix, F.Mx - 1);
+        T zv[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+#pragma unroll 1
+        for (int iy = y0; iy < y1; ++iy) {
+            const int jj = clampi(by - 2 + iy, F.My - 1);
+            const T* row = a + (long long)F.Mz * ((long long)F.My * ii + jj);
+            if (czn) {
+                zv[iy] = ldg(row + kk[2]);
+            } else {
+                T f[6];
+#pragma unroll
+                for (int iz = 0; iz < 6; ++iz) f[iz] = ldg(row + kk[iz]);
+                zv[iy] = weno6_eval(f, cz);
+            }
+        }
+        yv[ix] = cyn ? zv[2] : weno6_eval(zv, cy);
+    }
+    return cxn ? yv[2] : weno6_eval(yv, cx);
+}
+
 // WENO6 along y only; x and z take the node whose cell holds p
 // (WENO6_interpolation_1d.cpp:315-430).
 template <typename T>

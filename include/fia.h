@@ -312,6 +312,11 @@ int fia_debug_learned_tc(fia_session* s, int enable, unsigned* status);
  * *deferred (if not null) receives the faces the local-memory clipper took since fia_create
  * (faces the shared pool cannot hold, or all faces while the path is off). */
 int fia_debug_clip_fast(fia_session* s, int enable, unsigned long long* deferred);
+/* FP64 form: enable 1 evaluates every WENO6 interpolation in full, 0 (the default) collapses
+ * it along the axes on which the point lies on a node plane of the field (vertices at rest,
+ * psi points of the pieces: equal in exact arithmetic, fewer evaluations), -1 leaves it;
+ * returns the setting. */
+int fia_debug_full_weno(fia_session* s, int enable);
 
 /* Test hooks: single pieces of the path on host data (FP64 buffers), mirroring the oracle. */
 /* one flux pass of a node field (comp -1 density, 0..2 velocity) with the session velocity */

@@ -247,11 +247,16 @@ static real interp(int method, const Field& F, const real* p, real h) {
 //   linear  : + trilinear at 1/4 and 3/4 of the cell, times h/2  (calc_psi_3D.cpp:92-131)
 enum PsiMode { PSI_PLAIN = 0, PSI_WENO6 = 1, PSI_LINEAR = 2 };
 
-static void compute_psi(const Field& F, real h, int mode, const Gauss1D& g, std::vector<real>& psi) {
+// Columns [xlo, xhi) only (xhi < 0: all); the others stay zero (the bounded CPU baseline
+// computes the columns its cells read).
+static void compute_psi(const Field& F, real h, int mode, const Gauss1D& g, std::vector<real>& psi, int xlo = 0,
+                        int xhi = -1) {
     int Mp[3] = {F.M[0], F.M[1] + 1, F.M[2]};
     psi.assign((size_t)Mp[0] * Mp[1] * Mp[2], 0.0);
+    if (xhi < 0 || xhi > Mp[0]) xhi = Mp[0];
+    if (xlo < 0) xlo = 0;
     for (int j = 1; j < Mp[1]; ++j)
-        for (int i = 0; i < Mp[0]; ++i)
+        for (int i = xlo; i < xhi; ++i)
             for (int k = 0; k < Mp[2]; ++k) {
                 real acc = psi[idx3(Mp, i, j - 1, k)];
                 if (mode == PSI_PLAIN) {
@@ -288,7 +293,9 @@ static void compute_psi(const Field& F, real h, int mode, const Gauss1D& g, std:
 struct V2 { real p[2]; real c[2]; };
 typedef std::function<void(const real (*pts)[2], int num, const real* ctr)> PolyOut;
 
-struct ClipStatus { int overflow = 0; int odd_cut = 0; };
+// multi: some cut produced more than one part on the far side of its iso-line (the line
+// crossed the polygon more than twice), so the partition depends on the vertex order
+struct ClipStatus { int overflow = 0; int odd_cut = 0; int multi = 0; };
 
 static void cut_face_rec(const V2* poly, int num, int dim, const std::function<void(const V2*, int)>& out, ClipStatus& st) {
     real mn = 1e308, mx = -1e308;
@@ -301,7 +308,7 @@ static void cut_face_rec(const V2* poly, int num, int dim, const std::function<v
         const real iso = start;
         V2 arr[2][40];
         int head[2] = {0, 0};
-        int slot = 0;
+        int slot = 0, parts = 0;
         arr[0][head[0]++] = poly[0];
         for (int n = 0; n < num; ++n) {
             int m = (n + 1) % num;
@@ -322,6 +329,7 @@ static void cut_face_rec(const V2* poly, int num, int dim, const std::function<v
                 } else {
                     arr[1][head[1]++] = add;
                     if (head[1] > 32) { st.overflow = 1; return; }
+                    if (++parts > 1) st.multi = 1;
                     cut_face_rec(arr[1], head[1], dim, out, st);
                     slot = 0;
                     if (t1 < 1.0) arr[0][head[0]++] = add;
@@ -422,7 +430,7 @@ inline void cross(const real* a, const real* b, real* o) {
 struct SubPoly { real pos[3]; real n[3]; };
 
 static int split_face(const real (*v)[3], real h, const real* color_off, real minimal_area,
-                      std::vector<SubPoly>& outv) {
+                      std::vector<SubPoly>& outv, int* multi = nullptr) {
     V2 quad[4];
     const real xi[4][2] = {{0.0, 0.0}, {1.0, 0.0}, {1.0, 1.0}, {0.0, 1.0}};
     for (int i = 0; i < 4; ++i) {
@@ -459,6 +467,7 @@ static int split_face(const real (*v)[3], real h, const real* color_off, real mi
             });
         }
     }, st);
+    if (multi) *multi = st.multi;
     return (st.overflow ? 1 : 0) | (st.odd_cut ? 2 : 0);
 }
 
@@ -633,10 +642,11 @@ static void pass_range(const Grid& G, const Velocity& vel, const Field& A, const
 }
 
 static int run_pass(const Grid& G, const Velocity& vel, const Field& A, const PassParams& P,
-                    real* out, int nthreads, long c0, long c1, long* faces, long* polys, real* vol = nullptr) {
+                    real* out, int nthreads, long c0, long c1, long* faces, long* polys, real* vol = nullptr,
+                    int psi_x0 = 0, int psi_x1 = -1) {
     Gauss1D g = make_gauss(P.k);
     std::vector<real> psi;
-    compute_psi(A, G.h, P.psi_mode, g, psi);
+    compute_psi(A, G.h, P.psi_mode, g, psi, psi_x0, psi_x1);
     Field Psi;
     Psi.a = psi.data();
     Psi.M[0] = A.M[0]; Psi.M[1] = A.M[1] + 1; Psi.M[2] = A.M[2];
@@ -852,6 +862,45 @@ int fo_move_substances_3D(int nx, int ny, int nz, double h, const double* u, con
                         split_off, minimal_area, nthreads, nullptr, nullptr, maccormack, volume_correction);
 }
 
+// move_substances_3D (flux branch, density) on the cells of the x-slab [x0, x1) only: the work
+// unit of the bounded CPU baseline, which times the step slab by slab.  The main pass and the
+// error-advection pass run on the slab's cells; the zero-velocity pass, whose result the error
+// pass reads within the backtrace reach, on the slab widened by `margin` cells each way (the
+// caller passes ceil(max displacement) + 1); psi is computed on the columns those cells read
+// (the WENO6 stencil reaches 3 more).  out[cell] is written for the slab's cells only.
+int fo_move_substances_slab(int nx, int ny, int nz, double h, const double* u, const double* v, const double* w,
+                            const double* rho, double dt, int interp_method, int k, int correction,
+                            int use_integral, const double* split_off, double minimal_area, int nthreads, int x0,
+                            int x1, int margin, double* out, long* faces) {
+    Grid G; G.N[0] = nx; G.N[1] = ny; G.N[2] = nz; G.h = h;
+    if (x0 < 0 || x1 > nx || x0 >= x1 || margin < 0) return -1;
+    Velocity vel = make_velocity(G, u, v, w);
+    Field A = make_field(rho, G, -1);
+    for (int d = 0; d < 3; ++d) { A.M[d] = G.N[d]; A.off[d] = 0.5; }
+    const long plane = (long)ny * nz, n = (long)nx * plane;
+    PassParams P;
+    P.comp = -1; P.interp = interp_method; P.k = k; P.minimal_area = minimal_area; P.dt = dt;
+    P.psi_mode = use_integral ? (interp_method == I_WENO6 ? PSI_WENO6 : PSI_LINEAR) : PSI_PLAIN;
+    P.use_integral = use_integral; P.zero_velocity = 0; P.maccormack = 0;
+    split_offsets(-1, 0, split_off, P.color_off);
+    const int reach = margin + 3;
+    int status = run_pass(G, vel, A, P, out, nthreads, x0 * plane, x1 * plane, faces, nullptr, nullptr, x0 - reach,
+                          x1 + reach);
+    if (!correction) return status;
+    const int xa = std::max(0, x0 - margin), xb = std::min(nx, x1 + margin);
+    std::vector<real> c(n, 0.0), c2(n, 0.0);
+    P.zero_velocity = 1; P.use_integral = 0; P.psi_mode = PSI_PLAIN;
+    status |= run_pass(G, vel, A, P, c.data(), nthreads, xa * plane, xb * plane, nullptr, nullptr, nullptr, xa - 3,
+                       xb + 3);
+    for (long i = xa * plane; i < xb * plane; ++i) c[i] = rho[i] - c[i];
+    Field C = A; C.a = c.data();
+    P.zero_velocity = 0; P.interp = I_1DY_LINEAR;
+    split_offsets(-1, 1, split_off, P.color_off);
+    status |= run_pass(G, vel, C, P, c2.data(), nthreads, x0 * plane, x1 * plane, nullptr, nullptr, nullptr, xa, xb);
+    for (long i = x0 * plane; i < x1 * plane; ++i) out[i] += c2[i];
+    return status;
+}
+
 // The advected cell volumes of the density's main pass (the volume points of its pieces).
 int fo_cell_volumes(int nx, int ny, int nz, double h, const double* u, const double* v, const double* w,
                     double dt, int interp_method, int k, int use_integral, const double* split_off,
@@ -990,3 +1039,6 @@ static int solve_A(const int* N, const real* b, real* p, real tol, int maxit) {
     return fo_pressure_solve(N[0], N[1], N[2], b, p, tol, maxit, &rr);
 }
 }  // namespace
+
+// the streaming-tile CPU baseline (uses the clipper and fields above)
+#include "cpu_stream.inl"

@@ -13,6 +13,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SRC = os.path.join(HERE, "fia_oracle.cpp")
+ORACLE_DEPS = [ORACLE_SRC, os.path.join(HERE, "cpu_stream.inl")]
 ORACLE_SO = os.path.join(HERE, "_build", "liboracle_%s.so" % platform.machine())
 REF_DIR = os.path.join(HERE, "_ref")
 
@@ -23,7 +24,8 @@ _lp = ctypes.POINTER(ctypes.c_long)
 
 def build_oracle(force=False):
     """Compile the oracle for this host (x86-64 here, aarch64 on the GPU host)."""
-    if not force and os.path.exists(ORACLE_SO) and os.path.getmtime(ORACLE_SO) >= os.path.getmtime(ORACLE_SRC):
+    if not force and os.path.exists(ORACLE_SO) and os.path.getmtime(ORACLE_SO) >= max(map(os.path.getmtime,
+                                                                                         ORACLE_DEPS)):
         return ORACLE_SO
     os.makedirs(os.path.dirname(ORACLE_SO), exist_ok=True)
     tmp = ORACLE_SO + ".tmp%d" % os.getpid()
@@ -115,6 +117,36 @@ class Oracle:
                                             so, ctypes.c_double(minimal_area), nthreads, int(maccormack),
                                             int(volume_correction))
         return r, st
+
+    def move_substances_slab(self, N, h, u, v, w, rho, dt, x0, x1, margin, interp=0, k=3, correction=1,
+                             use_integral=1, split_off=(0.5, 0.5), minimal_area=1.0, nthreads=1, out=None):
+        """move_substances_3D on the cells of the x-slab [x0, x1) (the CPU baseline's work unit);
+        returns (out, status, faces visited) with only the slab's cells of out written"""
+        u, v, w, rho = _f64(u), _f64(v), _f64(w), _f64(rho)
+        if out is None:
+            out = np.zeros(rho.size)
+        so = (ctypes.c_double * 2)(*split_off)
+        nf = ctypes.c_long(0)
+        st = self.lib.fo_move_substances_slab(N[0], N[1], N[2], ctypes.c_double(h), _ptr(u), _ptr(v), _ptr(w),
+                                              _ptr(rho), ctypes.c_double(dt), interp, k, correction, use_integral, so,
+                                              ctypes.c_double(minimal_area), nthreads, x0, x1, margin, _ptr(out),
+                                              ctypes.byref(nf))
+        return out, st, nf.value
+
+    def stream_move_substances_slab(self, N, h, u, v, w, rho, dt, x0, x1, margin, interp=0, k=3, correction=1,
+                                    use_integral=1, split_off=(0.5, 0.5), minimal_area=1.0, nthreads=1, out=None):
+        """the streaming-tile CPU baseline (oracle/cpu_stream.inl) on the x-slab [x0, x1), the same
+        interface as move_substances_slab"""
+        u, v, w, rho = _f64(u), _f64(v), _f64(w), _f64(rho)
+        if out is None:
+            out = np.zeros(rho.size)
+        so = (ctypes.c_double * 2)(*split_off)
+        nf = ctypes.c_long(0)
+        st = self.lib.fo_stream_move_substances_slab(N[0], N[1], N[2], ctypes.c_double(h), _ptr(u), _ptr(v), _ptr(w),
+                                                     _ptr(rho), ctypes.c_double(dt), interp, k, correction,
+                                                     use_integral, so, ctypes.c_double(minimal_area), nthreads, x0, x1,
+                                                     margin, _ptr(out), ctypes.byref(nf))
+        return out, st, nf.value
 
     def cell_volumes(self, N, h, u, v, w, dt, interp=0, k=3, use_integral=1, split_off=(0.5, 0.5), minimal_area=1.0,
                      nthreads=1, maccormack=0):

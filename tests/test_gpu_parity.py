@@ -255,3 +255,19 @@ def test_invalid_arguments_fail_loudly():
     with pytest.raises(fia.FiaError):
         g.set("u", np.zeros(5))
     g.close()
+
+
+def test_fp64_weno_collapse_matches_full_evaluation():
+    """The plain form collapses WENO6 along the axes on which a point lies on a node plane
+    (vertices at rest, psi points, faces at rest); the full evaluation gives the same steps to
+    rounding (the collapse is exact in real arithmetic)."""
+    outs = []
+    for full in (1, 0):
+        g, h, u, v, w, rho, dt = make(20, 16, 18, seed=9)
+        assert g.debug_full_weno(full) == full
+        g.move_substances_3D(dt, fia.advect_params())
+        g.advect_velocity_xyz_flux_advection_3D(dt, fia.advect_params())
+        outs.append([g.get(c) for c in ("density", "u", "v", "w")])
+        g.close()
+    for a, b in zip(*outs):
+        assert rel(a, b) < 1e-13
