@@ -61,21 +61,29 @@ struct ArrayVerts {
     __host__ __device__ __forceinline__ float y(int n) const { return py[n]; }
 };
 
+// Centroid and area of a polygon in (xi, eta) (facecutter.h:226-253), the shoelace sums taken
+// relative to the polygon's first vertex.  Equal in exact arithmetic to the sums over absolute
+// coordinates; in FP32 the absolute form cancels for a sliver (a piece a few 1e-4 wide beside an
+// iso-line, whose vertices are O(1) from the origin): its centroid came out up to ~1e-4 off,
+// on the far side of the iso-line that bounds it, and the error pass's nearest-cell
+// interpolation (1Dy-linear) then read psi of the wrong column.  Relative to the first vertex
+// the products are of the sliver's own size and its centroid is accurate to FP32 rounding.
 template <class V>
 __host__ __device__ __forceinline__ void centroid_v(const V& v, int num, float& cx, float& cy, float& area) {
+    const float x0 = v.x(0), y0 = v.y(0);
     float a = 0.f, sx = 0.f, sy = 0.f;
     for (int n = 0; n < num; ++n) {
         const int m = (n + 1 == num) ? 0 : n + 1;
-        const float xn = v.x(n), yn = v.y(n), xm = v.x(m), ym = v.y(m);
+        const float xn = v.x(n) - x0, yn = v.y(n) - y0, xm = v.x(m) - x0, ym = v.y(m) - y0;
         const float c = xn * ym - xm * yn;
         a += c; sx += c * (xn + xm); sy += c * (yn + ym);
     }
     a = fabsf(0.5f * a);
-    if (a != 0.f) { const float s = 1.0f / (6.0f * a); cx = sx * s; cy = sy * s; }
+    if (a != 0.f) { const float s = 1.0f / (6.0f * a); cx = x0 + sx * s; cy = y0 + sy * s; }
     else {
         sx = 0.f; sy = 0.f;
-        for (int n = 0; n < num; ++n) { sx += v.x(n); sy += v.y(n); }
-        cx = sx / float(num); cy = sy / float(num);
+        for (int n = 0; n < num; ++n) { sx += v.x(n) - x0; sy += v.y(n) - y0; }
+        cx = x0 + sx / float(num); cy = y0 + sy / float(num);
     }
     area = a;
 }
