@@ -477,61 +477,22 @@ __global__ void k_rest_fill32(PassDesc d, int fam, PieceStore ps, unsigned* stat
     normal_of(ps, fam)[id] = make_float2(nr.x, nr.y);
 }
 
-// Pieces are taken in tiles of one per thread.  With the y-integral quadrature a piece needs
-// either one interval (k density points, a 6-row z-pass) or two (2k points, 7 rows), about
-// 64 or 91 1D evaluations at k = 3; mixed in a warp, the short ones idle while the long ones
-// finish (ncu: 28.0 of 32 lanes active).  So each tile is first ordered by that class within
-// the CTA (warp ballots, one shared-memory permutation): all but one warp of a tile then do
-// uniform work.  The flux of piece t is still written to slot t, so the order of the
-// per-face sums, and the results, do not change.
 __global__ void __launch_bounds__(kQuadThreads, 4) k_quad32(PassDesc d, const float* __restrict__ a,
                                                          const float2* __restrict__ psi, PieceStore ps, long long npc,
                                                          unsigned long long* counters) {
     __shared__ float zcol[48 * kQuadThreads];   // each thread's z- and y-pass column (weno6_ycolumn)
-    __shared__ int order[kQuadThreads];         // the tile's pieces, one-interval class first
-    __shared__ int wcount[kQuadThreads / 32];   // per warp: pieces of class 0 | class 1 << 16
     unsigned long long ec = 0;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const long long ntiles = (npc + kQuadThreads - 1) / kQuadThreads;
-    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const long long t0 = tile * kQuadThreads;
-        long long t = t0 + threadIdx.x;
-        if (d.use_integral) {
-            int cls = 2;                                        // 2: past the end of the store
-            if (t < npc) {
-                const float oy = (d.comp == 1) ? -0.5f : 0.f;
-                const float r = snap_int(ps.rec[t].y - oy);
-                cls = (r - floorf(r) < 0.5f) ? 0 : 1;
-            }
-            const unsigned m0 = __ballot_sync(0xffffffffu, cls == 0), m1 = __ballot_sync(0xffffffffu, cls == 1);
-            if (lane == 0) wcount[warp] = __popc(m0) | (__popc(m1) << 16);
-            __syncthreads();
-            int before0 = 0, before1 = 0, total0 = 0, total1 = 0;
-#pragma unroll
-            for (int w = 0; w < kQuadThreads / 32; ++w) {
-                const int c0 = wcount[w] & 0xffff, c1 = wcount[w] >> 16;
-                if (w < warp) { before0 += c0; before1 += c1; }
-                total0 += c0; total1 += c1;
-            }
-            const unsigned below = (1u << lane) - 1u;
-            if (cls == 0) order[before0 + __popc(m0 & below)] = threadIdx.x;
-            else if (cls == 1) order[total0 + before1 + __popc(m1 & below)] = threadIdx.x;
-            __syncthreads();
-            t = threadIdx.x < total0 + total1 ? t0 + order[threadIdx.x] : npc;
-        }
-        if (t < npc) {
-            const float4 p = ps.rec[t];
-            const int tag = ps.face[t];
-            const int fam = tag >> 29;
-            int anc[3];
-            face_of(fam, d.A, tag & ((1 << 29) - 1), anc[0], anc[1], anc[2]);
-            const float2 b = __ldg(psi + psi_node(d.P, anc[0], anc[1], anc[2]));
-            const PsiLoad pl{psi, b.x, b.y};
-            Kahan F;
-            ec += (unsigned long long)piece_quad32(d, anc, p.x, p.y, p.z, p.w, a, pl, F, zcol + threadIdx.x);
-            ps.flux[t] = F.value();
-        }
-        if (d.use_integral) __syncthreads();                    // order and wcount are reused
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < npc; t += (long long)gridDim.x * blockDim.x) {
+        const float4 p = ps.rec[t];
+        const int tag = ps.face[t];
+        const int fam = tag >> 29;
+        int anc[3];
+        face_of(fam, d.A, tag & ((1 << 29) - 1), anc[0], anc[1], anc[2]);
+        const float2 b = __ldg(psi + psi_node(d.P, anc[0], anc[1], anc[2]));
+        const PsiLoad pl{psi, b.x, b.y};
+        Kahan F;
+        ec += (unsigned long long)piece_quad32(d, anc, p.x, p.y, p.z, p.w, a, pl, F, zcol + threadIdx.x);
+        ps.flux[t] = F.value();
     }
     for (int o = 16; o > 0; o >>= 1) ec += __shfl_down_sync(0xffffffffu, ec, o);
     if ((threadIdx.x & 31) == 0 && ec) atomicAdd(&counters[3], ec);
