@@ -137,6 +137,8 @@ def run_plume(n, precision, steps):
 def test_fp32_plume_tracks_fp64():
     r64, v64, m64 = run_plume(32, fia.FIA_FP64, 40)
     r32, v32, m32 = run_plume(32, fia.FIA_FP32C, 40)
+    print("FP32 plume 32^3 after 40 steps: density rel L2 vs FP64 %.3e, velocity %s"
+          % (rel(r32, r64), ", ".join("%.3e" % rel(a, b) for a, b in zip(v32, v64))))
     # measured 1.3e-3 (density) on GB300: discontinuity flips, see the module docstring
     assert rel(r32, r64) < 5e-3
     for a, b in zip(v32, v64):
