@@ -334,7 +334,7 @@ def north_star(fia, args):
     the state the chosen form's timed steps started from (same frame)."""
     import torch
     n = args.ns_grid
-    weights = os.path.join(PKG, "weights", "unet_precond.f32")
+    weights = args.weights
     tol = 1e-6
 
     def session(prec, state):
@@ -522,6 +522,8 @@ def main():
     ap.add_argument("--ns-warmup", type=int, default=3)
     ap.add_argument("--ns-steps", type=int, default=5)
     ap.add_argument("--ns-fp64-steps", type=int, default=3)
+    ap.add_argument("--weights", default=os.path.join(PKG, "weights", "unet_precond.f32"),
+                    help="learned preconditioner of the 256^3 target step")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

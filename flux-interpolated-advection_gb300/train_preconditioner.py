@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Trains the learned pressure preconditioner on the GPU with the library's own kernels.
 
-Training pairs B p = r (B = -A) come from three sources:
+Training pairs B p = r (B = -A) come from four sources:
  * the simulator itself: plume runs on an n^3 grid (default 128^3), each with a seeded source
    position in [0.3,0.7] x [0.1,0.2] x [0.3,0.7] and 0-4 seeded solid spheres of radius
    U[0.05,0.15]; every step, before the projection, the projection is solved with Jacobi-PCG
@@ -12,8 +12,14 @@ Training pairs B p = r (B = -A) come from three sources:
    residuals, whose spectrum is much rougher than a divergence field's; a network trained on
    divergences alone maps rough residuals to large smooth corrections orthogonal to them and
    the iteration stalls;
+ * stress runs (--stress-runs): the plume in a developed flow at CFL 4 (16 seeded Fourier
+   modes) with eight small solid spheres of radius U[0.04, 0.1], the configuration under which
+   flexible CG used to stall near the solids, each with its pairs captured like the plume runs'
+   and multi-scale pairs on its solids;
  * on-policy pairs: residual and error (r_k, e_k = p - x_k) after k flexible-CG iterations with
-   the network of the first training phase.
+   the network of the first training phase, on multi-scale problems without solids and, with
+   --onpolicy-stress, with the stress runs' solids (where the residual concentrates beside the
+   spheres).
 The network (fia_unet.cu) is trained with Adam on the energy-norm loss
 (z - p)^T B (z - p) / p^T B p of the whole two-level preconditioner, the last run's pairs held
 out for validation.  Finally flexible CG with the trained network is compared with Jacobi-PCG
@@ -21,6 +27,7 @@ on a fresh plume state.
 
     python train_preconditioner.py [--grid 128] [--runs 6] [--steps 30] [--iters 6000] \
         [--batch 4] [--lr 1e-3] [--onpolicy 120] [--onpolicy-share 0.25] [--seed 1] \
+        [--stress-runs 2] [--stress-steps 20] [--onpolicy-stress 60] \
         [--eval-grids 128,256] [--out weights/unet_precond.f32]
 
 Writes the FP32 parameter vector (fia_learned_num_parameters() floats, little endian) to
@@ -56,6 +63,22 @@ def scene(rng):
                 continue
             centers.append(c); radii.append(r)
             break
+    return src, centers, radii
+
+
+def stress_scene(rng, count=8):
+    """eight solid spheres of radius U[0.04, 0.1] kept clear of the plume source (the stress
+    configuration's solids, drawn from the training seed)"""
+    src = np.array([0.5, 0.15, 0.5])
+    centers, radii = [], []
+    while len(radii) < count:
+        r = rng.uniform(0.04, 0.1)
+        c = rng.uniform(r + 0.02, 1.0 - r - 0.02, size=3)
+        if np.linalg.norm(c - src) < r + 0.15:
+            continue
+        if any(np.linalg.norm(c - c2) < r + r2 for c2, r2 in zip(centers, radii)):
+            continue
+        centers.append(c); radii.append(r)
     return src, centers, radii
 
 
@@ -114,14 +137,20 @@ def add_multiscale_pairs(g, n, rng, count):
     return solid, pin
 
 
-def add_onpolicy_pairs(g, n, rng, count, iters=(2, 4, 8, 16)):
+def add_onpolicy_pairs(g, n, rng, count, iters=(2, 4, 8, 16), solids=None):
     """(r_k, e_k) after k flexible-CG iterations with the current network, on multi-scale
-    problems without solids"""
-    solid = np.zeros((n, n, n), dtype=bool)
-    pin = n ** 3 - 1
+    problems without solids, or with the given solid spheres (centres, radii)"""
+    if solids:
+        g.set_solid_spheres(*solids)
+        solid = g.solid_mask().reshape(n, n, n).astype(bool)
+        pin = int(np.nonzero(~solid.reshape(-1))[0][-1])
+    else:
+        solid = np.zeros((n, n, n), dtype=bool)
+        pin = n ** 3 - 1
     added = 0
     while added < count:
         p = multiscale_field(n, rng)
+        p[solid] = 0.0
         p.reshape(-1)[pin] = 0.0
         r = apply_B(p, solid, pin)
         k = int(rng.choice(iters))
@@ -129,8 +158,11 @@ def add_onpolicy_pairs(g, n, rng, count, iters=(2, 4, 8, 16)):
                                                               fallback_iter=k))
         e = p - x.reshape(n, n, n).astype(np.float64)
         e.reshape(-1)[pin] = 0.0
+        e[solid] = 0.0
         g.learned_add_pair(apply_B(e, solid, pin).ravel(), e.ravel())
         added += 1
+    if solids:
+        g.set_solid_spheres([], [])
 
 
 def reset(g, n):
@@ -159,6 +191,34 @@ def capture_runs(g, n, rng, runs, steps, log, synthetic):
               flush=True)
     g.set_solid_spheres([], [])
     return bounds
+
+
+def capture_stress_runs(g, n, rng, runs, steps, log, synthetic, cfl=4.0):
+    """the plume in a developed flow at CFL `cfl` with eight small spheres; returns the pair
+    ranges and the solids of each run"""
+    import scenes
+    bounds, solids = [], []
+    for run in range(runs):
+        src, centers, radii = stress_scene(rng)
+        reset(g, n)
+        g.set("density", scenes.plume_density(n))
+        u, v, w = scenes.fourier_velocity(n, seed=int(rng.integers(1 << 30)), target_max=cfl * (1.0 / n) * 60.0)
+        for name, a in (("u", u), ("v", v), ("w", w)):
+            g.set(name, a)
+        g.set_solid_spheres(centers, radii)
+        first = g.learned_num_pairs()
+        t0 = time.time()
+        for i in range(steps):
+            g.step(fia.step_params(cfl=cfl, source_center=tuple(src), capture_pair=1, capture_tol=1e-10, frame=i))
+        add_multiscale_pairs(g, n, rng, synthetic)
+        bounds.append((first, g.learned_num_pairs()))
+        solids.append((centers, radii))
+        log.append({"stress_run": run, "spheres": len(radii), "cfl": cfl, "pairs": bounds[-1][1] - first,
+                    "seconds": time.time() - t0})
+        print("stress run %d: %d spheres, CFL %g, %d pairs, %.1f s" % (run, len(radii), cfl, bounds[-1][1] - first,
+                                                                       time.time() - t0), flush=True)
+    g.set_solid_spheres([], [])
+    return bounds, solids
 
 
 def compare_solvers(g, n, seed, steps=12):
@@ -204,6 +264,10 @@ def main():
     ap.add_argument("--onpolicy", type=int, default=120, help="flexible-CG residual pairs after phase 1")
     ap.add_argument("--onpolicy-share", type=float, default=0.25,
                     help="fraction of each batch drawn from the on-policy pairs once they exist")
+    ap.add_argument("--stress-runs", type=int, default=2, help="plume runs at CFL 4 with eight small spheres")
+    ap.add_argument("--stress-steps", type=int, default=20)
+    ap.add_argument("--onpolicy-stress", type=int, default=60,
+                    help="flexible-CG residual pairs with the stress runs' solids after phase 1")
     ap.add_argument("--eval-grids", default="128", help="grids of the final solver comparison")
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--lr", type=float, default=1e-3)
@@ -218,8 +282,10 @@ def main():
     record = {"grid": n, "runs": [], "args": vars(args)}
     t0 = time.time()
     bounds = capture_runs(g, n, rng, args.runs, args.steps, record["runs"], args.synthetic)
+    stress_bounds, stress_solids = capture_stress_runs(g, n, rng, args.stress_runs, args.stress_steps,
+                                                       record["runs"], args.synthetic)
     record["capture_seconds"] = time.time() - t0
-    train = [i for b in bounds[:-1] for i in range(b[0], b[1])]
+    train = [i for b in bounds[:-1] + stress_bounds for i in range(b[0], b[1])]
     val = list(range(bounds[-1][0], bounds[-1][1]))
     if args.init:
         g.learned_set_weights(np.fromfile(args.init, dtype=np.float32))
@@ -238,6 +304,9 @@ def main():
             first = g.learned_num_pairs()
             t1 = time.time()
             add_onpolicy_pairs(g, n, rng, args.onpolicy)
+            for k, sol in enumerate(stress_solids):
+                share = args.onpolicy_stress * (k + 1) // len(stress_solids) - args.onpolicy_stress * k // len(stress_solids)
+                add_onpolicy_pairs(g, n, rng, share, solids=sol)
             onpol = list(range(first, g.learned_num_pairs()))
             record["onpolicy_seconds"] = time.time() - t1
             print("added %d on-policy pairs (%.1f s)" % (len(onpol), time.time() - t1), flush=True)
