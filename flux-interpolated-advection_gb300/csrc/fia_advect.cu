@@ -285,15 +285,12 @@ __device__ __forceinline__ void centroid(const T* px, const T* py, int num, T& c
     area = a;
 }
 
-// Accumulates the flux of one emitted piece (xi-eta polygon px/py with centroid c).
+// 3D centroid and the y component of the scaled normal of an emitted piece (xi-eta polygon
+// px/py with centroid (cxi, ceta); split_face_3D.cpp:67-93)
 template <typename T>
-__device__ __forceinline__ T piece_flux(const PassDesc& d, const FaceGeom<T>& g, const T* px, const T* py,
-                                        int num, T cxi, T ceta, const T* __restrict__ a,
-                                        const T* __restrict__ psi, T* vol) {
-    const T h = T(d.h);
-    // 3D centroid and the y component of the scaled normal (split_face_3D.cpp:67-93)
-    const T cx = bilin(g.x, cxi, ceta), cy = bilin(g.y, cxi, ceta), cz = bilin(g.z, cxi, ceta);
-    T ny;
+__device__ __forceinline__ void piece_geom(const FaceGeom<T>& g, const T* px, const T* py, int num, T cxi, T ceta,
+                                           T& cx, T& cy, T& cz, T& ny) {
+    cx = bilin(g.x, cxi, ceta); cy = bilin(g.y, cxi, ceta); cz = bilin(g.z, cxi, ceta);
     if (num == 3) {
         const T ax = bilin(g.x, px[1], py[1]) - bilin(g.x, px[0], py[0]);
         const T az = bilin(g.z, px[1], py[1]) - bilin(g.z, px[0], py[0]);
@@ -313,9 +310,14 @@ __device__ __forceinline__ T piece_flux(const PassDesc& d, const FaceGeom<T>& g,
         }
         ny = acc * T(0.5);
     }
-    // the piece's volume point (polygon_3D.cpp:480-486): y n_y
-    if (vol) *vol += cy * ny;
+}
+
+// The quadrature of one piece with centroid (cx, cy, cz) and y-normal ny (polygon_3D.cpp:257-487)
+template <typename T>
+__device__ __forceinline__ T piece_quad(const PassDesc& d, T cx, T cy, T cz, T ny, const T* __restrict__ a,
+                                        const T* __restrict__ psi) {
     if (ny == T(0)) return T(0);
+    const T h = T(d.h);
     T F = T(0);
     if (d.use_integral) {
         // polygon_3D.cpp:257-487 with the grid origin shifted by -h/2 along a staggered axis
@@ -348,15 +350,41 @@ __device__ __forceinline__ T piece_flux(const PassDesc& d, const FaceGeom<T>& g,
     return F;
 }
 
-// Emits a polygon (optionally triangulated to minimal_area, facecutter.h:255-324).
+// Accumulates the flux of one emitted piece (xi-eta polygon px/py with centroid c) and its
+// volume point y n_y (polygon_3D.cpp:480-486).
 template <typename T>
+__device__ __forceinline__ T piece_flux(const PassDesc& d, const FaceGeom<T>& g, const T* px, const T* py,
+                                        int num, T cxi, T ceta, const T* __restrict__ a,
+                                        const T* __restrict__ psi, T* vol) {
+    T cx, cy, cz, ny;
+    piece_geom(g, px, py, num, cxi, ceta, cx, cy, cz, ny);
+    if (vol) *vol += cy * ny;
+    return piece_quad(d, cx, cy, cz, ny, a, psi);
+}
+
+// What the clipper does with each emitted piece: the per-face kernel evaluates it at once
+// (EvalPiece), the piece pipeline stores it (StorePiece, below).
+template <typename T>
+struct EvalPiece {
+    const PassDesc& d;
+    const T* __restrict__ a;
+    const T* __restrict__ psi;
+    T* vol;
+    __device__ __forceinline__ T operator()(const FaceGeom<T>& g, const T* px, const T* py, int num, T cxi,
+                                            T ceta) const {
+        return piece_flux(d, g, px, py, num, cxi, ceta, a, psi, vol);
+    }
+};
+
+// Emits a polygon (optionally triangulated to minimal_area, facecutter.h:255-324).
+template <typename T, class Emit>
 __device__ T emit_polygon(const PassDesc& d, const FaceGeom<T>& g, const T* px, const T* py, int num,
-                          const T* __restrict__ a, const T* __restrict__ psi, unsigned& st, int& npieces, T* vol) {
+                          const Emit& emit, unsigned& st, int& npieces) {
     T cx, cy, area;
     centroid(px, py, num, cx, cy, area);
     const T minA = T(d.minimal_area);
     if (!(area > minA)) {
-        if (area != T(0)) { ++npieces; return piece_flux(d, g, px, py, num, cx, cy, a, psi, vol); }
+        if (area != T(0)) { ++npieces; return emit(g, px, py, num, cx, cy); }
         return T(0);
     }
     // triangulate: fan from the centroid (num > 3) then recursive longest-edge bisection
@@ -397,7 +425,7 @@ __device__ T emit_polygon(const PassDesc& d, const FaceGeom<T>& g, const T* px, 
             tri[top][4] = tx[i2]; tri[top][5] = ty[i2]; ++top;
         } else if (tarea != T(0)) {
             ++npieces;
-            F += piece_flux(d, g, tx, ty, 3, tcx, tcy, a, psi, vol);
+            F += emit(g, tx, ty, 3, tcx, tcy);
         }
     }
     return F;
@@ -407,9 +435,9 @@ __device__ T emit_polygon(const PassDesc& d, const FaceGeom<T>& g, const T* px, 
 // `multi` is set when some iso-line crosses a piece more than twice: the piece that holds
 // the first vertex then merges several disjoint parts (facecutter.h:163-181), so the
 // partition depends on the vertex order and the two adjacent cells see different pieces.
-template <typename T>
-__device__ T clip_face(const PassDesc& d, const FaceGeom<T>& g, const T* __restrict__ a,
-                       const T* __restrict__ psi, unsigned& st, int& npieces, bool& multi, T* vol = nullptr) {
+template <typename T, class Emit>
+__device__ T clip_face(const PassDesc& d, const FaceGeom<T>& g, const Emit& emit, unsigned& st, int& npieces,
+                       bool& multi) {
     const T h = T(d.h);
     CV<T> pool[kPool];
     unsigned char sstart[kMaxStack], snum[kMaxStack], sdim[kMaxStack];
@@ -503,7 +531,7 @@ __device__ T clip_face(const PassDesc& d, const FaceGeom<T>& g, const T* __restr
                 if (num >= 3) {
                     T px[kMaxVerts], py[kMaxVerts];
                     for (int q = 0; q < num; ++q) { px[q] = poly[q].p0; py[q] = poly[q].p1; }
-                    F += emit_polygon(d, g, px, py, num, a, psi, st, npieces, vol);
+                    F += emit_polygon(d, g, px, py, num, emit, st, npieces);
                 }
                 top = pstart;
             }
@@ -568,7 +596,7 @@ __global__ void __launch_bounds__(128) k_faces(PassDesc d, int fam, const T* __r
         }
         bool multi = false;
         T V = T(0), Vr = T(0);
-        const T F = clip_face(d, g, a, psi, st, npieces, multi, fvol ? &V : nullptr);
+        const T F = clip_face(d, g, EvalPiece<T>{d, a, psi, fvol ? &V : nullptr}, st, npieces, multi);
         T Fr = -F;
         Vr = -V;
         if (multi) {
@@ -579,7 +607,7 @@ __global__ void __launch_bounds__(128) k_faces(PassDesc d, int fam, const T* __r
             r.x[3] = g.x[1]; r.y[3] = g.y[1]; r.z[3] = g.z[1];
             int np2 = 0; bool m2 = false;
             Vr = T(0);
-            Fr = clip_face(d, r, a, psi, st, np2, m2, fvol ? &Vr : nullptr);
+            Fr = clip_face(d, r, EvalPiece<T>{d, a, psi, fvol ? &Vr : nullptr}, st, np2, m2);
             ++nmulti;
         }
         if (!isfinite(F) || !isfinite(Fr)) st |= ST_NONFINITE;

@@ -270,6 +270,16 @@ __device__ __forceinline__ void face_of(int fam, const NodeField& A, long long i
     i = (int)(id / ((long long)Fz * Fy));
 }
 
+// face_of for the tags of the piece store (face ids below 2^29): two 32-bit divisions
+__device__ __forceinline__ void face_of32(int fam, const NodeField& A, unsigned id, int& i, int& j, int& k) {
+    const unsigned Fy = A.My + (fam == 1), Fz = A.Mz + (fam == 2);
+    const unsigned t = id / Fz;
+    k = (int)(id - t * Fz);
+    const unsigned ii = t / Fy;
+    i = (int)ii;
+    j = (int)(t - ii * Fy);
+}
+
 // corners of face id of family fam, in cells relative to its anchor, backtraced by disp
 __device__ __forceinline__ void face_geometry(const PassDesc& d, int fam, long long id, const float* __restrict__ disp,
                                               LocalFace& g) {
@@ -487,7 +497,7 @@ __global__ void __launch_bounds__(kQuadThreads, 4) k_quad32(PassDesc d, const fl
         const int tag = ps.face[t];
         const int fam = tag >> 29;
         int anc[3];
-        face_of(fam, d.A, tag & ((1 << 29) - 1), anc[0], anc[1], anc[2]);
+        face_of32(fam, d.A, (unsigned)(tag & ((1 << 29) - 1)), anc[0], anc[1], anc[2]);
         const float2 b = __ldg(psi + psi_node(d.P, anc[0], anc[1], anc[2]));
         const PsiLoad pl{psi, b.x, b.y};
         Kahan F;

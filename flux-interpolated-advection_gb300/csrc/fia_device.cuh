@@ -68,6 +68,24 @@ __device__ __forceinline__ WenoCoef<T> weno_coef(const T* t) {
     return w;
 }
 
+// FP32 coefficients: weno_coef with the divisions by constants replaced by products (one
+// rounding more each) and the ideal weights scaled by 20, C = (t4 t5, -2 t5 t0, t0 t1),
+// which the normalised weights of weno6_eval do not see.
+__device__ __forceinline__ WenoCoef<float> weno_coef32(const float* t) {
+    WenoCoef<float> w;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float p = t[i] * t[i + 1];
+        w.a[i] = t[i];
+        w.b[i] = 0.5f * p;
+        w.c[i] = (p * t[i + 2]) * (1.f / 6.f);
+    }
+    w.C[0] = t[4] * t[5];
+    w.C[1] = -2.f * (t[5] * t[0]);
+    w.C[2] = t[0] * t[1];
+    return w;
+}
+
 // One 1D WENO6 evaluation: smoothness indicators with integer coefficients over 180,
 // alpha_i = C_i / (1e-6 + beta_i)^2, normalised weights (WENO6_interpolation_3d.cpp:94-123).
 // The smoothness indicators are evaluated as quadratic forms of the first differences
@@ -88,18 +106,24 @@ __device__ __forceinline__ T weno6_eval(const T* f, const WenoCoef<T>& w) {
     T P[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) P[i] = f[i] + D[i] * w.a[i] + S[i] * w.b[i] + Tt[i] * w.c[i];
-    T e0, e1, e2;
     if constexpr (FASTDIV) {
-        // FP32 form: the indicators in Horner form, and all three (and eps) scaled by 180,
-        // which cancels in the normalised weights: 180 eps + 180 beta_i with no division
-        const T s0 = D0 * (T(244) * D0 - T(1171) * D1 + T(683) * D2) + D1 * (T(1561) * D1 - T(1951) * D2)
-                     + T(814) * D2 * D2;
-        const T s1 = D1 * (T(244) * D1 - T(781) * D2 + T(293) * D3) + D2 * (T(961) * D2 - T(781) * D3)
-                     + T(244) * D3 * D3;
-        const T s2 = D2 * (T(814) * D2 - T(1951) * D3 + T(683) * D4) + D3 * (T(1561) * D3 - T(1171) * D4)
-                     + T(244) * D4 * D4;
+        // FP32 form: the indicators in Horner form, all three (and eps) scaled by 180, which
+        // cancels in the normalised weights, with 180 eps as the start of each chain; then
+        // alpha_i = C_i r_i^2 with r_i = 1/e_i (approximate reciprocals, 1 ulp) and one
+        // approximate division by the weight sum.  Range: e_i >= 180 eps = 1.8e-4, so
+        // r_i^2 <= 3.1e7; for sample differences of order 1 the e_i stay far below the 1e19
+        // at which r_i^2 would leave the normal range.
         const T eps180 = T(0.00018);
-        e0 = eps180 + s0; e1 = eps180 + s1; e2 = eps180 + s2;
+        const T w2 = T(814) * D2;
+        const T e0 = fmaf(D0, T(244) * D0 - T(1171) * D1 + T(683) * D2,
+                          fmaf(D1, T(1561) * D1 - T(1951) * D2, fmaf(w2, D2, eps180)));
+        const T e1 = fmaf(D1, T(244) * D1 - T(781) * D2 + T(293) * D3,
+                          fmaf(D2, T(961) * D2 - T(781) * D3, fmaf(T(244) * D3, D3, eps180)));
+        const T e2 = fmaf(D2, w2 - T(1951) * D3 + T(683) * D4,
+                          fmaf(D3, T(1561) * D3 - T(1171) * D4, fmaf(T(244) * D4, D4, eps180)));
+        const T r0 = __fdividef(T(1), e0), r1 = __fdividef(T(1), e1), r2 = __fdividef(T(1), e2);
+        const T a0 = (w.C[0] * r0) * r0, a1 = (w.C[1] * r1) * r1, a2 = (w.C[2] * r2) * r2;
+        return __fdividef(fmaf(a2, P[2], fmaf(a1, P[1], a0 * P[0])), (a0 + a1) + a2);
     } else {
         const T r180 = T(1) / T(180);
         const T b0 = (T(244) * D0 * D0 - T(1171) * D0 * D1 + T(683) * D0 * D2 + T(1561) * D1 * D1
@@ -109,23 +133,17 @@ __device__ __forceinline__ T weno6_eval(const T* f, const WenoCoef<T>& w) {
         const T b2 = (T(814) * D2 * D2 - T(1951) * D2 * D3 + T(683) * D2 * D4 + T(1561) * D3 * D3
                       - T(1171) * D3 * D4 + T(244) * D4 * D4) * r180;
         const T eps = T(0.000001);
-        e0 = eps + b0; e1 = eps + b1; e2 = eps + b2;
+        const T e0 = eps + b0, e1 = eps + b1, e2 = eps + b2;
+        // alpha_i = C_i / e_i^2 and w_i = alpha_i / sum(alpha).  Multiplying every alpha by
+        // e0^2 e1^2 e2^2 / max(e^2)^2 leaves the weights unchanged and needs two divisions
+        // instead of six; the scaling by the largest e^2 keeps the products in range.
+        const T q0 = e0 * e0, q1 = e1 * e1, q2 = e2 * e2;
+        const T qm = fmax(q0, fmax(q1, q2));
+        const T rq = T(1) / qm;
+        const T t0 = q0 * rq, t1 = q1 * rq, t2 = q2 * rq;
+        const T a0 = w.C[0] * (t1 * t2), a1 = w.C[1] * (t0 * t2), a2 = w.C[2] * (t0 * t1);
+        return (a0 * P[0] + a1 * P[1] + a2 * P[2]) / (a0 + a1 + a2);
     }
-    // alpha_i = C_i / e_i^2 and w_i = alpha_i / sum(alpha).  Multiplying every alpha by
-    // e0^2 e1^2 e2^2 / max(e^2)^2 leaves the weights unchanged and needs two divisions
-    // instead of six; the scaling by the largest e^2 keeps the products in range.
-    const T q0 = e0 * e0, q1 = e1 * e1, q2 = e2 * e2;
-    const T qm = fmax(q0, fmax(q1, q2));
-    // FP32 form: the two divisions by __fdividef (2 ulp; qm is at least (180 eps)^2 and, for
-    // sample values of order 1, below 1e9, and the weight sum lies in [min C, 3]: both far
-    // inside its range, which ends at 2^126)
-    T rq;
-    if constexpr (FASTDIV) rq = __fdividef(T(1), qm);
-    else rq = T(1) / qm;
-    const T t0 = q0 * rq, t1 = q1 * rq, t2 = q2 * rq;
-    const T a0 = w.C[0] * (t1 * t2), a1 = w.C[1] * (t0 * t2), a2 = w.C[2] * (t0 * t1);
-    if constexpr (FASTDIV) return __fdividef(a0 * P[0] + a1 * P[1] + a2 * P[2], a0 + a1 + a2);
-    else return (a0 * P[0] + a1 * P[1] + a2 * P[2]) / (a0 + a1 + a2);
 }
 
 // Tensor-product WENO6 of a node field at p (z, then y, then x), stencil indices clamped

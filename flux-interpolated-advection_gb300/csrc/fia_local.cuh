@@ -66,21 +66,23 @@ struct Kahan {
 
 // Loads node values as floats: plain array, or psi pairs relative to a base pair.
 // row(i) gives a row pointer; at(row, k) the value k nodes further along the row (k a
-// compile-time constant in an unrolled loop, so one load with an immediate offset)
+// compile-time constant in an unrolled loop, so one load with an immediate offset).
+// Node offsets are 32-bit: fia_create admits grids with (nx+2)(ny+2)(nz+2) <= 2^31, which
+// bounds every node field of the path.
 struct PlainLoad {
     const float* __restrict__ a;
-    __device__ __forceinline__ float operator()(long long i) const { return __ldg(a + i); }
-    __device__ __forceinline__ const float* row(long long i) const { return a + i; }
+    __device__ __forceinline__ float operator()(int i) const { return __ldg(a + i); }
+    __device__ __forceinline__ const float* row(int i) const { return a + i; }
     __device__ __forceinline__ float at(const float* p, int k) const { return __ldg(p + k); }
 };
 struct PsiLoad {
     const float2* __restrict__ a;
     float hi0, lo0;
-    __device__ __forceinline__ float operator()(long long i) const {
+    __device__ __forceinline__ float operator()(int i) const {
         const float2 v = __ldg(a + i);
         return (v.x - hi0) + (v.y - lo0);
     }
-    __device__ __forceinline__ const float2* row(long long i) const { return a + i; }
+    __device__ __forceinline__ const float2* row(int i) const { return a + i; }
     __device__ __forceinline__ float at(const float2* p, int k) const {
         const float2 v = __ldg(p + k);
         return (v.x - hi0) + (v.y - lo0);
@@ -90,7 +92,7 @@ struct PsiLoad {
 // the six z-values of two stencil rows: row pointers and immediate offsets when the z-stencil
 // lies inside the field (zin), else the clamped indices kk
 template <class L>
-__device__ __forceinline__ void load_rows(const L& load, long long row0, long long row1, bool zin, int bz,
+__device__ __forceinline__ void load_rows(const L& load, int row0, int row1, bool zin, int bz,
                                           const int* kk, float* f0, float* f1) {
     if (zin) {
         const auto p0 = load.row(row0 + bz - 2), p1 = load.row(row1 + bz - 2);
@@ -128,7 +130,7 @@ __device__ float weno6_3d_loc(const L& load, const NodeField& F, const int* anc,
         ty[i] = sy + float(2 - i);
         tz[i] = sz + float(2 - i);
     }
-    const WenoCoef<float> cx = weno_coef(tx), cy = weno_coef(ty), cz = weno_coef(tz);
+    const WenoCoef<float> cx = weno_coef32(tx), cy = weno_coef32(ty), cz = weno_coef32(tz);
     int kk[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) kk[i] = clampi(bz - 2 + i, F.Mz - 1);
@@ -139,8 +141,8 @@ __device__ float weno6_3d_loc(const L& load, const NodeField& F, const int* anc,
         float zv[6];
 #pragma unroll
         for (int iy = 0; iy < 6; iy += 2) {
-            const long long j0 = clampi(by - 2 + iy, F.My - 1), j1 = clampi(by - 1 + iy, F.My - 1);
-            const long long row0 = F.Mz * (F.My * (long long)ii + j0), row1 = F.Mz * (F.My * (long long)ii + j1);
+            const int j0 = clampi(by - 2 + iy, F.My - 1), j1 = clampi(by - 1 + iy, F.My - 1);
+            const int row0 = F.Mz * (F.My * ii + j0), row1 = F.Mz * (F.My * ii + j1);
             float f0[6], f1[6];
 #pragma unroll
             for (int iz = 0; iz < 6; ++iz) { f0[iz] = load(row0 + kk[iz]); f1[iz] = load(row1 + kk[iz]); }
@@ -175,7 +177,7 @@ __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, 
     float tx[6], tz[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) { tx[i] = sx + float(2 - i); tz[i] = sz + float(2 - i); }
-    const WenoCoef<float> cx = weno_coef(tx), cz = weno_coef(tz);
+    const WenoCoef<float> cx = weno_coef32(tx), cz = weno_coef32(tz);
     int kk[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) kk[i] = clampi(bz - 2 + i, F.Mz - 1);
@@ -183,13 +185,13 @@ __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, 
     const bool zin = bz >= 2 && bz + 3 <= F.Mz - 1;
 #pragma unroll 1
     for (int ix = 0; ix < 6; ix += 2) {
-        const long long i0 = clampi(bx - 2 + ix, F.Mx - 1), i1 = clampi(bx - 1 + ix, F.Mx - 1);
+        const int i0 = clampi(bx - 2 + ix, F.Mx - 1), i1 = clampi(bx - 1 + ix, F.Mx - 1);
         float* z0 = zs + 7 * ix * STRIDE;
         float* z1 = z0 + 7 * STRIDE;
 #pragma unroll 1
         for (int r = 0; r < nr; ++r) {
-            const long long jj = clampi(by0 - 2 + r, F.My - 1);
-            const long long row0 = F.Mz * (F.My * i0 + jj), row1 = F.Mz * (F.My * i1 + jj);
+            const int jj = clampi(by0 - 2 + r, F.My - 1);
+            const int row0 = F.Mz * (F.My * i0 + jj), row1 = F.Mz * (F.My * i1 + jj);
             float f0[6], f1[6];
             load_rows(load, row0, row1, zin, bz, kk, f0, f1);
             const float2 v = weno6_pair(f0, f1, cz);
@@ -206,7 +208,7 @@ __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, 
         float ty[6];
 #pragma unroll
         for (int i = 0; i < 6; ++i) ty[i] = sy + float(2 - i);
-        const WenoCoef<float> cy = weno_coef(ty);
+        const WenoCoef<float> cy = weno_coef32(ty);
         const float* zb = zs + (up ? STRIDE : 0);
 #pragma unroll 1
         for (int ix = 0; ix < 6; ix += 2) {
@@ -238,9 +240,9 @@ __device__ float weno6_1dy_loc(const L& load, const NodeField& F, const int* anc
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
         t[i] = sy + float(2 - i);
-        f[i] = load(idx3(F, ix, clampi(by - 2 + i, F.My - 1), iz));
+        f[i] = load(F.Mz * (F.My * ix + clampi(by - 2 + i, F.My - 1)) + iz);
     }
-    return weno6_call(f, weno_coef(t));
+    return weno6_call(f, weno_coef32(t));
 }
 
 template <class L>
@@ -259,7 +261,7 @@ __device__ float lin3d_loc(const L& load, const NodeField& F, const int* anc, co
 #pragma unroll
         for (int iy = 0; iy < 2; ++iy) {
             const int jj = clampi(by + iy, F.My - 1);
-            const long long row = (long long)F.Mz * ((long long)F.My * ii + jj);
+            const int row = F.Mz * (F.My * ii + jj);
             zv[iy] = (1.f - sz) * load(row + k0) + sz * load(row + k1);
         }
         yv[ix] = (1.f - sy) * zv[0] + sy * zv[1];
@@ -274,8 +276,8 @@ __device__ float lin1dy_loc(const L& load, const NodeField& F, const int* anc, c
     const int ix = clampi(cell_of(anc[0], q[0], F.oxf - 0.5f), F.Mx - 1);
     const int iz = clampi(cell_of(anc[2], q[2], F.ozf - 0.5f), F.Mz - 1);
     locate(anc[1], q[1], F.oyf, by, sy);
-    const float f0 = load(idx3(F, ix, clampi(by, F.My - 1), iz));
-    const float f1 = load(idx3(F, ix, clampi(by + 1, F.My - 1), iz));
+    const float f0 = load(F.Mz * (F.My * ix + clampi(by, F.My - 1)) + iz);
+    const float f1 = load(F.Mz * (F.My * ix + clampi(by + 1, F.My - 1)) + iz);
     return (1.f - sy) * f0 + sy * f1;
 }
 
@@ -298,16 +300,16 @@ __device__ int weno6_3d_noderow(const L& load, const NodeField& F, const int* an
     float tx[6], tz[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) { tx[i] = sx + float(2 - i); tz[i] = sz + float(2 - i); }
-    const WenoCoef<float> cx = weno_coef(tx), cz = weno_coef(tz);
+    const WenoCoef<float> cx = weno_coef32(tx), cz = weno_coef32(tz);
     int kk[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) kk[i] = clampi(bz - 2 + i, F.Mz - 1);
-    const long long jj = clampi(by, F.My - 1);
+    const int jj = clampi(by, F.My - 1);
     const bool zin = bz >= 2 && bz + 3 <= F.Mz - 1;
 #pragma unroll 1
     for (int ix = 0; ix < 6; ix += 2) {
-        const long long i0 = clampi(bx - 2 + ix, F.Mx - 1), i1 = clampi(bx - 1 + ix, F.Mx - 1);
-        const long long row0 = F.Mz * (F.My * i0 + jj), row1 = F.Mz * (F.My * i1 + jj);
+        const int i0 = clampi(bx - 2 + ix, F.Mx - 1), i1 = clampi(bx - 1 + ix, F.Mx - 1);
+        const int row0 = F.Mz * (F.My * i0 + jj), row1 = F.Mz * (F.My * i1 + jj);
         float f0[6], f1[6];
         load_rows(load, row0, row1, zin, bz, kk, f0, f1);
         const float2 v = weno6_pair(f0, f1, cz);
@@ -339,7 +341,7 @@ __device__ float weno6_3d_collapse(const L& load, const NodeField& F, const int*
         ty[i] = sy + float(2 - i);
         tz[i] = sz + float(2 - i);
     }
-    const WenoCoef<float> cx = weno_coef(tx), cy = weno_coef(ty), cz = weno_coef(tz);
+    const WenoCoef<float> cx = weno_coef32(tx), cy = weno_coef32(ty), cz = weno_coef32(tz);
     int kk[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) kk[i] = clampi(bz - 2 + i, F.Mz - 1);
@@ -347,11 +349,11 @@ __device__ float weno6_3d_collapse(const L& load, const NodeField& F, const int*
     float yv[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll 1
     for (int ix = x0; ix < x1; ++ix) {
-        const long long ii = clampi(bx - 2 + ix, F.Mx - 1);
+        const int ii = clampi(bx - 2 + ix, F.Mx - 1);
         float zv[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll 1
         for (int iy = y0; iy < y1; ++iy) {
-            const long long row = F.Mz * (F.My * ii + clampi(by - 2 + iy, F.My - 1));
+            const int row = F.Mz * (F.My * ii + clampi(by - 2 + iy, F.My - 1));
             if (czn) {
                 zv[iy] = load(row + kk[2]);
             } else {
