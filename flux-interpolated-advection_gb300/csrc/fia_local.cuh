@@ -162,7 +162,7 @@ __device__ float weno6_3d_loc(const L& load, const NodeField& F, const int* anc,
 // 0 (nothing accumulated) if [ya, yb] spans more than one cell of the field.
 // The 6 x 7 z-pass results live in shared memory, zs[(7 ix + r) * stride] (the calling
 // thread's column of a block-wide array, stride = threads per block, 48 words: in registers
-// they held 42 of the face kernel's 128), a point's six y-pass results in words 42-47.
+// they held 42 of the face kernel's 128); a point's six y-pass results stay in registers.
 template <int STRIDE, class L, class P>
 __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, float qx, float qz, float ya,
                              float yb, int npts, const P& point, Kahan& acc, float* zs) {
@@ -210,7 +210,8 @@ __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, 
         for (int i = 0; i < 6; ++i) ty[i] = sy + float(2 - i);
         const WenoCoef<float> cy = weno_coef32(ty);
         const float* zb = zs + (up ? STRIDE : 0);
-#pragma unroll 1
+        float yv[6];
+#pragma unroll
         for (int ix = 0; ix < 6; ix += 2) {
             float f0[6], f1[6];
 #pragma unroll
@@ -219,11 +220,8 @@ __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, 
                 f1[i] = zb[(7 * ix + 7 + i) * STRIDE];
             }
             const float2 v = weno6_pair(f0, f1, cy);
-            zs[(42 + ix) * STRIDE] = v.x; zs[(43 + ix) * STRIDE] = v.y;
+            yv[ix] = v.x; yv[ix + 1] = v.y;
         }
-        float yv[6];
-#pragma unroll
-        for (int i = 0; i < 6; ++i) yv[i] = zs[(42 + i) * STRIDE];
         acc.add(weno6_eval<float, true>(yv, cx) * w);
     }
     return (seven ? 42 : 36) + 7 * npts;
