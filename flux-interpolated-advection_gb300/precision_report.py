@@ -4,14 +4,17 @@ with relative L2 differences of density and velocity between every pair of arms 
 numbers of steps ("a|b": |a - b| / |b|), and each arm's mass drift.
 
     python precision_report.py [--grid 64] [--steps 25,50,100] [--cfl 2]
-                               [--arm NAME:PRECISION:TOL[:SOLVER[:DRHO]]] ...
+                               [--arm NAME:PRECISION:TOL[:SOLVER[:DRHO[:DU]]]] ...
 
 PRECISION is fp64 (plain form) or fp32c (chosen form); TOL the pressure tolerance (FP64
 residual in both forms); SOLVER pcg (Jacobi-PCG) or learned (flexible CG with the committed
 preconditioner, fp32c only); DRHO a relative perturbation of the initial density: the
 source sphere holds 1 + DRHO * xi with xi seeded uniform in [0, 1) per cell (the source
-re-injects max(density, 1), so the perturbation is kept).  Without --arm the chosen form (fp32c, Jacobi-PCG) is compared with the
-plain form at --tol.
+re-injects max(density, 1), so the perturbation is kept); DU a relative jitter of the velocity
+after every step: each face velocity times 1 + DU * xi, xi seeded uniform in [-1, 1) (DU of
+about 6e-8 is the size of FP32 rounding, so an FP64 arm with it measures how far the scheme
+carries FP32-sized perturbations made at every step).  Without --arm the chosen form (fp32c,
+Jacobi-PCG) is compared with the plain form at --tol.
 
 Every arm starts from the plume density (sphere r = 0.1 at (0.5, 0.15, 0.5)) at rest, with
 the source re-injected every step, buoyancy 1 and CFL --cfl.  Prints one JSON line.
@@ -37,9 +40,10 @@ def rel(a, b):
 def parse_arm(spec, default_tol):
     f = spec.split(":")
     if len(f) < 2 or f[1] not in ("fp64", "fp32c"):
-        raise SystemExit("bad --arm %r (NAME:PRECISION:TOL[:SOLVER[:DRHO]])" % spec)
+        raise SystemExit("bad --arm %r (NAME:PRECISION:TOL[:SOLVER[:DRHO[:DU]]])" % spec)
     arm = {"name": f[0], "precision": f[1], "tol": float(f[2]) if len(f) > 2 and f[2] else default_tol,
-           "solver": f[3] if len(f) > 3 and f[3] else "pcg", "drho": float(f[4]) if len(f) > 4 and f[4] else 0.0}
+           "solver": f[3] if len(f) > 3 and f[3] else "pcg", "drho": float(f[4]) if len(f) > 4 and f[4] else 0.0,
+           "du": float(f[5]) if len(f) > 5 and f[5] else 0.0}
     if arm["solver"] not in ("pcg", "learned") or (arm["solver"] == "learned" and arm["precision"] != "fp32c"):
         raise SystemExit("bad solver in --arm %r" % spec)
     return arm
@@ -75,9 +79,9 @@ def main():
             g.learned_set_weights(np.fromfile(args.weights, dtype="<f4"))
             solver.update(method=fia.FIA_SOLVER_FCG_LEARNED, fallback_iter=200)
         arm.update(grid=g, params=fia.step_params(cfl=args.cfl, solver=solver), masses=[], seconds=0.0,
-                   status=0)
+                   status=0, rng=np.random.Generator(np.random.PCG64(args.seed + 1)))
     out = {"grid": n, "cfl": args.cfl,
-           "arms": [{k: a[k] for k in ("name", "precision", "tol", "solver", "drho")} for a in arms],
+           "arms": [{k: a[k] for k in ("name", "precision", "tol", "solver", "drho", "du")} for a in arms],
            "checkpoints": []}
     step = 0
     for cp in checkpoints:
@@ -89,6 +93,10 @@ def main():
                 arm["seconds"] += time.time() - t0
                 arm["status"] |= rep.status
                 arm["masses"].append((rep.mass_before_advection, rep.mass_after_advection, rep.mass_after))
+                if arm["du"]:
+                    for c in "uvw":
+                        a = arm["grid"].get(c)
+                        arm["grid"].set(c, a * (1.0 + arm["du"] * arm["rng"].uniform(-1.0, 1.0, size=a.size)))
             step += 1
         fields = [{c: arm["grid"].get(c) for c in ("density", "u", "v", "w")} for arm in arms]
         row = {"step": step, "density": {}, "velocity": {}}

@@ -141,3 +141,17 @@ def test_gauss_rule_rejects_even_and_out_of_range_counts(lib, k):
     x = np.zeros(20); w = np.zeros(20)
     assert lib.fia_gauss_rule(k, x.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                               w.ctypes.data_as(ctypes.POINTER(ctypes.c_double))) == fia.FIA_ERR_INVALID
+
+
+def test_precision_report_arm_specs():
+    """The arm grammar of precision_report.py: NAME:PRECISION:TOL[:SOLVER[:DRHO[:DU]]]."""
+    import precision_report as pr
+    a = pr.parse_arm("p64:fp64:1e-6", 1e-8)
+    assert (a["name"], a["precision"], a["tol"], a["solver"], a["drho"], a["du"]) == ("p64", "fp64", 1e-6, "pcg", 0.0, 0.0)
+    a = pr.parse_arm("j:fp64:1e-6:pcg:1e-7:6e-8", 1e-8)
+    assert (a["drho"], a["du"]) == (1e-7, 6e-8)
+    a = pr.parse_arm("c:fp32c::learned", 1e-8)
+    assert (a["tol"], a["solver"]) == (1e-8, "learned")
+    for bad in ("x", "x:fp16:1e-6", "x:fp64:1e-6:learned", "x:fp32c:1e-6:amg"):
+        with pytest.raises(SystemExit):
+            pr.parse_arm(bad, 1e-8)
