@@ -563,6 +563,39 @@ __device__ __forceinline__ void face_corners(int fam, int i, int j, int k, int* 
     }
 }
 
+// the four corners of face id of family fam: backtraced (verts) or at rest
+template <typename T>
+__device__ __forceinline__ void face_geom(const PassDesc& d, int fam, long long id, const T* __restrict__ verts,
+                                          FaceGeom<T>& g) {
+    const int Fy = d.A.My + (fam == 1), Fz = d.A.Mz + (fam == 2);
+    const int k = (int)(id % Fz);
+    const int j = (int)((id / Fz) % Fy);
+    const int i = (int)(id / ((long long)Fz * Fy));
+    int ci[4], cj[4], ck[4];
+    face_corners(fam, i, j, k, ci, cj, ck);
+    const int Ly = d.A.My + 1, Lz = d.A.Mz + 1;
+    for (int q = 0; q < 4; ++q) {
+        if (d.zero_velocity) {
+            T p[3];
+            vertex_rest_position(d, ci[q], cj[q], ck[q], p);
+            g.x[q] = p[0]; g.y[q] = p[1]; g.z[q] = p[2];
+        } else {
+            const long long vid = ((long long)ci[q] * Ly + cj[q]) * Lz + ck[q];
+            g.x[q] = verts[3 * vid]; g.y[q] = verts[3 * vid + 1]; g.z[q] = verts[3 * vid + 2];
+        }
+    }
+}
+
+// the upper cell's own face: vertex order (v0, v3, v2, v1), which is the reference's x-/y-/z-
+// face order (backtrace_..._for_integrate_density.cpp:77-112)
+template <typename T>
+__device__ __forceinline__ FaceGeom<T> upper_face(const FaceGeom<T>& g) {
+    FaceGeom<T> r = g;
+    r.x[1] = g.x[3]; r.y[1] = g.y[3]; r.z[1] = g.z[3];
+    r.x[3] = g.x[1]; r.y[3] = g.y[1]; r.z[3] = g.z[1];
+    return r;
+}
+
 // flux = wgt * F (acc = 0) or flux + wgt * F (acc = 1): the weighted faces of the flux
 // MacCormack scheme accumulate into one flux per face (wgt = 1, acc = 0 otherwise)
 template <typename T>
@@ -577,34 +610,15 @@ __global__ void __launch_bounds__(128) k_faces(PassDesc d, int fam, const T* __r
     unsigned st = 0;
     int npieces = 0, nmulti = 0;
     if (id < nface) {
-        const int k = (int)(id % Fz);
-        const int j = (int)((id / Fz) % Fy);
-        const int i = (int)(id / ((long long)Fz * Fy));
-        int ci[4], cj[4], ck[4];
-        face_corners(fam, i, j, k, ci, cj, ck);
         FaceGeom<T> g;
-        const int Ly = d.A.My + 1, Lz = d.A.Mz + 1;
-        for (int q = 0; q < 4; ++q) {
-            if (d.zero_velocity) {
-                T p[3];
-                vertex_rest_position(d, ci[q], cj[q], ck[q], p);
-                g.x[q] = p[0]; g.y[q] = p[1]; g.z[q] = p[2];
-            } else {
-                const long long vid = ((long long)ci[q] * Ly + cj[q]) * Lz + ck[q];
-                g.x[q] = verts[3 * vid]; g.y[q] = verts[3 * vid + 1]; g.z[q] = verts[3 * vid + 2];
-            }
-        }
+        face_geom(d, fam, id, verts, g);
         bool multi = false;
         T V = T(0), Vr = T(0);
         const T F = clip_face(d, g, EvalPiece<T>{d, a, psi, fvol ? &V : nullptr}, st, npieces, multi);
         T Fr = -F;
         Vr = -V;
         if (multi) {
-            // the upper cell's own face: vertex order (v0, v3, v2, v1), which is the reference's
-            // x-/y-/z- face order (backtrace_..._for_integrate_density.cpp:77-112)
-            FaceGeom<T> r = g;
-            r.x[1] = g.x[3]; r.y[1] = g.y[3]; r.z[1] = g.z[3];
-            r.x[3] = g.x[1]; r.y[3] = g.y[1]; r.z[3] = g.z[1];
+            const FaceGeom<T> r = upper_face(g);
             int np2 = 0; bool m2 = false;
             Vr = T(0);
             Fr = clip_face(d, r, EvalPiece<T>{d, a, psi, fvol ? &Vr : nullptr}, st, np2, m2);
@@ -631,6 +645,116 @@ __global__ void __launch_bounds__(128) k_faces(PassDesc d, int fam, const T* __r
         if (fc) { atomicAdd(&counters[0], (unsigned long long)fc); atomicAdd(&counters[1], pc); }
         if (mc) atomicAdd(&counters[2], (unsigned long long)mc);
         if (st) atomicOr(status, st);
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// The plain form's piece pipeline: k_clip64 (one thread per face: the clip, its pieces
+// appended contiguously per face), k_quad64 (one thread per piece: the quadrature) and
+// k_facesum64 (one thread per face: its pieces' fluxes summed in emission order).  The clip,
+// the per-piece arithmetic and the order of every sum are those of k_faces, which evaluates
+// each piece as the clipper emits it: there the lanes of a warp wait for the face with the
+// most pieces (a third of them active on average); here each lane has one piece.
+// ------------------------------------------------------------------------------------
+constexpr int kMaxPieces64 = 64;   // pieces of one face, both clips (as the FP32 store)
+
+struct StorePiece64 {
+    double4_32a* p;
+    int* n;
+    unsigned* st;
+    __device__ __forceinline__ double operator()(const FaceGeom<double>& g, const double* px, const double* py, int num,
+                                                 double cxi, double ceta) const {
+        double cx, cy, cz, ny;
+        piece_geom(g, px, py, num, cxi, ceta, cx, cy, cz, ny);
+        if (*n < kMaxPieces64) p[(*n)++] = make_double4_32a(cx, cy, cz, ny);
+        else *st |= ST_CLIP_OVERFLOW;
+        return 0.0;
+    }
+};
+
+__device__ __forceinline__ int2* range64(const PieceStore64& ps, int fam) {
+    return fam == 0 ? ps.range[0] : (fam == 1 ? ps.range[1] : ps.range[2]);
+}
+
+__global__ void __launch_bounds__(128) k_clip64(PassDesc d, int fam, const double* __restrict__ verts, PieceStore64 ps,
+                                                unsigned* status, unsigned long long* counters) {
+    const long long nface = (long long)(d.A.Mx + (fam == 0)) * (d.A.My + (fam == 1)) * (d.A.Mz + (fam == 2));
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    unsigned st = 0;
+    int npieces = 0, n = 0, nfwd = 0;
+    bool multi = false;
+    double4_32a buf[kMaxPieces64];
+    if (id < nface) {
+        FaceGeom<double> g;
+        face_geom(d, fam, id, verts, g);
+        clip_face(d, g, StorePiece64{buf, &n, &st}, st, npieces, multi);
+        nfwd = n;
+        if (multi) {
+            int np2 = 0;
+            bool m2 = false;
+            clip_face(d, upper_face(g), StorePiece64{buf, &n, &st}, st, np2, m2);
+        }
+    }
+    const long long start = warp_slots(ps.count, n, lane);
+    if (id < nface) {
+        // a range beyond the capacity is kept as it is: the host sees the count, grows the
+        // store and clips again
+        if (start + n <= ps.cap)
+            for (int q = 0; q < n; ++q) ps.rec[start + q] = buf[q];
+        range64(ps, fam)[id] = make_int2((int)start, nfwd | ((n - nfwd) << 15) | ((multi ? 1 : 0) << 30));
+    }
+    unsigned long long pc = (unsigned long long)npieces;
+    unsigned fc = id < nface ? 1u : 0u, mc = multi ? 1u : 0u;
+    for (int o = 16; o > 0; o >>= 1) {
+        pc += __shfl_down_sync(0xffffffffu, pc, o);
+        fc += __shfl_down_sync(0xffffffffu, fc, o);
+        mc += __shfl_down_sync(0xffffffffu, mc, o);
+        st |= __shfl_down_sync(0xffffffffu, st, o);
+    }
+    if (lane == 0) {
+        if (fc) { atomicAdd(&counters[0], (unsigned long long)fc); atomicAdd(&counters[1], pc); }
+        if (mc) atomicAdd(&counters[2], (unsigned long long)mc);
+        if (st) atomicOr(status, st);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_quad64(PassDesc d, const double* __restrict__ a,
+                                                const double* __restrict__ psi, PieceStore64 ps, long long npc) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < npc; t += (long long)gridDim.x * blockDim.x) {
+        const double4_32a p = ps.rec[t];
+        ps.flux[t] = piece_quad(d, p.x, p.y, p.z, p.w, a, psi);
+    }
+}
+
+__global__ void k_facesum64(PassDesc d, int fam, PieceStore64 ps, double* __restrict__ flux,
+                            double* __restrict__ flux_rev, unsigned* status, double wgt, int acc,
+                            double* __restrict__ fvol, double* __restrict__ fvol_rev) {
+    const long long nface = (long long)(d.A.Mx + (fam == 0)) * (d.A.My + (fam == 1)) * (d.A.Mz + (fam == 2));
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= nface) return;
+    const int2 r = range64(ps, fam)[id];
+    const int nf = r.y & 0x7fff, nr = (r.y >> 15) & 0x7fff;
+    const bool multi = (r.y >> 30) & 1;
+    double F = 0.0, V = 0.0;
+    for (int q = 0; q < nf; ++q) {
+        F += ps.flux[(long long)r.x + q];
+        if (fvol) { const double4_32a p = ps.rec[(long long)r.x + q]; V += p.y * p.w; }
+    }
+    double Fr = -F, Vr = -V;
+    if (multi) {
+        Fr = 0.0; Vr = 0.0;
+        for (int q = nf; q < nf + nr; ++q) {
+            Fr += ps.flux[(long long)r.x + q];
+            if (fvol) { const double4_32a p = ps.rec[(long long)r.x + q]; Vr += p.y * p.w; }
+        }
+    }
+    if (!isfinite(F) || !isfinite(Fr)) atomicOr(status, (unsigned)ST_NONFINITE);
+    flux[id] = acc ? flux[id] + wgt * F : wgt * F;
+    flux_rev[id] = acc ? flux_rev[id] + wgt * Fr : wgt * Fr;
+    if (fvol) {
+        fvol[id] = acc ? fvol[id] + wgt * V : wgt * V;
+        fvol_rev[id] = acc ? fvol_rev[id] + wgt * Vr : wgt * Vr;
     }
 }
 
@@ -697,9 +821,88 @@ static cudaError_t launch_faces_from(const PassDesc& d, const T* a, const PassWo
     return cudaGetLastError();
 }
 
+// One face stage of the piece pipeline: clip (growing the store and clipping again when it is
+// too small), per-piece quadrature, per-face sums weighted into the face fluxes.
+static cudaError_t face_stage64(const PassDesc& d, const double* a, const PassWork<double>& w, const double* verts,
+                                double wgt, int acc, cudaStream_t s) {
+    PieceStore64& ps = *w.pieces64;
+    long long nface[3], big = 0;
+    for (int fam = 0; fam < 3; ++fam) {
+        nface[fam] = (long long)(d.A.Mx + (fam == 0)) * (d.A.My + (fam == 1)) * (d.A.Mz + (fam == 2));
+        big = nface[fam] > big ? nface[fam] : big;
+    }
+    unsigned npc = 0;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        cudaError_t e = cudaMemsetAsync(ps.count, 0, sizeof(unsigned), s);
+        if (e != cudaSuccess) return e;
+        for (int fam = 0; fam < 3; ++fam)
+            k_clip64<<<blocks_for(nface[fam], 128), 128, 0, s>>>(d, fam, verts, ps, w.status, w.counters);
+        e = cudaMemcpyAsync(&npc, ps.count, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return e;
+        if ((long long)npc <= ps.cap) break;
+        // more pieces than the store holds: grow it and clip again (the counters of the first
+        // attempt stay counted)
+        e = piece_store64_reserve(ps, (long long)npc + npc / 4 + 1024, big);
+        if (e != cudaSuccess) return e;
+    }
+    if ((long long)npc > ps.cap) return cudaErrorMemoryAllocation;
+    if (npc > 0) {
+        const long long nb = std::min<long long>(blocks_for(npc, 128), 152LL * 16);
+        prof_mark(w, 0, s);
+        k_quad64<<<(unsigned)nb, 128, 0, s>>>(d, a, w.psi, ps, (long long)npc);
+        prof_mark(w, 1, s);
+    }
+    for (int fam = 0; fam < 3; ++fam)
+        k_facesum64<<<blocks_for(nface[fam], 256), 256, 0, s>>>(d, fam, ps, w.flux[fam], w.flux_rev[fam], w.status, wgt,
+                                                              acc, d.volumes ? w.fvol[fam] : nullptr,
+                                                              d.volumes ? w.fvol_rev[fam] : nullptr);
+    return cudaGetLastError();
+}
+
+template <typename T>
+static cudaError_t faces_weighted(const PassDesc& d, const T* a, const PassWork<T>& w, const T* verts, T wgt, int acc,
+                                  cudaStream_t s) {
+    if constexpr (sizeof(T) == sizeof(double)) {
+        if (w.pieces64) return face_stage64(d, a, w, verts, wgt, acc, s);
+    }
+    return launch_faces_from<T>(d, a, w, verts, wgt, acc, s);
+}
+
 template <typename T>
 cudaError_t launch_faces(const PassDesc& d, const T* a, const PassWork<T>& w, cudaStream_t s) {
-    return launch_faces_from<T>(d, a, w, w.verts, T(1), 0, s);
+    return faces_weighted<T>(d, a, w, w.verts, T(1), 0, s);
+}
+
+cudaError_t piece_store64_reserve(PieceStore64& p, long long pieces, long long faces_per_family) {
+    cudaDeviceSynchronize();
+    // ranges hold 31-bit starts
+    if (pieces >= (1LL << 31)) pieces = (1LL << 31) - 1;
+    if (pieces > p.cap) {
+        cudaFree(p.rec); cudaFree(p.flux);
+        p.rec = nullptr; p.flux = nullptr; p.cap = 0;
+        cudaError_t e = cudaMalloc(&p.rec, pieces * sizeof(double4_32a));
+        if (e == cudaSuccess) e = cudaMalloc(&p.flux, pieces * sizeof(double));
+        if (e != cudaSuccess) return e;
+        p.cap = pieces;
+    }
+    if (!p.count) {
+        cudaError_t e = cudaMalloc(&p.count, sizeof(unsigned));
+        if (e != cudaSuccess) return e;
+    }
+    if (!p.range[0]) {
+        for (int f = 0; f < 3; ++f) {
+            cudaError_t e = cudaMalloc(&p.range[f], faces_per_family * sizeof(int2));
+            if (e != cudaSuccess) return e;
+        }
+    }
+    return cudaSuccess;
+}
+
+void piece_store64_free(PieceStore64& p) {
+    cudaFree(p.rec); cudaFree(p.flux); cudaFree(p.count);
+    for (int f = 0; f < 3; ++f) cudaFree(p.range[f]);
+    p = PieceStore64();
 }
 
 template <typename T>
@@ -730,9 +933,9 @@ cudaError_t run_pass(const PassDesc& d, const VelocityFields& vel, const T* a, c
                                                               vel.fu, vel.fv, vel.fw, w.verts, w.verts2);
         PassDesc rest = d;
         rest.zero_velocity = 1;
-        e = launch_faces_from<T>(rest, a, w, w.verts, T(0.5), 0, s);            // the face at rest
-        if (e == cudaSuccess) e = launch_faces_from<T>(d, a, w, w.verts, T(1), 1, s);   // backtraced
-        if (e == cudaSuccess) e = launch_faces_from<T>(d, a, w, w.verts2, T(-0.5), 1, s);   // traced back
+        e = faces_weighted<T>(rest, a, w, w.verts, T(0.5), 0, s);            // the face at rest
+        if (e == cudaSuccess) e = faces_weighted<T>(d, a, w, w.verts, T(1), 1, s);   // backtraced
+        if (e == cudaSuccess) e = faces_weighted<T>(d, a, w, w.verts2, T(-0.5), 1, s);   // traced back
     }
     if (e != cudaSuccess) return e;
     if (d.volumes) {

@@ -66,6 +66,18 @@ struct PieceStore {
 cudaError_t piece_store_reserve(PieceStore& p, long long pieces, long long faces_per_family);
 void piece_store_free(PieceStore& p);
 
+// Pieces of the plain form's face pipeline (clip -> per-piece quadrature -> per-face sum),
+// as PieceStore: every face's pieces contiguous, in emission order, forward clip first.
+struct PieceStore64 {
+    double4_32a* rec = nullptr;      // (cx, cy, cz, ny): centroid (absolute), y component of the scaled normal
+    double* flux = nullptr;      // flux of each piece
+    int2* range[3] = {nullptr, nullptr, nullptr};   // per face: start, nfwd | nrev << 15 | multi << 30
+    unsigned* count = nullptr;   // device counter: pieces appended
+    long long cap = 0;           // pieces the buffers hold
+};
+cudaError_t piece_store64_reserve(PieceStore64& p, long long pieces, long long faces_per_family);
+void piece_store64_free(PieceStore64& p);
+
 // Workspace owned by the caller (device pointers).
 template <typename T>
 struct PassWork {
@@ -84,6 +96,7 @@ struct PassWork {
     int* prof_n;            // pairs recorded so far
     int prof_cap;
     PieceStore* pieces = nullptr;   // FP32 form only
+    PieceStore64* pieces64 = nullptr;   // FP64 form: the piece pipeline; null: one thread per face (k_faces)
 };
 
 // records the opening / closing event of a timed face-kernel launch

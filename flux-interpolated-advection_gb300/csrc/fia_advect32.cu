@@ -303,20 +303,6 @@ __device__ __forceinline__ void face_geometry(const PassDesc& d, int fam, long l
     }
 }
 
-// contiguous store slots for the warp's pieces: warp prefix sum, one atomic per warp
-__device__ __forceinline__ long long warp_slots(unsigned* count, int cnt, int lane) {
-    int pre = cnt;
-    for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(0xffffffffu, pre, o);
-        if (lane >= o) pre += t;
-    }
-    const int total = __shfl_sync(0xffffffffu, pre, 31);
-    unsigned base = 0;
-    if (lane == 31 && total > 0) base = atomicAdd(count, (unsigned)total);
-    base = __shfl_sync(0xffffffffu, base, 31);
-    return (long long)base + pre - cnt;
-}
-
 __device__ __forceinline__ void warp_counters(unsigned long long pc, unsigned fc, unsigned mc, unsigned st, int lane,
                                               unsigned* status, unsigned long long* counters) {
     for (int o = 16; o > 0; o >>= 1) {

@@ -60,6 +60,9 @@ struct fia_session {
     bool fcg_ready = false;
     double* p64 = nullptr;       // FP32 form: pressure accumulated in FP64 by the refinement
     int full_weno = 0;           // FP64 form: no WENO6 collapse on node planes (fia_debug_full_weno)
+    // clipped pieces of a pass (FP64 form); piece_pipeline 0: one thread per face instead
+    PieceStore64 pieces64;
+    int piece_pipeline = 1;
 };
 
 namespace {
@@ -218,6 +221,7 @@ PassWork<T> work(fia_session* s) {
     w.prof_n = &s->prof_n;
     w.prof_cap = (int)(s->prof_ev.size() / 2);
     w.pieces = &s->pieces;
+    w.pieces64 = (s->precision == FIA_FP64 && s->piece_pipeline) ? &s->pieces64 : nullptr;
     return w;
 }
 
@@ -958,6 +962,7 @@ fia_session* fia_create(int nx, int ny, int nz, double cell_length, int precisio
         // faces of one family of any (staggered) field fit in (nx+2)(ny+2)(nz+2)
         ok = piece_store_reserve(s->pieces, 10 * big + 1024, big) == cudaSuccess;
     }
+    if (ok && precision == FIA_FP64) ok = piece_store64_reserve(s->pieces64, 10 * big + 1024, big) == cudaSuccess;
     if (!ok) {
         g_last_error = "fia_create: device allocation failed";
         fia_destroy(s);
@@ -1003,6 +1008,7 @@ void fia_destroy(fia_session* s) {
         for (int j = 0; j <= kFcgMaxDirs; ++j) { cudaFree(s->fcg.d[j]); cudaFree(s->fcg.q[j]); }
     unet::net_destroy(s->net);
     piece_store_free(s->pieces);
+    piece_store64_free(s->pieces64);
     if (s->p64) cudaFree(s->p64);
     if (s->solid) cudaFree(s->solid);
     for (void* p : s->allocations) cudaFree(p);
@@ -1442,14 +1448,29 @@ int fia_debug_learned_grad(fia_session* s, int pair, float* grads, double* loss)
 }
 
 int fia_debug_set_piece_capacity(fia_session* s, long long pieces) {
-    if (!s || s->precision != FIA_FP32C || pieces < 1) return FIA_ERR_INVALID;
+    if (!s || pieces < 1) return FIA_ERR_INVALID;
     CK(cudaStreamSynchronize(s->stream));
     const long long big = (long long)(s->N[0] + 2) * (s->N[1] + 2) * (s->N[2] + 2);
+    if (s->precision == FIA_FP64) {
+        piece_store64_free(s->pieces64);
+        CK(piece_store64_reserve(s->pieces64, pieces, big));
+        return FIA_OK;
+    }
     const int fast = s->pieces.clip_fast;
     piece_store_free(s->pieces);
     s->pieces.clip_fast = fast;
     CK(piece_store_reserve(s->pieces, pieces, big));
     return FIA_OK;
+}
+
+int fia_debug_piece_pipeline(fia_session* s, int enable) {
+    if (!s || enable < -1 || enable > 1) return FIA_ERR_INVALID;
+    if (enable >= 0) {
+        if (s->precision != FIA_FP64) return FIA_ERR_INVALID;
+        CK(cudaStreamSynchronize(s->stream));
+        s->piece_pipeline = enable;
+    }
+    return s->precision == FIA_FP64 ? s->piece_pipeline : 0;
 }
 
 int fia_debug_full_weno(fia_session* s, int enable) {

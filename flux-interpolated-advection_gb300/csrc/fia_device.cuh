@@ -38,6 +38,21 @@ __host__ __device__ __forceinline__ float snap_int(float x) {
     return fabsf(x - r) <= tol ? r : x;
 }
 
+// Contiguous store slots for the pieces of a warp's faces (cnt per lane): warp prefix sum and
+// one atomic per warp on the store's counter.  Every lane of the warp calls it.
+__device__ __forceinline__ long long warp_slots(unsigned* count, int cnt, int lane) {
+    int pre = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, pre, o);
+        if (lane >= o) pre += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, pre, 31);
+    unsigned base = 0;
+    if (lane == 31 && total > 0) base = atomicAdd(count, (unsigned)total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    return (long long)base + pre - cnt;
+}
+
 // Read-only load through the non-coherent cache.
 template <typename T> __device__ __forceinline__ T ldg(const T* p) { return __ldg(p); }
 

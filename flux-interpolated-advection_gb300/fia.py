@@ -184,6 +184,7 @@ def _declare(lib):
     lib.fia_debug_learned_tc.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_uint)]
     lib.fia_debug_clip_fast.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_ulonglong)]
     lib.fia_debug_full_weno.argtypes = [vp, ip]
+    lib.fia_debug_piece_pipeline.argtypes = [vp, ip]
     lib.fia_debug_learned_grad.argtypes = [vp, ip, fp, dp]
     lib.fia_debug_grid_op.argtypes = [vp, ip, fp, fp]
     lib.fia_debug_solve_rhs.argtypes = [vp, fp, fp, ctypes.POINTER(SolverParams), ctypes.POINTER(SolverReport)]
@@ -503,6 +504,11 @@ class Grid3D:
         """FP64 form: 1 evaluates every WENO6 in full, 0 collapses it on node planes (default),
         -1 leaves it; returns the setting"""
         return _check(self.lib.fia_debug_full_weno(self.s, enable), "fia_debug_full_weno")
+
+    def debug_piece_pipeline(self, enable=-1):
+        """FP64 form: 1 runs the faces as the piece pipeline (default), 0 as one thread per face,
+        -1 leaves it; returns the setting"""
+        return _check(self.lib.fia_debug_piece_pipeline(self.s, enable), "fia_debug_piece_pipeline")
 
     def debug_precondition(self, r):
         a = np.ascontiguousarray(r, dtype=np.float32).ravel()

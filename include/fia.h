@@ -298,7 +298,7 @@ int fia_debug_grid_op(fia_session* s, int op, const float* in, float* out);
  * the solver of sp, x starting from 0. */
 int fia_debug_solve_rhs(fia_session* s, const float* rhs, float* x, const fia_solver_params* sp,
                         fia_solver_report* rep);
-/* FP32 form: capacity of the clipped-piece store (it grows when a pass needs more) */
+/* capacity of the session's clipped-piece store (either form; it grows when a pass needs more) */
 int fia_debug_set_piece_capacity(fia_session* s, long long pieces);
 long long fia_debug_piece_capacity(fia_session* s);
 /* gradient of the energy-norm loss of pair i with respect to all parameters (no update) */
@@ -317,6 +317,12 @@ int fia_debug_clip_fast(fia_session* s, int enable, unsigned long long* deferred
  * psi points of the pieces: equal in exact arithmetic, fewer evaluations), -1 leaves it;
  * returns the setting. */
 int fia_debug_full_weno(fia_session* s, int enable);
+/* FP64 form: enable 1 (the default) runs each pass's faces as the piece pipeline (a thread per
+ * face clips and stores its pieces, a thread per piece integrates, a thread per face sums in
+ * emission order), 0 as one thread per face that integrates each piece as it is clipped (the
+ * same arithmetic and order of sums), -1 leaves it; returns the setting (0 for an FP32C
+ * session, which always runs its own piece pipeline). */
+int fia_debug_piece_pipeline(fia_session* s, int enable);
 
 /* Test hooks: single pieces of the path on host data (FP64 buffers), mirroring the oracle. */
 /* one flux pass of a node field (comp -1 density, 0..2 velocity) with the session velocity */

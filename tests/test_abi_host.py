@@ -64,6 +64,8 @@ def test_null_session_is_rejected_by_every_entry_point(lib):
         "fia_write_density_frame": lambda: lib.fia_write_density_frame(None, b"/nonexistent/frame.fia", 0),
         "fia_append_totals": lambda: lib.fia_append_totals(None, b"/nonexistent/run_", 0.0),
         "fia_debug_clip_fast": lambda: lib.fia_debug_clip_fast(None, 1, ctypes.byref(n)),
+        "fia_debug_full_weno": lambda: lib.fia_debug_full_weno(None, 1),
+        "fia_debug_piece_pipeline": lambda: lib.fia_debug_piece_pipeline(None, 1),
     }
     for name, call in calls.items():
         assert call() == fia.FIA_ERR_INVALID, name

@@ -271,3 +271,39 @@ def test_fp64_weno_collapse_matches_full_evaluation():
         g.close()
     for a, b in zip(*outs):
         assert rel(a, b) < 1e-13
+
+
+PIPE_CASES = [
+    ("default", dict(), 2.0),
+    ("maccormack_volumes", dict(use_MacCormack_scheme=True, enable_cell_volume_correction=True), 2.0),
+    ("triangulated_k5_cfl4", dict(minimal_area=0.05, num_gauss_quadrature_point_for_integrate_density=5), 4.0),
+    ("linear_no_integral", dict(interpolation_method="linear", use_integral=False), 2.0),
+]
+
+
+@pytest.mark.parametrize("name,kw,cfl", PIPE_CASES, ids=[c[0] for c in PIPE_CASES])
+def test_fp64_piece_pipeline_matches_per_face_kernel(name, kw, cfl):
+    """The plain form's piece pipeline (clip and store, a thread per piece, ordered face sums)
+    against one thread per face evaluating each piece as it is clipped: the same pieces, the
+    same per-piece arithmetic and the same order of every sum, so the same steps to rounding
+    (triangulated polygons are summed flat instead of per polygon); with a store too small
+    for the pass, the pipeline grows it and clips again."""
+    p = fia.advect_params(**kw)
+    outs, counts, stats = [], [], []
+    for pipe in (0, 1, 1):
+        g, h, u, v, w, rho, dt = make(20, 16, 18, seed=11, cfl=cfl)
+        assert g.debug_piece_pipeline(pipe) == pipe
+        if pipe and len(outs) == 2:
+            g.debug_set_piece_capacity(100)      # far too small: grown by the first pass
+        c0 = g.pass_counters()
+        stats.append(g.move_substances_3D(dt, p))
+        c1 = g.pass_counters()
+        g.advect_velocity_xyz_flux_advection_3D(dt, p)
+        outs.append([g.get(c) for c in ("density", "u", "v", "w")])
+        counts.append([c1[i] - c0[i] for i in range(3)])
+        g.close()
+    for a, b, c in zip(*outs):
+        assert rel(b, a) < 1e-14, name
+        assert np.array_equal(b, c), name
+    assert counts[0] == counts[1], name            # faces, pieces, faces clipped twice
+    assert stats[0] == stats[1] == stats[2], name
