@@ -312,10 +312,100 @@ __device__ __forceinline__ void piece_geom(const FaceGeom<T>& g, const T* px, co
     }
 }
 
-// The quadrature of one piece with centroid (cx, cy, cz) and y-normal ny (polygon_3D.cpp:257-487)
+// weno6_3d_collapse at points that share x and z (the density quadrature points of a piece,
+// polygon_3D.cpp:286-453) and whose stencils start in two consecutive y rows: the z-pass of
+// the 6 x 7 (x, y) stencil rows is evaluated once into the thread's column zs (word
+// (7 ix + r) * stride, shared memory), and each point takes its y- and x-passes from it.  The
+// same evaluations on the same values as weno6_3d_collapse point by point, so the same results,
+// in 42 + 7 per point 1D evaluations instead of 43 per point.  point(m, y, w) gives point m in
+// [ya, yb]; acc += value * w in order.  A point whose row falls outside the column is evaluated
+// on its own.
+template <typename T, class Pt>
+__device__ void weno6_column(const T* __restrict__ a, const NodeField& F, T h, T px, T pz, T ya, T yb, int npts,
+                             const Pt& point, T& acc, T* zs, int stride) {
+    const T rx = (px - T(F.ox) * h) / h, rz = (pz - T(F.oz) * h) / h;
+    const T sx = snap_int(rx), sz = snap_int(rz);
+    const bool cxn = sx == rint(sx), czn = sz == rint(sz);
+    const int bx = cxn ? (int)sx : (int)floor(rx);
+    const int bz = czn ? (int)sz : (int)floor(rz);
+    auto row_of = [&](T py) {
+        const T ry = (py - T(F.oy) * h) / h;
+        const T sy = snap_int(ry);
+        return sy == rint(sy) ? (int)sy : (int)floor(ry);
+    };
+    const int by0 = row_of(ya);
+    const int nr = row_of(yb) > by0 ? 7 : 6;
+    T tx[6], tz[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        tx[i] = (px - (T(bx - 2 + i) + T(F.ox)) * h) / h;
+        tz[i] = (pz - (T(bz - 2 + i) + T(F.oz)) * h) / h;
+    }
+    const WenoCoef<T> cx = weno_coef(tx), cz = weno_coef(tz);
+    int kk[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) kk[i] = clampi(bz - 2 + i, F.Mz - 1);
+    const int x0 = cxn ? 2 : 0, x1 = cxn ? 3 : 6;
+#pragma unroll 1
+    for (int ix = x0; ix < x1; ++ix) {
+        const int ii = clampi(bx - 2 + ix, F.Mx - 1);
+#pragma unroll 1
+        for (int r = 0; r < nr; ++r) {
+            const int jj = clampi(by0 - 2 + r, F.My - 1);
+            const T* row = a + (long long)F.Mz * ((long long)F.My * ii + jj);
+            T v;
+            if (czn) {
+                v = ldg(row + kk[2]);
+            } else {
+                T f[6];
+#pragma unroll
+                for (int iz = 0; iz < 6; ++iz) f[iz] = ldg(row + kk[iz]);
+                v = weno6_eval(f, cz);
+            }
+            zs[(7 * ix + r) * stride] = v;
+        }
+    }
+#pragma unroll 1
+    for (int m = 0; m < npts; ++m) {
+        T y, w;
+        point(m, y, w);
+        const T ry = (y - T(F.oy) * h) / h;
+        const T sy = snap_int(ry);
+        const bool cyn = sy == rint(sy);
+        const int by = cyn ? (int)sy : (int)floor(ry);
+        T val;
+        if (by < by0 || by - by0 > nr - 6) {
+            val = weno6_3d_collapse(a, F, h, px, y, pz);
+        } else {
+            T ty[6];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) ty[i] = (y - (T(by - 2 + i) + T(F.oy)) * h) / h;
+            const WenoCoef<T> cy = weno_coef(ty);
+            const T* zb = zs + (by - by0) * stride;
+            T yv[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+#pragma unroll 1
+            for (int ix = x0; ix < x1; ++ix) {
+                if (cyn) {
+                    yv[ix] = zb[(7 * ix + 2) * stride];
+                } else {
+                    T zv[6];
+#pragma unroll
+                    for (int iy = 0; iy < 6; ++iy) zv[iy] = zb[(7 * ix + iy) * stride];
+                    yv[ix] = weno6_eval(zv, cy);
+                }
+            }
+            val = cxn ? yv[2] : weno6_eval(yv, cx);
+        }
+        acc += val * w;
+    }
+}
+
+// The quadrature of one piece with centroid (cx, cy, cz) and y-normal ny (polygon_3D.cpp:257-487).
+// With a column zs (42 words at stride `stride`, see weno6_column) the WENO6 density points
+// share their z-pass.
 template <typename T>
 __device__ __forceinline__ T piece_quad(const PassDesc& d, T cx, T cy, T cz, T ny, const T* __restrict__ a,
-                                        const T* __restrict__ psi) {
+                                        const T* __restrict__ psi, T* zs = nullptr, int stride = 0) {
     if (ny == T(0)) return T(0);
     const T h = T(d.h);
     T F = T(0);
@@ -325,7 +415,31 @@ __device__ __forceinline__ T piece_quad(const PassDesc& d, T cx, T cy, T cz, T n
         const T ry = snap_int((cy - oy) / h);
         const int iy0 = (int)floor(ry);
         const T f = ry - T(iy0);
-        if (f < T(0.5)) {
+        if (zs && d.interp == INTERP_WENO6 && !d.full_weno) {
+            // the same points, weights and order as below
+            const int k = d.k;
+            if (f < T(0.5)) {
+                const T lo = T(iy0) * h + oy, L = cy - lo;
+                auto pt = [&](int q, T& y, T& w) {
+                    y = (L / T(2)) * T(d.gx[q]) + (L / T(2)) + lo;
+                    w = ny * f * h * T(d.gw[q]);
+                };
+                weno6_column(a, d.A, h, cx, cz, lo, cy, k, pt, F, zs, stride);
+            } else {
+                const T lo0 = T(iy0) * h + oy, hi0 = (T(iy0) + T(0.5)) * h + oy, L0 = hi0 - lo0;
+                const T lo1 = (T(iy0) + T(0.5)) * h + oy, hi1 = (T(iy0) + f) * h + oy, L1 = hi1 - lo1;
+                auto pt = [&](int m, T& y, T& w) {
+                    if (m < k) {
+                        y = (L0 / T(2)) * T(d.gx[m]) + (L0 / T(2)) + lo0;
+                        w = ny * T(0.5) * h * T(d.gw[m]);
+                    } else {
+                        y = (L1 / T(2)) * T(d.gx[m - k]) + (L1 / T(2)) + lo1;
+                        w = ny * (f - T(0.5)) * h * T(d.gw[m - k]);
+                    }
+                };
+                weno6_column(a, d.A, h, cx, cz, lo0, hi1, 2 * k, pt, F, zs, stride);
+            }
+        } else if (f < T(0.5)) {
             const T lo = T(iy0) * h + oy, L = cy - lo;
             for (int q = 0; q < d.k; ++q) {
                 const T yq = (L / T(2)) * T(d.gx[q]) + (L / T(2)) + lo;
@@ -719,11 +833,15 @@ __global__ void __launch_bounds__(128) k_clip64(PassDesc d, int fam, const doubl
     }
 }
 
-__global__ void __launch_bounds__(128) k_quad64(PassDesc d, const double* __restrict__ a,
-                                                const double* __restrict__ psi, PieceStore64 ps, long long npc) {
+constexpr int kQuad64Threads = 128;
+
+__global__ void __launch_bounds__(kQuad64Threads) k_quad64(PassDesc d, const double* __restrict__ a,
+                                                           const double* __restrict__ psi, PieceStore64 ps,
+                                                           long long npc) {
+    __shared__ double zcol[42 * kQuad64Threads];   // each thread's z-pass column (weno6_column)
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < npc; t += (long long)gridDim.x * blockDim.x) {
         const double4_32a p = ps.rec[t];
-        ps.flux[t] = piece_quad(d, p.x, p.y, p.z, p.w, a, psi);
+        ps.flux[t] = piece_quad(d, p.x, p.y, p.z, p.w, a, psi, zcol + threadIdx.x, kQuad64Threads);
     }
 }
 
@@ -848,9 +966,9 @@ static cudaError_t face_stage64(const PassDesc& d, const double* a, const PassWo
     }
     if ((long long)npc > ps.cap) return cudaErrorMemoryAllocation;
     if (npc > 0) {
-        const long long nb = std::min<long long>(blocks_for(npc, 128), 152LL * 16);
+        const long long nb = std::min<long long>(blocks_for(npc, kQuad64Threads), 152LL * 16);
         prof_mark(w, 0, s);
-        k_quad64<<<(unsigned)nb, 128, 0, s>>>(d, a, w.psi, ps, (long long)npc);
+        k_quad64<<<(unsigned)nb, kQuad64Threads, 0, s>>>(d, a, w.psi, ps, (long long)npc);
         prof_mark(w, 1, s);
     }
     for (int fam = 0; fam < 3; ++fam)
