@@ -50,9 +50,10 @@ VELOCITY_SEED, DENSITY_SEED = 101, 102
 CFL = 2.0
 # FP32 operation count of one 1D WENO6 evaluation as implemented in fia_device.cuh
 # (weno6_eval, FP32 form: differences 12, three cubic candidates 18, three smoothness
-# indicators in Horner form 42, nonlinear weights and the weighted sum 26; an FMA counted as
-# two).  The face kernel counts the 1D evaluations it executes.
-WENO1D_FLOP = 98
+# indicators in Horner form with eps as the start of each chain 45, nonlinear weights by
+# reciprocals 9, the weighted sum and its normalisation 9; an FMA counted as two, a
+# reciprocal as one).  The face kernel counts the 1D evaluations it executes.
+WENO1D_FLOP = 93
 FP32_LANES_PER_SM = 128
 SMS = 152
 L2_BYTES = 129 * 2 ** 20
