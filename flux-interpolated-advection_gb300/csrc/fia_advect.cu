@@ -338,8 +338,8 @@ __device__ void weno6_column(const T* __restrict__ a, const NodeField& F, T h, T
     T tx[6], tz[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
-        tx[i] = (px - (T(bx - 2 + i) + T(F.ox)) * h) / h;
-        tz[i] = (pz - (T(bz - 2 + i) + T(F.oz)) * h) / h;
+        tx[i] = rx - T(bx - 2 + i);
+        tz[i] = rz - T(bz - 2 + i);
     }
     const WenoCoef<T> cx = weno_coef(tx), cz = weno_coef(tz);
     int kk[6];
@@ -379,7 +379,7 @@ __device__ void weno6_column(const T* __restrict__ a, const NodeField& F, T h, T
         } else {
             T ty[6];
 #pragma unroll
-            for (int i = 0; i < 6; ++i) ty[i] = (y - (T(by - 2 + i) + T(F.oy)) * h) / h;
+            for (int i = 0; i < 6; ++i) ty[i] = ry - T(by - 2 + i);
             const WenoCoef<T> cy = weno_coef(ty);
             const T* zb = zs + (by - by0) * stride;
             T yv[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};

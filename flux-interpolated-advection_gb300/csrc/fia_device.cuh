@@ -61,7 +61,9 @@ template <typename T> __device__ __forceinline__ T ldg(const T* p) { return __ld
 // t_i = (p - x_i)/h of the six nodes, the three cubic candidates are
 //   P_i = f_i + (f_{i+1}-f_i) a_i + (f_{i+2}-2f_{i+1}+f_i) b_i + (f_{i+3}-3f_{i+2}+3f_{i+1}-f_i) c_i
 // with a_i = t_i, b_i = t_i t_{i+1}/2, c_i = t_i t_{i+1} t_{i+2}/6, and the ideal weights
-// C = (t4 t5/20, -t5 t0/10, t0 t1/20)  (WENO6_interpolation_3d.cpp:70-92).
+// C = (t4 t5/20, -t5 t0/10, t0 t1/20)  (WENO6_interpolation_3d.cpp:70-92).  The divisions by
+// constants are products here (one rounding more each: on GB300 an FP64 division is a dozen
+// FP64-pipe instructions), and C is kept scaled by 20.
 // --------------------------------------------------------------------------------
 template <typename T>
 struct WenoCoef {
@@ -73,30 +75,14 @@ __device__ __forceinline__ WenoCoef<T> weno_coef(const T* t) {
     WenoCoef<T> w;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
+        const T p = t[i] * t[i + 1];
         w.a[i] = t[i];
-        w.b[i] = t[i] * t[i + 1] / T(2);
-        w.c[i] = t[i] * t[i + 1] * t[i + 2] / T(6);
+        w.b[i] = T(0.5) * p;
+        w.c[i] = (p * t[i + 2]) * (T(1) / T(6));
     }
-    w.C[0] = t[4] * t[5] / T(20);
-    w.C[1] = -t[5] * t[0] / T(10);
-    w.C[2] = t[0] * t[1] / T(20);
-    return w;
-}
-
-// FP32 coefficients: weno_coef with the divisions by constants replaced by products (one
-// rounding more each) and the ideal weights scaled by 20, C = (t4 t5, -2 t5 t0, t0 t1),
-// which the normalised weights of weno6_eval do not see.
-__device__ __forceinline__ WenoCoef<float> weno_coef32(const float* t) {
-    WenoCoef<float> w;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        const float p = t[i] * t[i + 1];
-        w.a[i] = t[i];
-        w.b[i] = 0.5f * p;
-        w.c[i] = (p * t[i + 2]) * (1.f / 6.f);
-    }
+    // the ideal weights scaled by 20, which the normalised weights of weno6_eval do not see
     w.C[0] = t[4] * t[5];
-    w.C[1] = -2.f * (t[5] * t[0]);
+    w.C[1] = T(-2) * (t[5] * t[0]);
     w.C[2] = t[0] * t[1];
     return w;
 }
@@ -150,13 +136,11 @@ __device__ __forceinline__ T weno6_eval(const T* f, const WenoCoef<T>& w) {
         const T eps = T(0.000001);
         const T e0 = eps + b0, e1 = eps + b1, e2 = eps + b2;
         // alpha_i = C_i / e_i^2 and w_i = alpha_i / sum(alpha).  Multiplying every alpha by
-        // e0^2 e1^2 e2^2 / max(e^2)^2 leaves the weights unchanged and needs two divisions
-        // instead of six; the scaling by the largest e^2 keeps the products in range.
+        // e0^2 e1^2 e2^2 leaves the weights unchanged and needs one division instead of six; in
+        // FP64 the products stay in range (e_i >= 1e-6, and e_i^4 overflows only for sample
+        // differences beyond 1e75).
         const T q0 = e0 * e0, q1 = e1 * e1, q2 = e2 * e2;
-        const T qm = fmax(q0, fmax(q1, q2));
-        const T rq = T(1) / qm;
-        const T t0 = q0 * rq, t1 = q1 * rq, t2 = q2 * rq;
-        const T a0 = w.C[0] * (t1 * t2), a1 = w.C[1] * (t0 * t2), a2 = w.C[2] * (t0 * t1);
+        const T a0 = w.C[0] * (q1 * q2), a1 = w.C[1] * (q0 * q2), a2 = w.C[2] * (q0 * q1);
         return (a0 * P[0] + a1 * P[1] + a2 * P[2]) / (a0 + a1 + a2);
     }
 }
@@ -165,15 +149,16 @@ __device__ __forceinline__ T weno6_eval(const T* f, const WenoCoef<T>& w) {
 // to the array (WENO6_interpolation_3d.cpp:7-258 and the face-value variants).
 template <typename T>
 __device__ T weno6_3d(const T* __restrict__ a, const NodeField& F, T h, T px, T py, T pz) {
-    int bx = (int)floor((px - T(F.ox) * h) / h);
-    int by = (int)floor((py - T(F.oy) * h) / h);
-    int bz = (int)floor((pz - T(F.oz) * h) / h);
+    // positions in cells from the field's node 0; the stencil offsets t are these minus the
+    // stencil nodes (the reference divides each offset by h)
+    const T rx = (px - T(F.ox) * h) / h, ry = (py - T(F.oy) * h) / h, rz = (pz - T(F.oz) * h) / h;
+    const int bx = (int)floor(rx), by = (int)floor(ry), bz = (int)floor(rz);
     T tx[6], ty[6], tz[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
-        tx[i] = (px - (T(bx - 2 + i) + T(F.ox)) * h) / h;
-        ty[i] = (py - (T(by - 2 + i) + T(F.oy)) * h) / h;
-        tz[i] = (pz - (T(bz - 2 + i) + T(F.oz)) * h) / h;
+        tx[i] = rx - T(bx - 2 + i);
+        ty[i] = ry - T(by - 2 + i);
+        tz[i] = rz - T(bz - 2 + i);
     }
     const WenoCoef<T> cx = weno_coef(tx), cy = weno_coef(ty), cz = weno_coef(tz);
     int kk[6];
@@ -217,9 +202,9 @@ __device__ T weno6_3d_collapse(const T* __restrict__ a, const NodeField& F, T h,
     T tx[6], ty[6], tz[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
-        tx[i] = (px - (T(bx - 2 + i) + T(F.ox)) * h) / h;
-        ty[i] = (py - (T(by - 2 + i) + T(F.oy)) * h) / h;
-        tz[i] = (pz - (T(bz - 2 + i) + T(F.oz)) * h) / h;
+        tx[i] = rx - T(bx - 2 + i);
+        ty[i] = ry - T(by - 2 + i);
+        tz[i] = rz - T(bz - 2 + i);
     }
     const WenoCoef<T> cx = weno_coef(tx), cy = weno_coef(ty), cz = weno_coef(tz);
     int kk[6];
@@ -255,11 +240,12 @@ template <typename T>
 __device__ T weno6_1dy(const T* __restrict__ a, const NodeField& F, T h, T px, T py, T pz) {
     const int ix = clampi((int)floor(snap_int((px - (T(F.ox) * h - T(0.5) * h)) / h)), F.Mx - 1);
     const int iz = clampi((int)floor(snap_int((pz - (T(F.oz) * h - T(0.5) * h)) / h)), F.Mz - 1);
-    const int by = (int)floor((py - T(F.oy) * h) / h);
+    const T ry = (py - T(F.oy) * h) / h;
+    const int by = (int)floor(ry);
     T t[6], f[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
-        t[i] = (py - (T(by - 2 + i) + T(F.oy)) * h) / h;
+        t[i] = ry - T(by - 2 + i);
         f[i] = ldg(a + idx3(F, ix, clampi(by - 2 + i, F.My - 1), iz));
     }
     return weno6_eval(f, weno_coef(t));

@@ -130,7 +130,7 @@ __device__ float weno6_3d_loc(const L& load, const NodeField& F, const int* anc,
         ty[i] = sy + float(2 - i);
         tz[i] = sz + float(2 - i);
     }
-    const WenoCoef<float> cx = weno_coef32(tx), cy = weno_coef32(ty), cz = weno_coef32(tz);
+    const WenoCoef<float> cx = weno_coef(tx), cy = weno_coef(ty), cz = weno_coef(tz);
     int kk[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) kk[i] = clampi(bz - 2 + i, F.Mz - 1);
@@ -177,7 +177,7 @@ __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, 
     float tx[6], tz[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) { tx[i] = sx + float(2 - i); tz[i] = sz + float(2 - i); }
-    const WenoCoef<float> cx = weno_coef32(tx), cz = weno_coef32(tz);
+    const WenoCoef<float> cx = weno_coef(tx), cz = weno_coef(tz);
     int kk[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) kk[i] = clampi(bz - 2 + i, F.Mz - 1);
@@ -208,7 +208,7 @@ __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, 
         float ty[6];
 #pragma unroll
         for (int i = 0; i < 6; ++i) ty[i] = sy + float(2 - i);
-        const WenoCoef<float> cy = weno_coef32(ty);
+        const WenoCoef<float> cy = weno_coef(ty);
         const float* zb = zs + (up ? STRIDE : 0);
         float yv[6];
 #pragma unroll
@@ -240,7 +240,7 @@ __device__ float weno6_1dy_loc(const L& load, const NodeField& F, const int* anc
         t[i] = sy + float(2 - i);
         f[i] = load(F.Mz * (F.My * ix + clampi(by - 2 + i, F.My - 1)) + iz);
     }
-    return weno6_call(f, weno_coef32(t));
+    return weno6_call(f, weno_coef(t));
 }
 
 template <class L>
@@ -298,7 +298,7 @@ __device__ int weno6_3d_noderow(const L& load, const NodeField& F, const int* an
     float tx[6], tz[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) { tx[i] = sx + float(2 - i); tz[i] = sz + float(2 - i); }
-    const WenoCoef<float> cx = weno_coef32(tx), cz = weno_coef32(tz);
+    const WenoCoef<float> cx = weno_coef(tx), cz = weno_coef(tz);
     int kk[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) kk[i] = clampi(bz - 2 + i, F.Mz - 1);
@@ -339,7 +339,7 @@ __device__ float weno6_3d_collapse(const L& load, const NodeField& F, const int*
         ty[i] = sy + float(2 - i);
         tz[i] = sz + float(2 - i);
     }
-    const WenoCoef<float> cx = weno_coef32(tx), cy = weno_coef32(ty), cz = weno_coef32(tz);
+    const WenoCoef<float> cx = weno_coef(tx), cy = weno_coef(ty), cz = weno_coef(tz);
     int kk[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) kk[i] = clampi(bz - 2 + i, F.Mz - 1);
