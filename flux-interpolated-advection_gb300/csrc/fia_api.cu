@@ -1489,7 +1489,10 @@ int fia_debug_clip_fast(fia_session* s, int enable, unsigned long long* deferred
     return FIA_OK;
 }
 
-long long fia_debug_piece_capacity(fia_session* s) { return s ? s->pieces.cap : -1; }
+long long fia_debug_piece_capacity(fia_session* s) {
+    if (!s) return -1;
+    return s->precision == FIA_FP64 ? s->pieces64.cap : s->pieces.cap;
+}
 
 int fia_debug_solve_rhs(fia_session* s, const float* rhs, float* x, const fia_solver_params* sp,
                         fia_solver_report* rep) {

@@ -162,7 +162,10 @@ int fia_api_version(void);
 const char* fia_error_string(int code);
 
 /* Session: device-resident Grid_3D of nx*ny*nz cells (replaces the Grid_3D ctor,
- * grid_3d.cpp:13-47).  Returns NULL on failure. */
+ * grid_3d.cpp:13-47).  Returns NULL on failure.  Besides the fields it holds the store of a
+ * pass's clipped pieces, sized for 10 pieces per node of the largest field at creation
+ * (16 + 8 bytes a piece in the FP32C form, 40 in the FP64 form) and grown when a pass needs
+ * more. */
 fia_session* fia_create(int nx, int ny, int nz, double cell_length, int precision);
 void fia_destroy(fia_session* s);
 int fia_last_status(const fia_session* s);
