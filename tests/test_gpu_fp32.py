@@ -139,10 +139,11 @@ def test_fp32_plume_tracks_fp64():
     r32, v32, m32 = run_plume(32, fia.FIA_FP32C, 40)
     print("FP32 plume 32^3 after 40 steps: density rel L2 vs FP64 %.3e, velocity %s"
           % (rel(r32, r64), ", ".join("%.3e" % rel(a, b) for a, b in zip(v32, v64))))
-    # measured 1.3e-3 (density) on GB300: discontinuity flips, see the module docstring
-    assert rel(r32, r64) < 5e-3
+    # measured on GB300: density 1.0e-3, velocity 1.4-2.3e-4 (discontinuity flips, see the
+    # module docstring); the bounds are about twice that
+    assert rel(r32, r64) < 2.5e-3
     for a, b in zip(v32, v64):
-        assert rel(a, b) < 5e-3
+        assert rel(a, b) < 6e-4
     for before, after in m32:
         assert abs(after - before) <= 1e-6 * before
 
