@@ -160,6 +160,16 @@ __device__ __forceinline__ void vertex_rest_position(const PassDesc& d, int i, i
     if (d.comp >= 0) p[d.comp] -= T(1) * T(0.5) * h;
 }
 
+// uniform in [-1, 1) from a vertex index, an axis and a seed (splitmix64 finaliser)
+__device__ __forceinline__ double jitter_unit(long long id, int axis, unsigned seed) {
+    unsigned long long x = (unsigned long long)id * 3ull + (unsigned long long)axis + ((unsigned long long)seed << 40);
+    x += 0x9e3779b97f4a7c15ull;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+    x ^= x >> 31;
+    return (double)(x >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+}
+
 template <typename T>
 __global__ void k_backtrace(PassDesc d, const T* __restrict__ u, const T* __restrict__ v,
                             const T* __restrict__ w, NodeField fu, NodeField fv, NodeField fw,
@@ -186,6 +196,8 @@ __global__ void k_backtrace(PassDesc d, const T* __restrict__ u, const T* __rest
         const T vz = interp_c(d, d.interp, w, fw, h, p[0], p[1], p[2]);
         const T dt = T(d.dt);
         p[0] -= vx * dt; p[1] -= vy * dt; p[2] -= vz * dt;
+        if (d.vertex_jitter != 0.0)
+            for (int c = 0; c < 3; ++c) p[c] += T(d.vertex_jitter * jitter_unit(id, c, d.jitter_seed)) * h;
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -710,8 +722,38 @@ __device__ __forceinline__ FaceGeom<T> upper_face(const FaceGeom<T>& g) {
     return r;
 }
 
-// flux = wgt * F (acc = 0) or flux + wgt * F (acc = 1): the weighted faces of the flux
-// MacCormack scheme accumulate into one flux per face (wgt = 1, acc = 0 otherwise)
+// The flux of face id of family fam, clipped and integrated piece by piece as the clipper emits
+// them: flux = wgt * F (acc = 0) or flux + wgt * F (acc = 1) -- the weighted faces of the flux
+// MacCormack scheme accumulate into one flux per face (wgt = 1, acc = 0 otherwise).
+template <typename T>
+__device__ __forceinline__ void face_eval(const PassDesc& d, int fam, long long id, const T* __restrict__ a,
+                                          const T* __restrict__ psi, const T* __restrict__ verts,
+                                          T* __restrict__ flux, T* __restrict__ flux_rev, T wgt, int acc,
+                                          T* __restrict__ fvol, T* __restrict__ fvol_rev, unsigned& st,
+                                          int& npieces, int& nmulti) {
+    FaceGeom<T> g;
+    face_geom(d, fam, id, verts, g);
+    bool multi = false;
+    T V = T(0), Vr = T(0);
+    const T F = clip_face(d, g, EvalPiece<T>{d, a, psi, fvol ? &V : nullptr}, st, npieces, multi);
+    T Fr = -F;
+    Vr = -V;
+    if (multi) {
+        const FaceGeom<T> r = upper_face(g);
+        int np2 = 0; bool m2 = false;
+        Vr = T(0);
+        Fr = clip_face(d, r, EvalPiece<T>{d, a, psi, fvol ? &Vr : nullptr}, st, np2, m2);
+        ++nmulti;
+    }
+    if (!isfinite(F) || !isfinite(Fr)) st |= ST_NONFINITE;
+    flux[id] = acc ? flux[id] + wgt * F : wgt * F;
+    flux_rev[id] = acc ? flux_rev[id] + wgt * Fr : wgt * Fr;
+    if (fvol) {
+        fvol[id] = acc ? fvol[id] + wgt * V : wgt * V;
+        fvol_rev[id] = acc ? fvol_rev[id] + wgt * Vr : wgt * Vr;
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(128) k_faces(PassDesc d, int fam, const T* __restrict__ a,
                                                const T* __restrict__ psi, const T* __restrict__ verts,
@@ -723,29 +765,7 @@ __global__ void __launch_bounds__(128) k_faces(PassDesc d, int fam, const T* __r
     const long long nface = (long long)Fx * Fy * Fz;
     unsigned st = 0;
     int npieces = 0, nmulti = 0;
-    if (id < nface) {
-        FaceGeom<T> g;
-        face_geom(d, fam, id, verts, g);
-        bool multi = false;
-        T V = T(0), Vr = T(0);
-        const T F = clip_face(d, g, EvalPiece<T>{d, a, psi, fvol ? &V : nullptr}, st, npieces, multi);
-        T Fr = -F;
-        Vr = -V;
-        if (multi) {
-            const FaceGeom<T> r = upper_face(g);
-            int np2 = 0; bool m2 = false;
-            Vr = T(0);
-            Fr = clip_face(d, r, EvalPiece<T>{d, a, psi, fvol ? &Vr : nullptr}, st, np2, m2);
-            ++nmulti;
-        }
-        if (!isfinite(F) || !isfinite(Fr)) st |= ST_NONFINITE;
-        flux[id] = acc ? flux[id] + wgt * F : wgt * F;
-        flux_rev[id] = acc ? flux_rev[id] + wgt * Fr : wgt * Fr;
-        if (fvol) {
-            fvol[id] = acc ? fvol[id] + wgt * V : wgt * V;
-            fvol_rev[id] = acc ? fvol_rev[id] + wgt * Vr : wgt * Vr;
-        }
-    }
+    if (id < nface) face_eval(d, fam, id, a, psi, verts, flux, flux_rev, wgt, acc, fvol, fvol_rev, st, npieces, nmulti);
     // warp-aggregated counters and status
     unsigned long long pc = (unsigned long long)npieces;
     unsigned fc = id < nface ? 1u : 0u, mc = (unsigned)nmulti;
@@ -775,13 +795,13 @@ constexpr int kMaxPieces64 = 64;   // pieces of one face, both clips (as the FP3
 struct StorePiece64 {
     double4_32a* p;
     int* n;
-    unsigned* st;
+    bool* spill;   // the face has more pieces than the buffer: it is evaluated by k_faces_deferred64
     __device__ __forceinline__ double operator()(const FaceGeom<double>& g, const double* px, const double* py, int num,
                                                  double cxi, double ceta) const {
+        if (*n >= kMaxPieces64) { *spill = true; return 0.0; }
         double cx, cy, cz, ny;
         piece_geom(g, px, py, num, cxi, ceta, cx, cy, cz, ny);
-        if (*n < kMaxPieces64) p[(*n)++] = make_double4_32a(cx, cy, cz, ny);
-        else *st |= ST_CLIP_OVERFLOW;
+        p[(*n)++] = make_double4_32a(cx, cy, cz, ny);
         return 0.0;
     }
 };
@@ -797,17 +817,23 @@ __global__ void __launch_bounds__(128) k_clip64(PassDesc d, int fam, const doubl
     const int lane = threadIdx.x & 31;
     unsigned st = 0;
     int npieces = 0, n = 0, nfwd = 0;
-    bool multi = false;
+    bool multi = false, spill = false;
     double4_32a buf[kMaxPieces64];
     if (id < nface) {
         FaceGeom<double> g;
         face_geom(d, fam, id, verts, g);
-        clip_face(d, g, StorePiece64{buf, &n, &st}, st, npieces, multi);
+        clip_face(d, g, StorePiece64{buf, &n, &spill}, st, npieces, multi);
         nfwd = n;
         if (multi) {
             int np2 = 0;
             bool m2 = false;
-            clip_face(d, upper_face(g), StorePiece64{buf, &n, &st}, st, np2, m2);
+            clip_face(d, upper_face(g), StorePiece64{buf, &n, &spill}, st, np2, m2);
+        }
+        if (spill) {
+            // too many pieces for the buffer (triangulated faces at high CFL): the face is
+            // listed and evaluated as a whole by k_faces_deferred64
+            n = 0;
+            ps.deferred[atomicAdd(ps.count + 1, 1u)] = (fam << 29) | (int)id;
         }
     }
     const long long start = warp_slots(ps.count, n, lane);
@@ -816,7 +842,8 @@ __global__ void __launch_bounds__(128) k_clip64(PassDesc d, int fam, const doubl
         // store and clips again
         if (start + n <= ps.cap)
             for (int q = 0; q < n; ++q) ps.rec[start + q] = buf[q];
-        range64(ps, fam)[id] = make_int2((int)start, nfwd | ((n - nfwd) << 15) | ((multi ? 1 : 0) << 30));
+        range64(ps, fam)[id] = spill ? make_int2(-1, 0)
+                                     : make_int2((int)start, nfwd | ((n - nfwd) << 15) | ((multi ? 1 : 0) << 30));
     }
     unsigned long long pc = (unsigned long long)npieces;
     unsigned fc = id < nface ? 1u : 0u, mc = multi ? 1u : 0u;
@@ -852,6 +879,7 @@ __global__ void k_facesum64(PassDesc d, int fam, PieceStore64 ps, double* __rest
     const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= nface) return;
     const int2 r = range64(ps, fam)[id];
+    if (r.x < 0) return;   // a listed face: k_faces_deferred64 writes it
     const int nf = r.y & 0x7fff, nr = (r.y >> 15) & 0x7fff;
     const bool multi = (r.y >> 30) & 1;
     double F = 0.0, V = 0.0;
@@ -874,6 +902,31 @@ __global__ void k_facesum64(PassDesc d, int fam, PieceStore64 ps, double* __rest
         fvol[id] = acc ? fvol[id] + wgt * V : wgt * V;
         fvol_rev[id] = acc ? fvol_rev[id] + wgt * Vr : wgt * Vr;
     }
+}
+
+// The faces k_clip64 listed (all families), evaluated as k_faces does; their counters were
+// counted by k_clip64.  Grid-stride over the list length in ps.count[1].
+__global__ void __launch_bounds__(128) k_faces_deferred64(PassDesc d, const double* __restrict__ a,
+                                                          const double* __restrict__ psi,
+                                                          const double* __restrict__ verts, PieceStore64 ps,
+                                                          double* fx, double* fy, double* fz, double* rx, double* ry,
+                                                          double* rz, unsigned* status, double wgt, int acc,
+                                                          double* vx, double* vy, double* vz, double* vrx,
+                                                          double* vry, double* vrz) {
+    const long long nd = (long long)ps.count[1];
+    unsigned st = 0;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nd; t += (long long)gridDim.x * blockDim.x) {
+        const int tag = ps.deferred[t];
+        const int fam = tag >> 29;
+        const long long id = tag & ((1 << 29) - 1);
+        int np = 0, nm = 0;
+        double* f = fam == 0 ? fx : (fam == 1 ? fy : fz);
+        double* r = fam == 0 ? rx : (fam == 1 ? ry : rz);
+        double* v = vx ? (fam == 0 ? vx : (fam == 1 ? vy : vz)) : nullptr;
+        double* vr = vx ? (fam == 0 ? vrx : (fam == 1 ? vry : vrz)) : nullptr;
+        face_eval(d, fam, id, a, psi, verts, f, r, wgt, acc, v, vr, st, np, nm);
+    }
+    if (st) atomicOr(status, st);
 }
 
 // rho'(i,j,k) = (Fx(i+1) + Rx(i) + Fy(j+1) + Ry(j) + Fz(k+1) + Rz(k)) / V, where F is the
@@ -951,7 +1004,7 @@ static cudaError_t face_stage64(const PassDesc& d, const double* a, const PassWo
     }
     unsigned npc = 0;
     for (int attempt = 0; attempt < 2; ++attempt) {
-        cudaError_t e = cudaMemsetAsync(ps.count, 0, sizeof(unsigned), s);
+        cudaError_t e = cudaMemsetAsync(ps.count, 0, 2 * sizeof(unsigned), s);
         if (e != cudaSuccess) return e;
         for (int fam = 0; fam < 3; ++fam)
             k_clip64<<<blocks_for(nface[fam], 128), 128, 0, s>>>(d, fam, verts, ps, w.status, w.counters);
@@ -975,6 +1028,12 @@ static cudaError_t face_stage64(const PassDesc& d, const double* a, const PassWo
         k_facesum64<<<blocks_for(nface[fam], 256), 256, 0, s>>>(d, fam, ps, w.flux[fam], w.flux_rev[fam], w.status, wgt,
                                                               acc, d.volumes ? w.fvol[fam] : nullptr,
                                                               d.volumes ? w.fvol_rev[fam] : nullptr);
+    const bool vol = d.volumes != 0;
+    k_faces_deferred64<<<152, 128, 0, s>>>(d, a, w.psi, verts, ps, w.flux[0], w.flux[1], w.flux[2], w.flux_rev[0],
+                                           w.flux_rev[1], w.flux_rev[2], w.status, wgt, acc,
+                                           vol ? w.fvol[0] : nullptr, vol ? w.fvol[1] : nullptr,
+                                           vol ? w.fvol[2] : nullptr, vol ? w.fvol_rev[0] : nullptr,
+                                           vol ? w.fvol_rev[1] : nullptr, vol ? w.fvol_rev[2] : nullptr);
     return cudaGetLastError();
 }
 
@@ -1005,7 +1064,7 @@ cudaError_t piece_store64_reserve(PieceStore64& p, long long pieces, long long f
         p.cap = pieces;
     }
     if (!p.count) {
-        cudaError_t e = cudaMalloc(&p.count, sizeof(unsigned));
+        cudaError_t e = cudaMalloc(&p.count, 2 * sizeof(unsigned));
         if (e != cudaSuccess) return e;
     }
     if (!p.range[0]) {
@@ -1013,12 +1072,14 @@ cudaError_t piece_store64_reserve(PieceStore64& p, long long pieces, long long f
             cudaError_t e = cudaMalloc(&p.range[f], faces_per_family * sizeof(int2));
             if (e != cudaSuccess) return e;
         }
+        cudaError_t e = cudaMalloc(&p.deferred, 3 * faces_per_family * sizeof(int));
+        if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
 }
 
 void piece_store64_free(PieceStore64& p) {
-    cudaFree(p.rec); cudaFree(p.flux); cudaFree(p.count);
+    cudaFree(p.rec); cudaFree(p.flux); cudaFree(p.count); cudaFree(p.deferred);
     for (int f = 0; f < 3; ++f) cudaFree(p.range[f]);
     p = PieceStore64();
 }

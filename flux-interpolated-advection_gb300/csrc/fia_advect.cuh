@@ -21,6 +21,8 @@ struct PassDesc {
     int maccormack;         // flux MacCormack: faces at rest (0.5), backtraced (1), traced back (-0.5)
     int volumes;            // also sum y n_y of the pieces per face into PassWork::fvol (cell volumes)
     int full_weno;          // FP64 form: evaluate every WENO6 in full (no collapse on node planes)
+    double vertex_jitter;   // FP64 form, sensitivity studies: backtraced vertices moved by up to this many
+    unsigned jitter_seed;   //   cells, independently per vertex and axis (a hash of vertex, axis and seed)
     double color_off[2];    // split method: colour = x/h - off0, z/h - off1
     int k;                  // Gauss points per half cell
     double gx[kMaxGauss];   // Gauss nodes on [-1,1] (centre first, then -/+ pairs)
@@ -72,7 +74,8 @@ struct PieceStore64 {
     double4_32a* rec = nullptr;      // (cx, cy, cz, ny): centroid (absolute), y component of the scaled normal
     double* flux = nullptr;      // flux of each piece
     int2* range[3] = {nullptr, nullptr, nullptr};   // per face: start, nfwd | nrev << 15 | multi << 30
-    unsigned* count = nullptr;   // device counter: pieces appended
+    unsigned* count = nullptr;   // device counters: [0] pieces appended, [1] faces listed for whole-face evaluation
+    int* deferred = nullptr;     // those faces (family << 29 | face index), room for every face
     long long cap = 0;           // pieces the buffers hold
 };
 cudaError_t piece_store64_reserve(PieceStore64& p, long long pieces, long long faces_per_family);

@@ -60,6 +60,8 @@ struct fia_session {
     bool fcg_ready = false;
     double* p64 = nullptr;       // FP32 form: pressure accumulated in FP64 by the refinement
     int full_weno = 0;           // FP64 form: no WENO6 collapse on node planes (fia_debug_full_weno)
+    double vertex_jitter = 0.0;  // FP64 form: backtraced vertices jittered (fia_debug_vertex_jitter)
+    mutable unsigned jitter_calls = 0;
     // clipped pieces of a pass (FP64 form); piece_pipeline 0: one thread per face instead
     PieceStore64 pieces64;
     int piece_pipeline = 1;
@@ -206,6 +208,10 @@ PassDesc base_desc(const fia_session* s, int comp, double dt) {
     d.h = s->h;
     d.dt = dt;
     d.full_weno = s->full_weno;
+    if (s->vertex_jitter != 0.0) {
+        d.vertex_jitter = s->vertex_jitter;
+        d.jitter_seed = ++s->jitter_calls;
+    }
     return d;
 }
 
@@ -1460,6 +1466,12 @@ int fia_debug_set_piece_capacity(fia_session* s, long long pieces) {
     piece_store_free(s->pieces);
     s->pieces.clip_fast = fast;
     CK(piece_store_reserve(s->pieces, pieces, big));
+    return FIA_OK;
+}
+
+int fia_debug_vertex_jitter(fia_session* s, double cells) {
+    if (!s || s->precision != FIA_FP64 || !(cells >= 0.0) || cells > 0.5) return FIA_ERR_INVALID;
+    s->vertex_jitter = cells;
     return FIA_OK;
 }
 

@@ -185,6 +185,7 @@ def _declare(lib):
     lib.fia_debug_clip_fast.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_ulonglong)]
     lib.fia_debug_full_weno.argtypes = [vp, ip]
     lib.fia_debug_piece_pipeline.argtypes = [vp, ip]
+    lib.fia_debug_vertex_jitter.argtypes = [vp, ctypes.c_double]
     lib.fia_debug_learned_grad.argtypes = [vp, ip, fp, dp]
     lib.fia_debug_grid_op.argtypes = [vp, ip, fp, fp]
     lib.fia_debug_solve_rhs.argtypes = [vp, fp, fp, ctypes.POINTER(SolverParams), ctypes.POINTER(SolverReport)]
@@ -509,6 +510,11 @@ class Grid3D:
         """FP64 form: 1 runs the faces as the piece pipeline (default), 0 as one thread per face,
         -1 leaves it; returns the setting"""
         return _check(self.lib.fia_debug_piece_pipeline(self.s, enable), "fia_debug_piece_pipeline")
+
+    def debug_vertex_jitter(self, cells):
+        """FP64 form: move every backtraced vertex by up to `cells` cells per axis (independent,
+        hashed, per pass); 0 switches it off"""
+        _check(self.lib.fia_debug_vertex_jitter(self.s, ctypes.c_double(cells)), "fia_debug_vertex_jitter")
 
     def debug_precondition(self, r):
         a = np.ascontiguousarray(r, dtype=np.float32).ravel()

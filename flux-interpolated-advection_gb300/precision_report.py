@@ -4,7 +4,7 @@ with relative L2 differences of density and velocity between every pair of arms 
 numbers of steps ("a|b": |a - b| / |b|), and each arm's mass drift.
 
     python precision_report.py [--grid 64] [--steps 25,50,100] [--cfl 2]
-                               [--arm NAME:PRECISION:TOL[:SOLVER[:DRHO[:DU]]]] ...
+                               [--arm NAME:PRECISION:TOL[:SOLVER[:DRHO[:DU[:DV]]]]] ...
 
 PRECISION is fp64 (plain form) or fp32c (chosen form); TOL the pressure tolerance (FP64
 residual in both forms); SOLVER pcg (Jacobi-PCG) or learned (flexible CG with the committed
@@ -13,7 +13,9 @@ source sphere holds 1 + DRHO * xi with xi seeded uniform in [0, 1) per cell (the
 re-injects max(density, 1), so the perturbation is kept); DU a relative jitter of the velocity
 after every step: each face velocity times 1 + DU * xi, xi seeded uniform in [-1, 1) (DU of
 about 6e-8 is the size of FP32 rounding, so an FP64 arm with it measures how far the scheme
-carries FP32-sized perturbations made at every step).  Without --arm the chosen form (fp32c,
+carries FP32-sized perturbations made at every step); DV (fp64 only) moves every backtraced
+vertex by up to DV cells per axis, independently per vertex, axis and pass (the rounding of
+FP32 vertex positions is about 1e-7 cells).  Without --arm the chosen form (fp32c,
 Jacobi-PCG) is compared with the plain form at --tol.
 
 Every arm starts from the plume density (sphere r = 0.1 at (0.5, 0.15, 0.5)) at rest, with
@@ -40,12 +42,14 @@ def rel(a, b):
 def parse_arm(spec, default_tol):
     f = spec.split(":")
     if len(f) < 2 or f[1] not in ("fp64", "fp32c"):
-        raise SystemExit("bad --arm %r (NAME:PRECISION:TOL[:SOLVER[:DRHO[:DU]]])" % spec)
+        raise SystemExit("bad --arm %r (NAME:PRECISION:TOL[:SOLVER[:DRHO[:DU[:DV]]]])" % spec)
     arm = {"name": f[0], "precision": f[1], "tol": float(f[2]) if len(f) > 2 and f[2] else default_tol,
            "solver": f[3] if len(f) > 3 and f[3] else "pcg", "drho": float(f[4]) if len(f) > 4 and f[4] else 0.0,
-           "du": float(f[5]) if len(f) > 5 and f[5] else 0.0}
+           "du": float(f[5]) if len(f) > 5 and f[5] else 0.0, "dv": float(f[6]) if len(f) > 6 and f[6] else 0.0}
     if arm["solver"] not in ("pcg", "learned") or (arm["solver"] == "learned" and arm["precision"] != "fp32c"):
         raise SystemExit("bad solver in --arm %r" % spec)
+    if arm["dv"] and arm["precision"] != "fp64":
+        raise SystemExit("vertex jitter is an fp64 arm option: %r" % spec)
     return arm
 
 
@@ -72,6 +76,8 @@ def main():
             xi = np.random.Generator(np.random.PCG64(args.seed)).uniform(0.0, 1.0, size=rho.size)
             rho = rho * (1.0 + arm["drho"] * xi)
         g.set("density", rho)
+        if arm["dv"]:
+            g.debug_vertex_jitter(arm["dv"])
         for c, m in (("u", (n + 1) * n * n), ("v", n * (n + 1) * n), ("w", n * n * (n + 1))):
             g.set(c, np.zeros(m))
         solver = {"tol": arm["tol"], "max_iter": 50000}
@@ -81,7 +87,7 @@ def main():
         arm.update(grid=g, params=fia.step_params(cfl=args.cfl, solver=solver), masses=[], seconds=0.0,
                    status=0, rng=np.random.Generator(np.random.PCG64(args.seed + 1)))
     out = {"grid": n, "cfl": args.cfl,
-           "arms": [{k: a[k] for k in ("name", "precision", "tol", "solver", "drho", "du")} for a in arms],
+           "arms": [{k: a[k] for k in ("name", "precision", "tol", "solver", "drho", "du", "dv")} for a in arms],
            "checkpoints": []}
     step = 0
     for cp in checkpoints:

@@ -326,6 +326,11 @@ int fia_debug_full_weno(fia_session* s, int enable);
  * same arithmetic and order of sums), -1 leaves it; returns the setting (0 for an FP32C
  * session, which always runs its own piece pipeline). */
 int fia_debug_piece_pipeline(fia_session* s, int enable);
+/* FP64 form, for sensitivity studies: every backtraced vertex of every later pass is moved by
+ * up to `cells` cells (0 <= cells <= 0.5; 0, the default, switches it off) along each axis,
+ * independently per vertex, axis and pass (a hash, uniform in [-cells, cells)), before the
+ * clamp: perturbations of the size of FP32 rounding of the vertex positions. */
+int fia_debug_vertex_jitter(fia_session* s, double cells);
 
 /* Test hooks: single pieces of the path on host data (FP64 buffers), mirroring the oracle. */
 /* one flux pass of a node field (comp -1 density, 0..2 velocity) with the session velocity */

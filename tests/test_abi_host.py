@@ -66,6 +66,7 @@ def test_null_session_is_rejected_by_every_entry_point(lib):
         "fia_debug_clip_fast": lambda: lib.fia_debug_clip_fast(None, 1, ctypes.byref(n)),
         "fia_debug_full_weno": lambda: lib.fia_debug_full_weno(None, 1),
         "fia_debug_piece_pipeline": lambda: lib.fia_debug_piece_pipeline(None, 1),
+        "fia_debug_vertex_jitter": lambda: lib.fia_debug_vertex_jitter(None, 1e-7),
     }
     for name, call in calls.items():
         assert call() == fia.FIA_ERR_INVALID, name
@@ -151,9 +152,11 @@ def test_precision_report_arm_specs():
     a = pr.parse_arm("p64:fp64:1e-6", 1e-8)
     assert (a["name"], a["precision"], a["tol"], a["solver"], a["drho"], a["du"]) == ("p64", "fp64", 1e-6, "pcg", 0.0, 0.0)
     a = pr.parse_arm("j:fp64:1e-6:pcg:1e-7:6e-8", 1e-8)
-    assert (a["drho"], a["du"]) == (1e-7, 6e-8)
+    assert (a["drho"], a["du"], a["dv"]) == (1e-7, 6e-8, 0.0)
+    a = pr.parse_arm("v:fp64:1e-6:pcg:0:0:1e-7", 1e-8)
+    assert (a["drho"], a["du"], a["dv"]) == (0.0, 0.0, 1e-7)
     a = pr.parse_arm("c:fp32c::learned", 1e-8)
     assert (a["tol"], a["solver"]) == (1e-8, "learned")
-    for bad in ("x", "x:fp16:1e-6", "x:fp64:1e-6:learned", "x:fp32c:1e-6:amg"):
+    for bad in ("x", "x:fp16:1e-6", "x:fp64:1e-6:learned", "x:fp32c:1e-6:amg", "x:fp32c:1e-6:pcg:0:0:1e-7"):
         with pytest.raises(SystemExit):
             pr.parse_arm(bad, 1e-8)

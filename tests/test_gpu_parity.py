@@ -309,3 +309,24 @@ def test_fp64_piece_pipeline_matches_per_face_kernel(name, kw, cfl):
         assert np.array_equal(b, c), name
     assert counts[0] == counts[1], name            # faces, pieces, faces clipped twice
     assert stats[0] == stats[1] == stats[2], name
+
+
+def test_fp64_vertex_jitter_is_a_small_perturbation():
+    """The sensitivity hook of the plain form: backtraced vertices jittered by 1e-7 cells change
+    a density step by a small nonzero amount; switched off, the step is the plain one."""
+    outs = []
+    for amp in (0.0, 1e-7, 0.0):
+        g, h, u, v, w, rho, dt = make(16, 16, 16, seed=13)
+        if amp:
+            g.debug_vertex_jitter(amp)
+        g.move_substances_3D(dt, fia.advect_params())
+        outs.append(g.get("density"))
+        g.close()
+    assert np.array_equal(outs[0], outs[2])
+    assert 0.0 < rel(outs[1], outs[0]) < 1e-4
+    with pytest.raises(fia.FiaError):
+        g32 = fia.Grid3D(8, 8, 8, 1.0 / 8, precision=fia.FIA_FP32C)
+        try:
+            g32.debug_vertex_jitter(1e-7)
+        finally:
+            g32.close()
