@@ -1003,8 +1003,13 @@ static cudaError_t face_stage64(const PassDesc& d, const double* a, const PassWo
         big = nface[fam] > big ? nface[fam] : big;
     }
     unsigned npc = 0;
+    // the work counters as they were before the clip: a second attempt starts from them again
+    cudaError_t ec = cudaMemcpyAsync(ps.saved, w.counters, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, s);
+    if (ec != cudaSuccess) return ec;
     for (int attempt = 0; attempt < 2; ++attempt) {
         cudaError_t e = cudaMemsetAsync(ps.count, 0, 2 * sizeof(unsigned), s);
+        if (e == cudaSuccess && attempt > 0)
+            e = cudaMemcpyAsync(w.counters, ps.saved, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, s);
         if (e != cudaSuccess) return e;
         for (int fam = 0; fam < 3; ++fam)
             k_clip64<<<blocks_for(nface[fam], 128), 128, 0, s>>>(d, fam, verts, ps, w.status, w.counters);
@@ -1012,8 +1017,7 @@ static cudaError_t face_stage64(const PassDesc& d, const double* a, const PassWo
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return e;
         if ((long long)npc <= ps.cap) break;
-        // more pieces than the store holds: grow it and clip again (the counters of the first
-        // attempt stay counted)
+        // more pieces than the store holds: grow it and clip again
         e = piece_store64_reserve(ps, (long long)npc + npc / 4 + 1024, big);
         if (e != cudaSuccess) return e;
     }
@@ -1065,6 +1069,7 @@ cudaError_t piece_store64_reserve(PieceStore64& p, long long pieces, long long f
     }
     if (!p.count) {
         cudaError_t e = cudaMalloc(&p.count, 2 * sizeof(unsigned));
+        if (e == cudaSuccess) e = cudaMalloc(&p.saved, 5 * sizeof(unsigned long long));
         if (e != cudaSuccess) return e;
     }
     if (!p.range[0]) {
@@ -1079,7 +1084,7 @@ cudaError_t piece_store64_reserve(PieceStore64& p, long long pieces, long long f
 }
 
 void piece_store64_free(PieceStore64& p) {
-    cudaFree(p.rec); cudaFree(p.flux); cudaFree(p.count); cudaFree(p.deferred);
+    cudaFree(p.rec); cudaFree(p.flux); cudaFree(p.count); cudaFree(p.deferred); cudaFree(p.saved);
     for (int f = 0; f < 3; ++f) cudaFree(p.range[f]);
     p = PieceStore64();
 }

@@ -61,6 +61,7 @@ struct PieceStore {
     unsigned* count = nullptr;   // device counters: [0] pieces, [1] faces listed for the local-memory clipper
     int* deferred = nullptr;     // those faces (family << 29 | face index), room for every face
     float4* rest = nullptr;      // the pieces of a face at rest (same for every face of a family)
+    unsigned long long* saved = nullptr;   // the session's work counters before a clip (restored on a retry)
     long long cap = 0;           // pieces the buffers hold
     int clip_fast = 1;           // 0: every face through the local-memory clipper
 };
@@ -76,6 +77,7 @@ struct PieceStore64 {
     int2* range[3] = {nullptr, nullptr, nullptr};   // per face: start, nfwd | nrev << 15 | multi << 30
     unsigned* count = nullptr;   // device counters: [0] pieces appended, [1] faces listed for whole-face evaluation
     int* deferred = nullptr;     // those faces (family << 29 | face index), room for every face
+    unsigned long long* saved = nullptr;   // the session's work counters before a clip (restored on a retry)
     long long cap = 0;           // pieces the buffers hold
 };
 cudaError_t piece_store64_reserve(PieceStore64& p, long long pieces, long long faces_per_family);

@@ -620,8 +620,13 @@ static cudaError_t face_stage32(const PassDesc& d, const float* a, const float2*
     if (ea == cudaSuccess)
         ea = cudaFuncSetAttribute(k_clip32, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
     if (ea != cudaSuccess) return ea;
+    // the work counters as they were before the clip: a second attempt starts from them again
+    ea = cudaMemcpyAsync(ps.saved, w.counters, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, s);
+    if (ea != cudaSuccess) return ea;
     for (int attempt = 0; attempt < 2; ++attempt) {
         cudaMemsetAsync(ps.count, 0, 2 * sizeof(unsigned), s);
+        if (attempt > 0)
+            cudaMemcpyAsync(w.counters, ps.saved, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, s);
         if (rest && ps.clip_fast) {
             k_rest_clip32<<<1, 32, 0, s>>>(d, 1, ps);
             k_rest_fill32<<<nblk(nface[1], 256), 256, 0, s>>>(d, 1, ps, w.status, w.counters);
@@ -636,8 +641,7 @@ static cudaError_t face_stage32(const PassDesc& d, const float* a, const float2*
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return e;
         if ((long long)npc <= ps.cap) break;
-        // more pieces than the store holds: grow it and clip again (counters of the first
-        // attempt stay counted)
+        // more pieces than the store holds: grow it and clip again
         e = piece_store_reserve(ps, (long long)npc + npc / 4 + 1024, std::max(nface[0], std::max(nface[1], nface[2])));
         if (e != cudaSuccess) return e;
     }
@@ -710,6 +714,7 @@ cudaError_t piece_store_reserve(PieceStore& p, long long pieces, long long faces
     }
     if (!p.count) {
         cudaError_t e = cudaMalloc(&p.count, 2 * sizeof(unsigned));
+        if (e == cudaSuccess) e = cudaMalloc(&p.saved, 5 * sizeof(unsigned long long));
         if (e != cudaSuccess) return e;
     }
     if (!p.range[0]) {
@@ -727,6 +732,7 @@ cudaError_t piece_store_reserve(PieceStore& p, long long pieces, long long faces
 
 void piece_store_free(PieceStore& p) {
     cudaFree(p.rec); cudaFree(p.face); cudaFree(p.flux); cudaFree(p.count); cudaFree(p.deferred); cudaFree(p.rest);
+    cudaFree(p.saved);
     for (int f = 0; f < 3; ++f) { cudaFree(p.range[f]); cudaFree(p.normal[f]); }
     p = PieceStore();
 }

@@ -7,11 +7,12 @@
 Runs --warmup + --steps steps of the plume (source r = 0.1 at (0.5, 0.15, 0.5), buoyancy 1)
 in the developed flow of bench.py scaled to the given CFL, with --spheres solid spheres of
 radius U[0.04, 0.1] (seed 7, kept clear of the source), FP32 advection and flexible CG with
-the learned preconditioner (Jacobi-PCG after --fallback-iter iterations).  Reports steps/s
-(device time), pieces per face, pressure iterations and fallbacks, the largest velocity and
-the mass.  The plain FP64 form is too slow to run at this size (about a minute per step at
-256^3), so the difference between the forms is measured on --compare-grid with the same
-settings.  Prints one JSON line.
+the learned preconditioner (Jacobi-PCG after --fallback-iter iterations; by default the
+weights trained with solid-heavy CFL-4 runs, weights/unet_precond_solids.f32).  Reports
+steps/s (device time), pieces per face, pressure iterations and fallbacks, the largest
+velocity and the mass.  The plain FP64 form is too slow to run many steps at this size, so the
+difference between the forms is measured on --compare-grid with the same settings.  Prints
+one JSON line.
 """
 import argparse
 import json
@@ -70,7 +71,7 @@ def main():
     ap.add_argument("--fallback-iter", type=int, default=200)
     ap.add_argument("--compare-grid", type=int, default=64)
     ap.add_argument("--compare-steps", type=int, default=20)
-    ap.add_argument("--weights", default=os.path.join(HERE, "weights", "unet_precond.f32"))
+    ap.add_argument("--weights", default=os.path.join(HERE, "weights", "unet_precond_solids.f32"))
     args = ap.parse_args()
     import torch
     n = args.grid
