@@ -325,31 +325,8 @@ __global__ void __launch_bounds__(kClipThreads, 4) k_clip32(PassDesc d, int fam,
     extern __shared__ float clip_smem[];
     const FastPool P{clip_smem + threadIdx.x};
     const int Fx = d.A.Mx + (fam == 0), Fy = d.A.My + (fam == 1), Fz = d.A.Mz + (fam == 2);
-    long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long nface = (long long)Fx * Fy * Fz;
-    if (kClipSort) {
-        // counting sort of the CTA's faces by clip class (the sort's words follow the pool)
-        int* hist = reinterpret_cast<int*>(clip_smem + kFastWords * kClipThreads);
-        int* order = hist + kClipClasses;
-        int key = kClipClasses - 1;   // past the last face: last
-        if (id < nface) {
-            LocalFace g0;
-            face_geometry(d, fam, id, disp, g0);
-            key = clip_class(d, g0);
-        }
-        if (threadIdx.x < kClipClasses) hist[threadIdx.x] = 0;
-        __syncthreads();
-        atomicAdd(&hist[key], 1);
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int run = 0;
-            for (int c = 0; c < kClipClasses; ++c) { const int n = hist[c]; hist[c] = run; run += n; }
-        }
-        __syncthreads();
-        order[atomicAdd(&hist[key], 1)] = threadIdx.x;
-        __syncthreads();
-        id = (long long)blockIdx.x * blockDim.x + order[threadIdx.x];
-    }
     const int lane = threadIdx.x & 31;
     int npieces = 0, nst = 0, nfwd = 0;
     bool multi = false, ok = false;
@@ -639,8 +616,7 @@ static cudaError_t face_stage32(const PassDesc& d, const float* a, const float2*
         }
     }
     unsigned npc = 0;
-    const int smem = kClipSmem + (kClipSort ? kClipSortSmem : 0);
-    cudaError_t ea = cudaFuncSetAttribute(k_clip32, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaError_t ea = cudaFuncSetAttribute(k_clip32, cudaFuncAttributeMaxDynamicSharedMemorySize, kClipSmem);
     if (ea == cudaSuccess)
         ea = cudaFuncSetAttribute(k_clip32, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
     if (ea != cudaSuccess) return ea;
@@ -657,7 +633,7 @@ static cudaError_t face_stage32(const PassDesc& d, const float* a, const float2*
         } else {
             for (int fam = 0; fam < 3; ++fam)
                 if (!rest || fam == 1)
-                    k_clip32<<<nblk(nface[fam], kClipThreads), kClipThreads, smem, s>>>(d, fam, disp, ps, w.status,
+                    k_clip32<<<nblk(nface[fam], kClipThreads), kClipThreads, kClipSmem, s>>>(d, fam, disp, ps, w.status,
                                                                                              w.counters, ps.clip_fast);
             k_clip32_deferred<<<152 * 8, 128, 0, s>>>(d, disp, ps, w.status, w.counters);
         }

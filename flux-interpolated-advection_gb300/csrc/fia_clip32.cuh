@@ -286,29 +286,7 @@ static __host__ __device__ void clip32(const PassDesc& d, const LocalFace& g, un
 constexpr int kFastR = 26, kFastS = 6, kClipThreads = 128;
 constexpr int kFastWords = 4 * kFastR + kFastS;
 constexpr int kClipSmem = kFastWords * kClipThreads * (int)sizeof(float);   // 56,320 B: 4 CTAs per SM
-// Before clipping, each CTA orders its faces by clip class (the number of iso-lines of each
-// colour the face's corners span, 0-3 each) so that the lanes of a warp run similar numbers of
-// cuts; the order of faces within the store changes, the pieces of each face do not.
-constexpr bool kClipSort = true;
-constexpr int kClipClasses = 16;
-constexpr int kClipSortSmem = (kClipClasses + kClipThreads) * (int)sizeof(int);
-static_assert(4 * (kClipSmem + kClipSortSmem + 1024) <= 233472, "four clip CTAs per SM");
-
-// clip class of a face: iso-lines spanned by its corners' colours, capped at 3 per colour
-__host__ __device__ __forceinline__ int clip_class(const PassDesc& d, const LocalFace& g) {
-    int c[2];
-#pragma unroll
-    for (int dim = 0; dim < 2; ++dim) {
-        const float* v = dim == 0 ? g.x : g.z;
-        float mn = v[0], mx = v[0];
-#pragma unroll
-        for (int q = 1; q < 4; ++q) { mn = fminf(mn, v[q]); mx = fmaxf(mx, v[q]); }
-        const float off = d.color_off_f[dim];
-        const float span = floorf(mx - off) - ceilf(mn - off) + 1.f;
-        c[dim] = span >= 3.f ? 3 : (span >= 1.f ? (int)span : 0);   // false for NaN: class 0
-    }
-    return c[0] * 4 + c[1];
-}
+static_assert(4 * (kClipSmem + 1024) <= 233472, "four clip CTAs per SM");
 
 #ifndef __CUDA_ARCH__
 // host builds of the clipper (the host check of the shared-pool clipper) stop on a slot outside
