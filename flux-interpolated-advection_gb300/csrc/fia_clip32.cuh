@@ -26,7 +26,9 @@ struct LocalFace {
     float x[4], y[4], z[4];   // vertex positions in cells relative to the anchor
 };
 
-constexpr int kMaxPieces32 = 64;   // pieces of one face, both clips (CFL 4 needs about 36 per clip)
+// pieces of one face, both clips, in the local-memory clipper (CFL 4 needs about 36 per clip;
+// triangulation at a small minimal_area several times that)
+constexpr int kMaxPieces32 = 128;
 
 // Pieces emitted by the clipper of one face: centroid (cells, relative to the face anchor)
 // and scaled y-normal, collected in order; the y-normals are summed here.

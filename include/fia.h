@@ -33,7 +33,8 @@ extern "C" {
 #define FIA_ERR_NOMEM -4        /* device allocation failed */
 
 /* status bits (positive returns, also fia_last_status) */
-#define FIA_STATUS_CLIP_OVERFLOW 1    /* a clipped piece exceeded 32 vertices (MAX_TMP_POINTS) */
+#define FIA_STATUS_CLIP_OVERFLOW 1    /* a clipped piece exceeded 32 vertices (MAX_TMP_POINTS), or in
+                                         the FP32C form a face produced more than 128 pieces */
 #define FIA_STATUS_CLIP_ODD_CUT 2     /* odd number of iso-line crossings; the reference exit(0)s */
 #define FIA_STATUS_NONFINITE 4        /* a non-finite face flux was produced */
 #define FIA_STATUS_SUBDIV_OVERFLOW 8  /* minimal_area triangulation stack exhausted */

@@ -118,4 +118,4 @@ def test_status_words_of_the_clipper(checker):
         assert st == NONFINITE and pieces == 0 and fast_ok == 0, (name, rows[name])
     for name in ("stretched", "huge"):
         st, pieces, fast_ok = rows[name]
-        assert st & OVERFLOW and pieces == 64 and fast_ok == 0, (name, rows[name])
+        assert st & OVERFLOW and pieces == 128 and fast_ok == 0, (name, rows[name])

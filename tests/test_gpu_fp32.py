@@ -196,3 +196,21 @@ def test_fp32_clip_shared_pool_matches_local_pool(cfl, minimal_area, maccormack)
         # 1.5% on GB300: at 32^3 the flow's shortest wavelength is four cells, so faces deform
         # far more than in the 256^3 plume
         assert n1 < 0.05 * n0
+
+
+def test_fp32_triangulated_high_cfl_keeps_every_piece():
+    """minimal_area 0.05 at CFL 4: the triangulation gives some faces more than 64 pieces.  The
+    chosen form's local-memory clipper holds 128 per face, so no piece is dropped (no overflow
+    bit) and the density step agrees with the plain form as a single step does."""
+    out = {}
+    for prec in (fia.FIA_FP64, fia.FIA_FP32C):
+        g, h, u, v, w, rho, dt = make(24, prec, seed=7, cfl=4.0)
+        st = g.move_substances_3D(dt, fia.advect_params(minimal_area=0.05))
+        out[prec] = (st, g.get("density"))
+        g.close()
+    (s64, r64), (s32, r32) = out[fia.FIA_FP64], out[fia.FIA_FP32C]
+    print("FP32 triangulated CFL 4: rel L2 vs FP64 %.3e, outside the worst 4 cells %.3e"
+          % (rel(r32, r64), rel_outside_worst(r32, r64, 4)))
+    assert s64 == 0 and s32 == 0
+    assert rel_outside_worst(r32, r64, 4) < 2e-5
+    assert rel(r32, r64) < 5e-4
