@@ -535,11 +535,12 @@ __device__ T emit_polygon(const PassDesc& d, const FaceGeom<T>& g, const T* px, 
         T tcx, tcy, tarea;
         centroid(tx, ty, 3, tcx, tcy, tarea);
         if (tarea > minA) {
+            // the first of the longest edges, lengths within kLongestEdgeTie counting as equal
             int mi = 0; T ml = T(-1);
             for (int n = 0; n < 3; ++n) {
                 const int m = (n + 1) % 3;
                 const T len = (tx[n] - tx[m]) * (tx[n] - tx[m]) + (ty[n] - ty[m]) * (ty[n] - ty[m]);
-                if (ml < len) { ml = len; mi = n; }
+                if (len > ml * T(1.0 + kLongestEdgeTie)) { ml = len; mi = n; }
             }
             const int i1 = (mi + 1) % 3, i2 = (mi + 2) % 3;
             const T mx = T(0.5) * (tx[mi] + tx[i1]), my = T(0.5) * (ty[mi] + ty[i1]);

@@ -8,6 +8,13 @@ namespace fia {
 
 constexpr int kMaxGauss = 15;
 
+// Triangulation of pieces above minimal_area bisects each triangle's longest edge
+// (facecutter.h:255-324).  Edges whose squared lengths agree to within this relative amount
+// count as equally long and the first of them is taken, as for an exact tie: equal lengths in
+// exact arithmetic (the fan triangles of a square) would otherwise be ordered by rounding,
+// differently in FP32 and FP64.  The oracle applies the same rule.
+constexpr double kLongestEdgeTie = 4e-6;
+
 // Everything one flux pass needs; passed to the kernels by value.
 struct PassDesc {
     NodeField A;            // advected node field (its cells are the control volumes)

@@ -156,11 +156,12 @@ static __host__ __device__ void emit32(const PassDesc& d, const LocalFace& g, co
         float tcx, tcy, ta;
         centroidf(tx, ty, 3, tcx, tcy, ta);
         if (ta > minA) {
+            // the first of the longest edges, lengths within kLongestEdgeTie counting as equal
             int mi = 0; float ml = -1.f;
             for (int n = 0; n < 3; ++n) {
                 const int m = (n + 1) % 3;
                 const float len = (tx[n] - tx[m]) * (tx[n] - tx[m]) + (ty[n] - ty[m]) * (ty[n] - ty[m]);
-                if (ml < len) { ml = len; mi = n; }
+                if (len > ml * float(1.0 + kLongestEdgeTie)) { ml = len; mi = n; }
             }
             const int i1 = (mi + 1) % 3, i2 = (mi + 2) % 3;
             const float mx = 0.5f * (tx[mi] + tx[i1]), my = 0.5f * (ty[mi] + ty[i1]);

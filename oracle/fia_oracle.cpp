@@ -371,7 +371,12 @@ static void center_of_gravity(const real (*pts)[2], int num, real* ctr, real* ar
     *area = a;
 }
 
-// facecutter.h:255-324; with the default minimal_area (1.0) a polygon is emitted as is.
+// facecutter.h:255-324; with the default minimal_area (1.0) a polygon is emitted as is.  The
+// longest edge is the first of the longest: edges whose squared lengths agree to within a
+// relative 4e-6 count as equally long (equal in exact arithmetic they are, as in a fan triangle
+// of a square, whose rounding would otherwise pick the edge differently in every precision;
+// the GPU library applies the same rule in both forms).
+constexpr real kLongestEdgeTie = 4e-6;
 static void subdivide(const real (*poly)[2], int num, real minimal_area, const PolyOut& out) {
     std::function<void(const real (*)[2])> tri_split = [&](const real (*t)[2]) {
         real ctr[2], area;
@@ -381,7 +386,7 @@ static void subdivide(const real (*poly)[2], int num, real minimal_area, const P
             for (int n = 0; n < 3; ++n) {
                 real dx = t[n][0] - t[(n + 1) % 3][0], dy = t[n][1] - t[(n + 1) % 3][1];
                 real len = dx * dx + dy * dy;
-                if (maxlen < len) { maxlen = len; maxi = n; }
+                if (len > maxlen * (1.0 + kLongestEdgeTie)) { maxlen = len; maxi = n; }
             }
             const real* p0 = t[maxi]; const real* p1 = t[(maxi + 1) % 3]; const real* p2 = t[(maxi + 2) % 3];
             real mid[2] = {0.5 * (p0[0] + p1[0]), 0.5 * (p0[1] + p1[1])};

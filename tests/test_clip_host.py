@@ -96,6 +96,52 @@ def test_fp32_clipper_pieces_match_the_oracle(checker, tmp_path):
     assert compared > 2900 and pieces > 2 * compared
 
 
+@pytest.mark.parametrize("cfl", [2.0, 4.0])
+def test_fp32_triangulated_pieces_match_the_oracle(checker, tmp_path, cfl):
+    """With minimal_area 0.05 the pieces are triangulated by longest-edge bisection
+    (facecutter.h:255-324).  The fan triangles of a square have equally long edges; both the
+    FP32 clipper and the oracle take lengths within a relative 4e-6 as equal and bisect the
+    first, so their triangles agree, and with them each face's y-normal sum and volume point
+    (sum of y n_y), which depend on the partition of a warped face.  Deformed faces up to the
+    given CFL, both colour offsets."""
+    np = pytest.importorskip("numpy")
+    from oracle import Oracle
+    O = Oracle()
+    rng = np.random.default_rng(5)
+    corners = {0: [(0, 0, 0), (0, 1, 0), (0, 1, 1), (0, 0, 1)], 1: [(0, 0, 0), (0, 0, 1), (1, 0, 1), (1, 0, 0)],
+               2: [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0)]}
+    faces, recs = [], []
+    for t in range(1500):
+        fam = t % 3
+        T = rng.uniform(-cfl, cfl, size=3)
+        v = (np.array(corners[fam], float) + T + rng.uniform(-0.3, 0.3, size=(4, 3))).astype(np.float32)
+        v = v.astype(np.float64)
+        off = (0.5, 0.5) if rng.integers(2) else (0.0, 0.0)
+        faces.append((v, off))
+        recs.append(np.concatenate([v.ravel(), off, [0.05]]).astype(np.float32))
+    fin, fout = str(tmp_path / "faces.bin"), str(tmp_path / "pieces.bin")
+    np.concatenate(recs).tofile(fin)
+    subprocess.check_call([checker, "dump", fin, fout])
+    raw = open(fout, "rb").read()
+    pos, compared, triangulated = 0, 0, 0
+    for v, off in faces:
+        n, multi = np.frombuffer(raw, np.int32, 2, pos)
+        pos += 16
+        p32 = np.frombuffer(raw, np.float32, 4 * n, pos).reshape(n, 4).astype(np.float64)
+        pos += 16 * n
+        if multi:
+            continue
+        p64, st = O.split_face(v, 1.0, off, 0.05, 1024)
+        assert st == 0
+        p64 = p64[p64[:, 4] != 0.0]
+        assert abs(p32[:, 3].sum() - p64[:, 4].sum()) < 2e-5
+        assert abs((p32[:, 1] * p32[:, 3]).sum() - (p64[:, 1] * p64[:, 4]).sum()) < 2e-5
+        compared += 1
+        triangulated += len(p64) > 8
+    assert pos == len(raw)
+    assert compared > 1400 and triangulated > 1000
+
+
 def test_status_words_of_the_clipper(checker):
     """The status bits that replace the reference's exit(0) in the face clipper
     (facecutter.h:191-204) and its fixed-size arrays (facecutter.h:29), on the host:
