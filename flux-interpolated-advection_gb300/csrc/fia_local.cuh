@@ -188,8 +188,20 @@ __device__ int weno6_ycolumn(const L& load, const NodeField& F, const int* anc, 
         const int i0 = clampi(bx - 2 + ix, F.Mx - 1), i1 = clampi(bx - 1 + ix, F.Mx - 1);
         float* z0 = zs + 7 * ix * STRIDE;
         float* z1 = z0 + 7 * STRIDE;
+        // two rows per iteration: two independent pairs of evaluations in flight
+        int r = 0;
 #pragma unroll 1
-        for (int r = 0; r < nr; ++r) {
+        for (; r + 1 < nr; r += 2) {
+            const int ja = clampi(by0 - 2 + r, F.My - 1), jb = clampi(by0 - 1 + r, F.My - 1);
+            float fa0[6], fa1[6], fb0[6], fb1[6];
+            load_rows(load, F.Mz * (F.My * i0 + ja), F.Mz * (F.My * i1 + ja), zin, bz, kk, fa0, fa1);
+            load_rows(load, F.Mz * (F.My * i0 + jb), F.Mz * (F.My * i1 + jb), zin, bz, kk, fb0, fb1);
+            const float2 va = weno6_pair(fa0, fa1, cz);
+            const float2 vb = weno6_pair(fb0, fb1, cz);
+            z0[r * STRIDE] = va.x; z1[r * STRIDE] = va.y;
+            z0[(r + 1) * STRIDE] = vb.x; z1[(r + 1) * STRIDE] = vb.y;
+        }
+        if (r < nr) {
             const int jj = clampi(by0 - 2 + r, F.My - 1);
             const int row0 = F.Mz * (F.My * i0 + jj), row1 = F.Mz * (F.My * i1 + jj);
             float f0[6], f1[6];
