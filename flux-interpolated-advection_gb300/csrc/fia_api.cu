@@ -70,6 +70,7 @@ struct fia_session {
 namespace {
 
 thread_local std::string g_last_error;
+thread_local std::string g_last_unsupported;   // why the last FIA_ERR_UNSUPPORTED of this thread
 
 int set_cuda_error(cudaError_t e, const char* where) {
     g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
@@ -195,6 +196,20 @@ int check_params(const fia_advect_params* p) {
     const int k = p->num_gauss_quadrature_point_for_integrate_density;
     if (k < 1 || k > kMaxGauss || (k % 2) == 0) return FIA_ERR_INVALID;
     if (!(p->minimal_area > 0.0)) return FIA_ERR_INVALID;
+    return FIA_OK;
+}
+
+// The chosen form does not triangulate pieces (minimal_area < 1; a piece's xi-eta area is at
+// most 1, so minimal_area >= 1, the reference's default, never triangulates).  The bisection
+// of the longest edge jumps where two edges are equally long, and FP32 vertex positions,
+// through crossing points on edges almost parallel to an iso-line, put a face on the other
+// side of such a tie often enough to move a pass by 1-6% against the oracle; the plain form
+// matches it.
+int check_form(const fia_session* s, double minimal_area) {
+    if (s->precision == FIA_FP32C && minimal_area < 1.0) {
+        g_last_unsupported = "minimal_area < 1 (triangulated pieces) is supported by the FP64 form only";
+        return FIA_ERR_UNSUPPORTED;
+    }
     return FIA_OK;
 }
 
@@ -563,7 +578,10 @@ int pressure(fia_session* s, const fia_solver_params* sp, fia_solver_report* rep
     int extra = 0, fcg_its = 0;
     double pms = 0.0;
     if (sp->method == FIA_SOLVER_FCG_LEARNED) {
-        if (s->precision != FIA_FP32C) return FIA_ERR_UNSUPPORTED;
+        if (s->precision != FIA_FP32C) {
+            g_last_unsupported = "the learned preconditioner needs an FP32C session";
+            return FIA_ERR_UNSUPPORTED;
+        }
         if (!s->net) return FIA_ERR_INVALID;
         if (sp->fallback_iter < 1) return FIA_ERR_INVALID;
         const int rc = pressure_fcg(s, sp, r, fcg_its, pms);
@@ -878,7 +896,8 @@ void fia_default_step_params(fia_step_params* p) {
 
 int fia_step(fia_session* s, const fia_step_params* p, fia_step_report* rep) {
     if (!s || !p || !(p->cfl > 0.0) || !(p->max_dt > 0.0)) return FIA_ERR_INVALID;
-    const int c = check_params(&p->advect);
+    int c = check_params(&p->advect);
+    if (c == FIA_OK) c = check_form(s, p->advect.minimal_area);
     if (c != FIA_OK) return c;
     return s->precision == FIA_FP64 ? step<double>(s, p, rep) : step<float>(s, p, rep);
 }
@@ -896,7 +915,7 @@ const char* fia_error_string(int code) {
         case FIA_OK: return "ok";
         case FIA_ERR_INVALID: return "invalid argument";
         case FIA_ERR_CUDA: return g_last_error.empty() ? "CUDA error" : g_last_error.c_str();
-        case FIA_ERR_UNSUPPORTED: return "unsupported option";
+        case FIA_ERR_UNSUPPORTED: return g_last_unsupported.empty() ? "unsupported option" : g_last_unsupported.c_str();
         case FIA_ERR_NOMEM: return "device allocation failed";
         default: return code > 0 ? "completed with numerical status bits set" : "unknown error";
     }
@@ -1083,14 +1102,16 @@ int fia_field_device_ptr(fia_session* s, int field, void** dev_ptr) {
 
 int fia_move_substances_3D(fia_session* s, double dt, const fia_advect_params* p) {
     if (!s || !(dt >= 0.0)) return FIA_ERR_INVALID;
-    const int c = check_params(p);
+    int c = check_params(p);
+    if (c == FIA_OK) c = check_form(s, p->minimal_area);
     if (c != FIA_OK) return c;
     return s->precision == FIA_FP64 ? move_substances<double>(s, dt, p) : move_substances<float>(s, dt, p);
 }
 
 int fia_advect_velocity_xyz(fia_session* s, double dt, const fia_advect_params* p) {
     if (!s || !(dt >= 0.0)) return FIA_ERR_INVALID;
-    const int c = check_params(p);
+    int c = check_params(p);
+    if (c == FIA_OK) c = check_form(s, p->minimal_area);
     if (c != FIA_OK) return c;
     return s->precision == FIA_FP64 ? advect_velocity<double>(s, dt, p) : advect_velocity<float>(s, dt, p);
 }
@@ -1244,8 +1265,10 @@ int fia_debug_flux_pass(fia_session* s, int comp, const double* field, double dt
                         int use_integral, int zero_velocity, const double* co, int k, double minimal_area,
                         double* out) {
     if (!s || !field || !out || !co || comp < -1 || comp > 2 || k < 1 || k > kMaxGauss || interp < 0 || interp > 2 ||
-        psi_mode < 0 || psi_mode > 2)
+        psi_mode < 0 || psi_mode > 2 || !(minimal_area > 0.0))
         return FIA_ERR_INVALID;
+    const int c = check_form(s, minimal_area);
+    if (c != FIA_OK) return c;
     if (s->precision == FIA_FP64)
         return debug_flux_pass<double>(s, comp, field, dt, interp, psi_mode, use_integral, zero_velocity, co, k,
                                        minimal_area, out);
@@ -1328,7 +1351,10 @@ int fia_get_solid_mask(fia_session* s, unsigned char* out) {
 
 // ------------------------------- learned preconditioner ---------------------------
 static int ensure_net(fia_session* s) {
-    if (s->precision != FIA_FP32C) return FIA_ERR_UNSUPPORTED;
+    if (s->precision != FIA_FP32C) {
+        g_last_unsupported = "the learned preconditioner needs an FP32C session";
+        return FIA_ERR_UNSUPPORTED;
+    }
     if (!s->net) {
         s->net = unet::net_create(s->N[0], s->N[1], s->N[2], s->stream);
         if (!s->net) { g_last_error = "fia_learned: device allocation failed"; return FIA_ERR_NOMEM; }

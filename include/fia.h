@@ -91,7 +91,9 @@ typedef struct fia_advect_params {
                                                                (move_substances_3d.cpp:243-493); both
                                                                forms (FIA_ERR_UNSUPPORTED in the
                                                                allocation-free entry point) */
-    double minimal_area;                                    /* xi-eta triangulation threshold (main.cpp:82) */
+    double minimal_area;                                    /* xi-eta triangulation threshold (main.cpp:82);
+                                                               below 1 (triangulated pieces) the FP64 form
+                                                               only: FIA_ERR_UNSUPPORTED in FP32C */
 } fia_advect_params;
 
 typedef struct fia_solver_params {
