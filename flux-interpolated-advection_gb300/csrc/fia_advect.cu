@@ -1042,11 +1042,18 @@ static cudaError_t face_stage64(const PassDesc& d, const double* a, const PassWo
     return cudaGetLastError();
 }
 
+// The piece pipeline where its face tags (family << 29 | index) hold every face; one thread
+// per face otherwise (grids beyond about 800^3) and where the session has no piece store.
 template <typename T>
 static cudaError_t faces_weighted(const PassDesc& d, const T* a, const PassWork<T>& w, const T* verts, T wgt, int acc,
                                   cudaStream_t s) {
     if constexpr (sizeof(T) == sizeof(double)) {
-        if (w.pieces64) return face_stage64(d, a, w, verts, wgt, acc, s);
+        long long big = 0;
+        for (int fam = 0; fam < 3; ++fam) {
+            const long long nf = (long long)(d.A.Mx + (fam == 0)) * (d.A.My + (fam == 1)) * (d.A.Mz + (fam == 2));
+            big = nf > big ? nf : big;
+        }
+        if (w.pieces64 && big < (1LL << 29)) return face_stage64(d, a, w, verts, wgt, acc, s);
     }
     return launch_faces_from<T>(d, a, w, verts, wgt, acc, s);
 }
